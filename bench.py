@@ -1,0 +1,344 @@
+"""Benchmark of the GB300 SunlightLB update step.
+
+Workload (the packed-bed permeability case): periodic 128^3 lattice, seeded
+random sequential addition of non-overlapping spheres with radius uniform in
+[4, 8] up to lattice solid fraction 0.30, fixed objects with link
+bounce-back, body force 1e-6 along x, tau = 1 (viscosity 1/6), Stokes flow,
+FP32 populations.  A step is one lattice Boltzmann update (bounce-back,
+streaming and collision of every node) of the whole lattice.
+
+Metric: million lattice updates per second (all nodes, fluid and solid, as
+the reference's own fwrstats counts them, src/lbmisc.c:264-274).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+Under torchrun each rank advances its own replica of the lattice (the single
+lattice is not split across GPUs); value is the sum over ranks of the nodes
+updated divided by the slowest rank's time.
+
+The JSON line carries:
+  value      device-resident throughput, CUDA events around each step on the
+             lattice's stream, L2 flushed (256 MiB write) between steps;
+  e2e        the same metric through the public C API with host buffers:
+             populations, geometry and body force uploaded from the host, the
+             steps run as check intervals (98 lbstep + measure, which reads
+             the mean flow and the drag back), populations read back at the end;
+  roofline   achieved HBM GB/s of the fused step kernel against the measured
+             copy bandwidth (120 algorithmic bytes per FP32 node update);
+  cpu_baseline  the CPU oracle (a restatement of the reference's C code) on
+             one host core, on a time-bounded sample of steps.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SIDE = 128
+PHI = 0.30
+RMIN, RMAX = 4.0, 8.0
+FORCE = 1e-6
+TAU = 1.0
+SEED = 1
+BYTES_PER_UPDATE = {0: 240, 1: 120}  # 2 * 15 populations * bytes per population
+CHECK = 100                           # check interval of the e2e run (98 steps + measure)
+
+
+def config(prec_name, l2):
+    return {"workload": f"packed-bed permeability, periodic {N_SIDE}^3, RSA spheres r~U[{RMIN:g},{RMAX:g}] "
+                        f"to solid fraction {PHI}, body force {FORCE:g} along x, tau {TAU:g}, Stokes",
+            "lattice": [N_SIDE, N_SIDE, N_SIDE], "populations": prec_name, "seed": SEED,
+            "velocity_set": "D3Q15", "l2": l2, "parallelism": "replicas"}
+
+
+def dist_env():
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.samples.append([c.strip() for c in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(prec_name):
+    """DRAM bytes per launch of the fused step from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "lb_step_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(prec_name)
+    except Exception:
+        return None
+
+
+def build_lattice(L, precision, spheres, solid):
+    from sunlightlb_gb300 import workloads as W
+    lb, _, _ = W.packed_bed(L, n=N_SIDE, phi=PHI, rmin=RMIN, rmax=RMAX, seed=SEED, force=FORCE, tau=TAU,
+                            precision=precision, spheres=spheres)
+    return lb
+
+
+def run_mine(args):
+    import torch
+    import sunlightlb_gb300
+    from sunlightlb_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = sunlightlb_gb300.library()
+    precision = 1 if args.precision == "fp32" else 0
+    prec_name = "fp32" if precision == 1 else "fp64"
+    spheres, solid = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
+    lb = build_lattice(L, precision, spheres, solid)
+    nodes = lb.nnodes
+
+    # -------- device-resident throughput: one step per timed iteration --------
+    L.lbsteps(lb, 2)  # first device call uploads the lattice
+    stream = torch.cuda.ExternalStream(L.lbgetstream(lb))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        L.lbstep(lb)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    k0 = L.lbkernelcount()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[s].record(stream)
+            L.lbstep(lb)
+            ends[s].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = L.lbkernelcount() - k0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    ms_per_step = total_ms / args.steps
+    value = world * nodes / (ms_per_step * 1e-3) / 1e6
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_UPDATE[precision] * nodes / (ms_per_step * 1e-3) / 1e9
+
+    # -------- end-to-end through the public API with host buffers -------------
+    e2e = run_e2e(L, precision, spheres, solid, args)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": "MLUPS (million lattice updates per second, all nodes), fused FP32 step",
+        "value": round(value, 1),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic seeded RSA sphere packing (the reference publishes no benchmark data set)",
+        "config": config(prec_name, "flushed between timed steps (256 MiB write)"),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "traffic": profile_traffic(prec_name),
+                     "bytes_per_update": BYTES_PER_UPDATE[precision], "kernel": "k_step (fused AA update)"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "wall_s_timed": round(wall, 4),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(spheres, solid, budget_s=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def run_e2e(L, precision, spheres, solid, args):
+    """MLUPS of check intervals run through the public API, host buffers:
+    a fresh lattice whose populations come from the host (lbpush uploads
+    them with the geometry and body force), intervals of 98 lbstep + measure
+    (mean flow and drag read back each interval), populations read back."""
+    import numpy as np
+    import torch
+    lb = build_lattice(L, precision, spheres, solid)
+    n = lb.nnodes
+    intervals = max(1, args.e2e_intervals)
+    a_host = lb.array("a") if lb.a else None
+    lb_a = L.lbpull(lb)  # allocates the host mirror (zero populations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L.lbpush(lb)
+    h2d = 15 * 8 * n + 4 * n + 3 * 8 * n  # populations (FP64), object map, body force arrays
+    d2h = 0
+    for _ in range(intervals):
+        L.lbsteps(lb, CHECK - 2)
+        L.measure(lb)
+        _ = (lb.vmeanx, lb.step)
+        d2h += 5 * 8 * 3 + 6 * 8  # three mean-flow sums and the object force/torque
+    pops = lb.pops()
+    d2h += pops.nbytes
+    dt = time.perf_counter() - t0
+    steps = intervals * CHECK
+    return {"value": round(n * steps / dt / 1e6, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps),
+            "steps": steps, "note": "public C API: lbpush, lbsteps + measure per 100 steps, lbpull"}
+
+
+def oracle_lib():
+    from sunlightlb_gb300 import build as b
+    from sunlightlb_gb300.binding import Library
+    path = os.path.join(ROOT, "oracle", "liboracle.so")
+    if not os.path.exists(path):
+        b.build_oracle(with_reference=False)
+    return Library(path, extended=True)
+
+
+def _cpu_worker(spheres, solid, budget_s, out, slot):
+    L = oracle_lib()
+    from sunlightlb_gb300 import workloads as W
+    lb = L.newlb(N_SIDE, N_SIDE, N_SIDE, "null")
+    lb.tau = TAU
+    lb.stokes_flow = 1
+    W.insert_solid(L, lb, solid)
+    L.flattenobj(lb)
+    L.syncobjs(lb)
+    L.addbf(lb, FORCE, 0.0, 0.0)
+    L.lbstep(lb)
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < 2 or time.perf_counter() - t0 < budget_s:
+        L.lbstep(lb)
+        steps += 1
+    out[slot] = (steps, time.perf_counter() - t0, lb.nnodes)
+
+
+def cpu_baseline(spheres, solid, budget_s=10.0, threads=1):
+    """The CPU oracle (restatement of the reference's single-threaded C
+    update, strict FP64) on host cores; one lattice per thread."""
+    out = [None] * threads
+    ts = [threading.Thread(target=_cpu_worker, args=(spheres, solid, budget_s, out, s)) for s in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    total = sum(s * n for s, _, n in out) / max(dt for _, dt, _ in out) / 1e6
+    steps = [s for s, _, _ in out]
+    return {"value": round(total, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{min(steps)}-{max(steps)} FP64 update steps per thread of the same {N_SIDE}^3 packing "
+                      f"({threads} lattice(s), about {budget_s:g} s of CPU time each)"}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle port of its
+    C code; the reference itself is not built on the GPU machine) on every host
+    core: one lattice per thread, aggregate MLUPS per step."""
+    from sunlightlb_gb300 import workloads as W
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    spheres, solid = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
+    budget = max(5.0, min(60.0, args.cpu_seconds * 2))
+    cb = cpu_baseline(spheres, solid, budget_s=budget, threads=threads)
+    line = {
+        "impl": "reference",
+        "metric": "MLUPS (million lattice updates per second, all nodes), fused FP32 step",
+        "value": cb["value"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic seeded RSA sphere packing",
+        "config": config("fp64 (CPU reference code)", "n/a (CPU)"),
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--e2e-intervals", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mine(args)
+
+
+if __name__ == "__main__":
+    main()

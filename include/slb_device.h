@@ -1,0 +1,166 @@
+/*
+ * slb_device.h -- C ABI of the GB300 device layer of SunlightLB.
+ *
+ * Plain C types only (pointers, sizes, doubles): this is the thin layer the
+ * host C implementation of sunlightlb.h calls to run the update path on one
+ * GPU.  Every function returns 0 on success and a non-zero status on error;
+ * slbc_last_error() then describes the failure.  The host layer maps a
+ * failure to the reference's fatal-error convention (error() -> exit,
+ * reference src/lbmisc.c:39-42).
+ *
+ * Device state of one lattice (an slbc_lattice):
+ *   - populations, structure of arrays: pop[q*npad + inode], in FP64, FP32
+ *     or BF16 (precision fixed at creation), stored in one of three layouts:
+ *       N  : pop[q][x] = a[x][q], the reference's post-phase array;
+ *       C0 : post-collision, pop[opp q][x] = a[x][q] (after an even step);
+ *       C1 : post-collision, streamed: a[x][q] lives at pop[q][x + c_q], or at
+ *            pop[opp q][x] when the link x -> x + c_q is a boundary link
+ *            (after an odd step);
+ *     the in-place AA update alternates C0 -> C1 -> C0;
+ *   - a per-node flag word (solid bit + 14 boundary-link bits);
+ *   - the list of solid boundary nodes, sorted by object then node, with
+ *     FP64 node forces accumulated during measurement;
+ *   - body force (uniform constant or per node) and wall velocities.
+ *
+ * Node index inode = esk*(esj*i + j) + k; populations q follow the D3Q15
+ * link table of reference src/lbmisc.c:87-104.
+ */
+
+#ifndef SLB_DEVICE_H_INC
+#define SLB_DEVICE_H_INC
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct slbc_lattice slbc_lattice;
+
+/* Run-time scalars of a lattice (fields of LBSys, reference
+ * src/sunlightlb.h:81-83) */
+typedef struct slbc_params {
+  double tau, rho0;
+  int stokes_flow, skip_solid, objects_moving;
+} slbc_params;
+
+/* Status (reference src/sunlightlb.h:47-49) matching a device layout */
+#define SLBC_LAYOUT_N  0
+#define SLBC_LAYOUT_C0 1
+#define SLBC_LAYOUT_C1 2
+
+const char *slbc_last_error(void);
+/* Number of kernel launches made by this library since load. */
+long slbc_launch_count(void);
+/* Number of CUDA devices visible (0 when none). */
+int slbc_device_count(void);
+
+/* Create the device state of an esi*esj*esk lattice with populations in
+ * `precision` (0 FP64, 1 FP32, 2 BF16), all populations zero (layout N).
+ * Replaces the device side of newlb, reference src/lbmisc.c:81-152. */
+int slbc_create(slbc_lattice **out, int esi, int esj, int esk, int precision);
+void slbc_destroy(slbc_lattice *h);
+int slbc_set_stream(slbc_lattice *h, void *stream);
+void *slbc_get_stream(slbc_lattice *h);
+int slbc_synchronize(slbc_lattice *h);
+
+/* Geometry: objidx[nnodes] = dense object index of the node (-1 = fluid);
+ * bnd_node[nbnd] / bnd_obj[nbnd] = solid nodes with at least one fluid
+ * neighbour, sorted by (object, node).  Builds the flag words on the GPU.
+ * Replaces the device side of makemask/syncobjs, reference
+ * src/lbobjs.c:526-560, 660-663. */
+int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj,
+                      const long *bnd_node, const int *bnd_obj, long nbnd);
+/* Adsorption bits (0x4000 of the reference mask) of every node, 1 byte per
+ * node (reference src/mpads.c:28-44). */
+int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads);
+int slbc_set_params(slbc_lattice *h, const slbc_params *p);
+/* Body force per node (NULL = zero); a force uniform over the fluid nodes is
+ * detected and kept as a kernel constant (reference src/lbobjs.c:593-619). */
+int slbc_set_bodyforce(slbc_lattice *h, const double *bx, const double *by, const double *bz);
+/* Wall velocities per node, already scaled by rho0/12 as vspread/vset store
+ * them (reference src/lbobjs.c:565-643); NULL releases them. */
+int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const double *uz);
+
+/* Populations in the reference AoS order a[15*inode + q] (FP64). put sets
+ * layout N; get reads from any layout. */
+int slbc_put_pops(slbc_lattice *h, const double *a);
+int slbc_get_pops(slbc_lattice *h, double *a);
+int slbc_layout(slbc_lattice *h);
+
+/* Fused update steps from a post-collision state (replaces lbstep,
+ * reference src/lbkernel.c:49-51): n in-place AA steps.  use_graph replays
+ * the steps from a captured CUDA graph. */
+int slbc_step(slbc_lattice *h, int n, int use_graph);
+/* Node-force accumulation of one bblforce (reference src/lbkernel.c:179-321
+ * and 464-618) on the post-collision state, followed by one fused step. */
+int slbc_force_step(slbc_lattice *h);
+/* Separate phases on layout N (reference src/lbkernel.c:35-45, 623-762,
+ * 769-877).  Any other layout is converted first. */
+int slbc_bbl(slbc_lattice *h, int with_force);
+int slbc_propagate(slbc_lattice *h);
+int slbc_collide(slbc_lattice *h);
+
+/* Node forces of the solid boundary nodes (reference src/lbmeasure.c:208-231) */
+int slbc_zero_force(slbc_lattice *h);
+int slbc_scale_force(slbc_lattice *h, double fac);
+/* Node forces of the boundary list, 3 per entry (x, y, z). */
+int slbc_get_force(slbc_lattice *h, double *f3);
+
+/* Sums of accvmean over fluid nodes (reference src/lbmeasure.c:58-106):
+ * out[0..2] = sum w*u, out[3] = sum w, out[4] = number of fluid nodes, with
+ * u the velocity corrected by fac*b and w = psi^2 (psi NULL: w = 1). */
+int slbc_vsum(slbc_lattice *h, double fac, const double *psi, double out[5]);
+/* Object force and torque (reference src/lbmeasure.c:236-263):
+ * pos[3*nobj] in, ft[6*nobj] out (frc xyz, trq xyz). */
+int slbc_distribf(slbc_lattice *h, const double *pos, double *ft);
+
+/* Warm start: populations rebuilt from (rho, u) with the lbloadvel formula
+ * (reference src/lbstore.c:340-401), leaving layout N at POST_PROPAGATE.
+ * rho may be NULL (rho = rho0). */
+int slbc_set_velocity(slbc_lattice *h, const double *rho, const double *ux,
+                      const double *uy, const double *uz, int skip_solid);
+
+/* Moment propagation (reference src/mpkernel.c:33-368, src/mpmisc.c:38-246).
+ * A tracer holds the scalar p of one MPSys; the density snapshot rho is per
+ * lattice (the reference keeps one lb->rho shared by all its MPSys). */
+typedef struct slbc_tracer slbc_tracer;
+/* New tracer, p = 0, in FP64 (use_f64 = 1) or FP32 (reference
+ * src/mpmisc.c:38-59). */
+int slbc_mp_create(slbc_lattice *h, slbc_tracer **out, int use_f64);
+void slbc_mp_destroy(slbc_tracer *t);
+/* Density snapshot rho = rho0 + sum_q a_q on fluid nodes, rho0 on solid
+ * nodes (reference src/mpmisc.c:64-79). */
+int slbc_mp_rhoinit(slbc_lattice *h);
+int slbc_mp_get_rho(slbc_lattice *h, double *rho);
+int slbc_mp_put(slbc_tracer *t, const double *p);
+int slbc_mp_get(slbc_tracer *t, double *p);
+/* n tracer updates (reference src/mpkernel.c:47-368) with diffusion
+ * parameter alpha and adsorption probability adprob (1 = the reference's
+ * all-or-nothing adsorption).  moving: objstate holds 9 doubles per object
+ * (pos xyz, vel xyz, ang xyz) for the moving-wall terms. */
+int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
+                 const double *objstate, int nobj);
+/* out[0] = sum p on fluid nodes, out[1] = sum p on solid nodes, out[2] = sum
+ * p on adsorbing nodes, out[3] = sum p*pos, out[4] = sum p*pos^2 on fluid
+ * nodes along axis (0,1,2; -1 none): reference src/mpmisc.c:121-158,466-499,
+ * src/mpads.c:149-172. */
+int slbc_mp_sums(slbc_tracer *t, int axis, double out[5]);
+/* Extremes of p over fluid nodes (reference src/mpmisc.c:164-208). */
+int slbc_mp_minmax(slbc_tracer *t, double out[2]);
+/* Set p = value on the fluid nodes of a region (reference src/mpobjs.c):
+ * kind 0 all; 1 slab, geo = x1,x2,y1,y2,z1,z2; 2 wall, geo = axis, pos;
+ * 3 sphere, geo = rad, ox, oy, oz; 4 cylinder, geo = axis, hole, rad, a, b. */
+int slbc_mp_fill(slbc_tracer *t, int kind, const double *geo, double value);
+/* p *= fac on fluid nodes (reference src/mpmisc.c:214-225). */
+int slbc_mp_scale(slbc_tracer *t, double fac);
+/* p = 0 on adsorbing nodes (reference src/mpads.c:177-186). */
+int slbc_mp_zero_ads(slbc_tracer *t);
+/* dst p += src p on fluid nodes (reference src/mpmisc.c:233-246). */
+int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLB_DEVICE_H_INC */

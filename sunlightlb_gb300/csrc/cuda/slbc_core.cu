@@ -1,0 +1,880 @@
+// extern "C" device layer of GB300 SunlightLB (declared in slb_device.h):
+// lattice state, geometry, host transfers, layout conversions, dispatch to
+// the per-precision kernels, reductions, CUDA-graph replay and tracers.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <atomic>
+#include <algorithm>
+
+#include "slbc_internal.cuh"
+#include "slbc_kernels.cuh"
+
+using namespace slbc;
+
+struct slbc_lattice {
+  Lattice L;
+  std::vector<unsigned char> solid_host;  // solidity per node, for body-force checks
+};
+
+struct slbc_tracer {
+  slbc_lattice *h = nullptr;
+  int f64 = 1;
+  void *p = nullptr, *p2 = nullptr;
+  double *objstate = nullptr;
+  int objstate_cap = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<long> g_launches{0};
+
+int fail(const char *what, cudaError_t e) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return (int)e ? (int)e : 1;
+}
+int fail_msg(const std::string &m) {
+  g_err = m;
+  return 1;
+}
+
+#define CK(call)                                 \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) return fail(#call, e_); \
+  } while (0)
+
+size_t elem_size(int precision) { return precision == 0 ? 8 : precision == 1 ? 4 : 2; }
+
+// kernels that do not depend on the population type -------------------------
+
+// Flag words from the object map: solid bit, and bit q when x - c_q differs
+// in solidity from x.
+__global__ void k_flags(const int *objidx, uint16_t *flags, int esi, int esj, int esk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, i = blockIdx.z;
+  if (k >= esk) return;
+  const int im = i == 0 ? esi - 1 : i - 1, ip = i == esi - 1 ? 0 : i + 1;
+  const int jm = j == 0 ? esj - 1 : j - 1, jp = j == esj - 1 ? 0 : j + 1;
+  const int km = k == 0 ? esk - 1 : k - 1, kp = k == esk - 1 ? 0 : k + 1;
+  const int I[3] = {im, i, ip}, J[3] = {jm, j, jp}, K[3] = {km, k, kp};
+  const int x = (i * esj + j) * esk + k;
+  const bool solid = objidx[x] >= 0;
+  uint16_t f = solid ? FLAG_SOLID : 0;
+#pragma unroll
+  for (int q = 1; q < 15; q++) {
+    const int y = (I[1 - CX(q)] * esj + J[1 - CY(q)]) * esk + K[1 - CZ(q)];
+    if ((objidx[y] >= 0) != solid) f |= (uint16_t)(1u << q);
+  }
+  flags[x] = f;
+}
+
+__global__ void k_final_sum(const double *partials, int n, int nv, double *out) {
+  // one thread per component, fixed order: deterministic
+  const int c = threadIdx.x;
+  if (c >= nv) return;
+  double s = 0.0;
+  for (int b = 0; b < n; b++) s += partials[nv * b + c];
+  out[c] = s;
+}
+
+__global__ void k_scale(double *v, long long n, double fac) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) v[e] *= fac;
+}
+
+// distribf, level 1: one block per work piece (object o, entries lo..hi).
+__global__ void k_distrib_piece(const int *bnd_node, const double *f, long long nbnd,
+                                const int *piece_obj, const int *piece_lo, const int *piece_hi,
+                                const double *pos, int esj, int esk, double *piece_sum) {
+  const int pc = blockIdx.x;
+  const int o = piece_obj[pc];
+  const double px = pos[3 * o], py = pos[3 * o + 1], pz = pos[3 * o + 2];
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int e = piece_lo[pc] + threadIdx.x; e < piece_hi[pc]; e += blockDim.x) {
+    const int x = bnd_node[e];
+    const int k = x % esk, r = x / esk, j = r % esj, i = r / esj;
+    const double rx = i - px, ry = j - py, rz = k - pz;
+    const double fx = f[e], fy = f[nbnd + e], fz = f[2 * nbnd + e];
+    v[0] += fx; v[1] += fy; v[2] += fz;
+    v[3] += ry * fz - rz * fy;
+    v[4] += rz * fx - rx * fz;
+    v[5] += rx * fy - ry * fx;
+  }
+  block_sum<6>(v);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 6; c++) piece_sum[6 * pc + c] = v[c];
+}
+
+// distribf, level 2: per object, its pieces in order.
+__global__ void k_distrib_obj(const int *obj_first_piece, const int *obj_npiece,
+                              const double *piece_sum, int nobj, double *ft) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nobj) return;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int pc = obj_first_piece[o]; pc < obj_first_piece[o] + obj_npiece[o]; pc++)
+    for (int c = 0; c < 6; c++) v[c] += piece_sum[6 * pc + c];
+  for (int c = 0; c < 6; c++) ft[6 * o + c] = v[c];
+}
+
+// tracer sums: fluid, solid, adsorbing, first and second moment along axis
+template <typename TP>
+__global__ void __launch_bounds__(kReduceThreads)
+k_mp_sums(const TP *p, const uint16_t *flags, const unsigned char *ads, long long n, int esj,
+          int esk, int axis, double *partials) {
+  double v[5] = {0, 0, 0, 0, 0};
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n;
+       x += (long long)gridDim.x * blockDim.x) {
+    const double pv = (double)p[x];
+    const bool solid = flags[x] & FLAG_SOLID;
+    if (solid) v[1] += pv; else v[0] += pv;
+    if (ads && ads[x]) v[2] += pv;
+    if (!solid && axis >= 0) {
+      const int k = (int)(x % esk), r = (int)(x / esk), j = r % esj, i = r / esj;
+      const double pos = axis == 0 ? i : axis == 1 ? j : k;
+      v[3] += pv * pos;
+      v[4] += pv * pos * pos;
+    }
+  }
+  block_sum<5>(v);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 5; c++) partials[5 * blockIdx.x + c] = v[c];
+}
+
+template <typename TP>
+__global__ void k_mp_minmax(const TP *p, const uint16_t *flags, long long n, double *partials) {
+  double lo = 1e300, hi = -1e300;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n;
+       x += (long long)gridDim.x * blockDim.x) {
+    if (flags[x] & FLAG_SOLID) continue;
+    const double pv = (double)p[x];
+    lo = pv < lo ? pv : lo;
+    hi = pv > hi ? pv : hi;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_down_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_down_sync(0xffffffffu, hi, o));
+  }
+  __shared__ double sl[32], sh[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sl[warp] = lo; sh[warp] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) { lo = fmin(lo, sl[w]); hi = fmax(hi, sh[w]); }
+    partials[2 * blockIdx.x] = lo;
+    partials[2 * blockIdx.x + 1] = hi;
+  }
+}
+
+// tracer injection on fluid nodes of a region (reference src/mpobjs.c)
+template <typename TP>
+__global__ void k_mp_fill(TP *p, const uint16_t *flags, int esi, int esj, int esk, int kind,
+                          double g0, double g1, double g2, double g3, double g4, double g5,
+                          double value) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= (long long)esi * esj * esk) return;
+  if (flags[x] & FLAG_SOLID) return;
+  const int k = (int)(x % esk), r = (int)(x / esk), j = r % esj, i = r / esj;
+  bool in = false;
+  switch (kind) {
+    case 0: in = true; break;
+    case 1: in = i > g0 && i < g1 && j > g2 && j < g3 && k > g4 && k < g5; break;
+    case 2: { const int c = (int)g0 == 0 ? i : (int)g0 == 1 ? j : k; in = c == (int)g1; } break;
+    case 3: {
+      const double rsq = (i - g1) * (i - g1) + (j - g2) * (j - g2) + (k - g3) * (k - g3);
+      in = rsq < g0 * g0;
+    } break;
+    case 4: {
+      const int ax = (int)g0;
+      const double u = ax == 0 ? j : i, v = ax == 2 ? j : k;
+      const double rsq = (u - g3) * (u - g3) + (v - g4) * (v - g4);
+      in = rsq < g2 * g2;
+      if (g1 != 0.0) in = !in;
+    } break;
+  }
+  if (in) p[x] = (TP)value;
+}
+
+template <typename TP>
+__global__ void k_mp_misc(TP *p, const TP *src, const uint16_t *flags, const unsigned char *ads,
+                          long long n, int op, double fac) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  const bool solid = flags[x] & FLAG_SOLID;
+  if (op == 0) { if (!solid) p[x] = p[x] * (TP)fac; }           // rescale
+  else if (op == 1) { if (ads && ads[x]) p[x] = TP(0); }       // adzero
+  else if (op == 2) { if (!solid) p[x] = p[x] + src[x]; }      // add
+}
+
+template <typename TD, typename TS>
+__global__ void k_convert(TD *dst, const TS *src, long long n) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) dst[e] = (TD)src[e];
+}
+
+int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+// per-precision dispatch ------------------------------------------------------
+#define DISPATCH(L, name, ...)                                               \
+  ((L).precision == 0 ? name##_f64(__VA_ARGS__) : name##_f32(__VA_ARGS__))
+
+int ensure_staging(Lattice &L, long long nodes, int per_node) {
+  const long long want = std::min<long long>(nodes, 1 << 20);
+  if (L.staging && L.staging_nodes >= want * per_node) return 0;
+  if (L.staging) cudaFree(L.staging);
+  L.staging = nullptr;
+  CK(cudaMalloc(&L.staging, (size_t)want * per_node * sizeof(double)));
+  L.staging_nodes = want * per_node;
+  return 0;
+}
+
+int ensure_scratch(Lattice &L) {
+  if (L.scratch) return 0;
+  CK(cudaMalloc(&L.scratch, 15 * (size_t)L.npad * elem_size(L.precision)));
+  return 0;
+}
+
+int ensure_partials(Lattice &L, int n) {
+  if (L.partials && L.npartials >= n) return 0;
+  if (L.partials) cudaFree(L.partials);
+  L.partials = nullptr;
+  CK(cudaMalloc(&L.partials, (size_t)n * sizeof(double)));
+  L.npartials = n;
+  return 0;
+}
+
+// put the state into a post-collision AA layout (C0 or C1)
+int to_aa(Lattice &L) {
+  if (L.layout == SLBC_LAYOUT_N) {
+    CK(DISPATCH(L, launch_swap, L));
+    L.layout = SLBC_LAYOUT_C0;
+  }
+  return 0;
+}
+
+// put the state into layout N
+int to_natural(Lattice &L) {
+  if (L.layout == SLBC_LAYOUT_C0) {
+    CK(DISPATCH(L, launch_swap, L));
+  } else if (L.layout == SLBC_LAYOUT_C1) {
+    if (ensure_scratch(L)) return 1;
+    CK(DISPATCH(L, launch_to_natural, L));
+    std::swap(L.pop, L.scratch);
+    L.generation++;  // captured graphs hold the old buffer
+  }
+  L.layout = SLBC_LAYOUT_N;
+  return 0;
+}
+
+int one_step(Lattice &L) {
+  const int odd = L.layout == SLBC_LAYOUT_C0;
+  CK(DISPATCH(L, launch_step, L, odd));
+  L.layout = odd ? SLBC_LAYOUT_C1 : SLBC_LAYOUT_C0;
+  return 0;
+}
+
+constexpr int kGraphPairs = 25;  // one graph = 50 steps, starting from C0
+
+int ensure_graph(Lattice &L) {
+  if (L.graph && L.graph_generation == L.generation) return 0;
+  if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
+  const int saved = L.layout;
+  L.layout = SLBC_LAYOUT_C0;
+  int rc = 0;
+  for (int s = 0; s < 2 * kGraphPairs && !rc; s++) rc = one_step(L);
+  L.layout = saved;
+  cudaError_t e = cudaStreamEndCapture(L.stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail("cudaStreamEndCapture", e);
+  // the captured launches were counted at capture time; replays count below
+  g_launches -= 2 * kGraphPairs;
+  e = cudaGraphInstantiate(&L.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail("cudaGraphInstantiate", e);
+  L.graph_steps = 2 * kGraphPairs;
+  L.graph_generation = L.generation;
+  return 0;
+}
+
+}  // namespace
+
+namespace slbc {
+void count_launch(int n) { g_launches += n; }
+int reduction_blocks(const Lattice &L) {
+  long long rows = (long long)L.esi * L.esj;
+  return (int)std::max<long long>(1, std::min<long long>(rows, 152 * 4));
+}
+}  // namespace slbc
+
+// ============================================================================
+extern "C" {
+
+const char *slbc_last_error(void) { return g_err.c_str(); }
+long slbc_launch_count(void) { return g_launches.load(); }
+
+int slbc_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+int slbc_create(slbc_lattice **out, int esi, int esj, int esk, int precision) {
+  *out = nullptr;
+  if (esi < 1 || esj < 1 || esk < 1) return fail_msg("slbc_create: lattice sides must be >= 1");
+  const long long n = (long long)esi * esj * esk;
+  if (n >= (1LL << 31)) return fail_msg("slbc_create: lattice has 2^31 nodes or more");
+  if (precision < 0 || precision > 1)
+    return fail_msg("slbc_create: precision must be 0 (FP64) or 1 (FP32)");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail_msg("slbc_create: no CUDA device is available (the GB300 library has no CPU path)");
+  slbc_lattice *h = new slbc_lattice();
+  Lattice &L = h->L;
+  L.esi = esi; L.esj = esj; L.esk = esk; L.precision = precision;
+  L.nnodes = n;
+  L.npad = (n + 63) / 64 * 64;
+  L.par.tau = 0.75; L.par.rho0 = 72.0;
+  h->solid_host.assign((size_t)n, 0);
+  cudaError_t e = cudaMalloc(&L.pop, 15 * (size_t)L.npad * elem_size(precision));
+  if (e == cudaSuccess) e = cudaMemset(L.pop, 0, 15 * (size_t)L.npad * elem_size(precision));
+  if (e == cudaSuccess) e = cudaMalloc(&L.flags, (size_t)n * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMemset(L.flags, 0, (size_t)n * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMalloc(&L.objidx, (size_t)n * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(L.objidx, 0xff, (size_t)n * sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&L.host_out, 64 * sizeof(double));
+  if (e != cudaSuccess) {
+    slbc_destroy(h);
+    return fail("slbc_create", e);
+  }
+  L.own_stream = true;
+  L.layout = SLBC_LAYOUT_N;
+  *out = h;
+  return 0;
+}
+
+void slbc_destroy(slbc_lattice *h) {
+  if (!h) return;
+  Lattice &L = h->L;
+  if (L.stream) cudaStreamSynchronize(L.stream);
+  void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
+                  L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
+                  L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.ref_mom};
+  for (void *b : bufs) if (b) cudaFree(b);
+  if (L.host_out) cudaFreeHost(L.host_out);
+  if (L.graph) cudaGraphExecDestroy(L.graph);
+  if (L.stream && L.own_stream) cudaStreamDestroy(L.stream);
+  delete h;
+}
+
+int slbc_set_stream(slbc_lattice *h, void *stream) {
+  Lattice &L = h->L;
+  CK(cudaStreamSynchronize(L.stream));
+  if (L.own_stream) cudaStreamDestroy(L.stream);
+  L.stream = (cudaStream_t)stream;
+  L.own_stream = false;
+  L.generation++;
+  return 0;
+}
+
+void *slbc_get_stream(slbc_lattice *h) { return (void *)h->L.stream; }
+
+int slbc_synchronize(slbc_lattice *h) {
+  CK(cudaStreamSynchronize(h->L.stream));
+  return 0;
+}
+
+int slbc_layout(slbc_lattice *h) { return h->L.layout; }
+
+int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *bnd_node,
+                      const int *bnd_obj, long nbnd) {
+  Lattice &L = h->L;
+  const long long n = L.nnodes;
+  for (long long x = 0; x < n; x++) h->solid_host[x] = objidx[x] >= 0;
+  CK(cudaMemcpyAsync(L.objidx, objidx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, L.stream));
+  {
+    const int bx = L.esk >= 128 ? 128 : 32;
+    dim3 grid((L.esk + bx - 1) / bx, L.esj, L.esi);
+    k_flags<<<grid, bx, 0, L.stream>>>(L.objidx, L.flags, L.esi, L.esj, L.esk);
+    count_launch();
+    CK(cudaGetLastError());
+  }
+  // boundary list
+  void *old[] = {L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj, L.piece_lo, L.piece_hi,
+                 L.piece_sum, L.obj_pos, L.obj_ft};
+  CK(cudaStreamSynchronize(L.stream));
+  for (void *b : old) if (b) cudaFree(b);
+  L.bnd_node = L.bnd_obj = nullptr; L.bnd_f = nullptr;
+  L.piece_obj = L.piece_lo = L.piece_hi = nullptr; L.piece_sum = nullptr;
+  L.obj_pos = L.obj_ft = nullptr;
+  L.nbnd = nbnd; L.nobj = nobj; L.npiece = 0;
+  if (nbnd > 0) {
+    std::vector<int> nodes((size_t)nbnd);
+    for (long e = 0; e < nbnd; e++) nodes[e] = (int)bnd_node[e];
+    CK(cudaMalloc(&L.bnd_node, nbnd * sizeof(int)));
+    CK(cudaMalloc(&L.bnd_obj, nbnd * sizeof(int)));
+    CK(cudaMalloc(&L.bnd_f, 3 * nbnd * sizeof(double)));
+    CK(cudaMemcpy(L.bnd_node, nodes.data(), nbnd * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L.bnd_obj, bnd_obj, nbnd * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemset(L.bnd_f, 0, 3 * nbnd * sizeof(double)));
+  }
+  if (nobj > 0) {
+    // distribf pieces: each object's run of the list, split into chunks
+    const int chunk = 4096;
+    std::vector<int> po, plo, phi, first((size_t)nobj, 0), cnt((size_t)nobj, 0);
+    long e = 0;
+    for (int o = 0; o < nobj; o++) {
+      first[o] = (int)po.size();
+      long lo = e;
+      while (e < nbnd && bnd_obj[e] == o) e++;
+      for (long s = lo; s < e; s += chunk) {
+        po.push_back(o); plo.push_back((int)s); phi.push_back((int)std::min<long>(e, s + chunk));
+        cnt[o]++;
+      }
+    }
+    if (e != nbnd) return fail_msg("slbc_set_geometry: boundary list not sorted by object");
+    L.npiece = (int)po.size();
+    CK(cudaMalloc(&L.obj_pos, 3 * nobj * sizeof(double)));
+    CK(cudaMalloc(&L.obj_ft, (6 * nobj + 2 * nobj) * sizeof(double)));
+    // first/count stored after the 6*nobj results, as ints
+    CK(cudaMemcpy((int *)(L.obj_ft + 6 * nobj), first.data(), nobj * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((int *)(L.obj_ft + 6 * nobj) + nobj, cnt.data(), nobj * sizeof(int), cudaMemcpyHostToDevice));
+    if (L.npiece > 0) {
+      CK(cudaMalloc(&L.piece_obj, L.npiece * sizeof(int)));
+      CK(cudaMalloc(&L.piece_lo, L.npiece * sizeof(int)));
+      CK(cudaMalloc(&L.piece_hi, L.npiece * sizeof(int)));
+      CK(cudaMalloc(&L.piece_sum, 6 * (size_t)L.npiece * sizeof(double)));
+      CK(cudaMemcpy(L.piece_obj, po.data(), L.npiece * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(L.piece_lo, plo.data(), L.npiece * sizeof(int), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(L.piece_hi, phi.data(), L.npiece * sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
+  L.generation++;
+  return 0;
+}
+
+int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads) {
+  Lattice &L = h->L;
+  if (!L.ads) CK(cudaMalloc(&L.ads, (size_t)L.nnodes));
+  CK(cudaMemcpyAsync(L.ads, ads, (size_t)L.nnodes, cudaMemcpyHostToDevice, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  return 0;
+}
+
+int slbc_set_params(slbc_lattice *h, const slbc_params *p) {
+  Lattice &L = h->L;
+  if (memcmp(&L.par, p, sizeof(slbc_params)) != 0) {
+    L.par = *p;
+    L.generation++;
+  }
+  return 0;
+}
+
+int slbc_set_bodyforce(slbc_lattice *h, const double *bx, const double *by, const double *bz) {
+  Lattice &L = h->L;
+  const long long n = L.nnodes;
+  bool uniform = true, found = false;
+  double c[3] = {0.0, 0.0, 0.0};
+  if (bx && by && bz) {
+    for (long long x = 0; x < n && uniform; x++) {
+      if (h->solid_host[x]) continue;
+      if (!found) { c[0] = bx[x]; c[1] = by[x]; c[2] = bz[x]; found = true; }
+      else if (bx[x] != c[0] || by[x] != c[1] || bz[x] != c[2]) uniform = false;
+    }
+  }
+  if (L.bf) { cudaStreamSynchronize(L.stream); cudaFree(L.bf); L.bf = nullptr; }
+  L.bf_uniform = uniform ? 1 : 0;
+  L.bf_const[0] = c[0]; L.bf_const[1] = c[1]; L.bf_const[2] = c[2];
+  if (!uniform) {
+    const size_t es = elem_size(L.precision);
+    CK(cudaMalloc(&L.bf, 3 * (size_t)L.npad * es));
+    std::vector<char> buf((size_t)n * es);
+    const double *src[3] = {bx, by, bz};
+    for (int c3 = 0; c3 < 3; c3++) {
+      for (long long x = 0; x < n; x++) {
+        if (L.precision == 0) ((double *)buf.data())[x] = src[c3][x];
+        else ((float *)buf.data())[x] = (float)src[c3][x];
+      }
+      CK(cudaMemcpy((char *)L.bf + c3 * (size_t)L.npad * es, buf.data(), (size_t)n * es,
+                    cudaMemcpyHostToDevice));
+    }
+  }
+  L.generation++;
+  return 0;
+}
+
+int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const double *uz) {
+  Lattice &L = h->L;
+  if (L.uw) { cudaStreamSynchronize(L.stream); cudaFree(L.uw); L.uw = nullptr; }
+  if (ux && uy && uz) {
+    const long long n = L.nnodes;
+    const size_t es = elem_size(L.precision);
+    CK(cudaMalloc(&L.uw, 3 * (size_t)L.npad * es));
+    std::vector<char> buf((size_t)n * es);
+    const double *src[3] = {ux, uy, uz};
+    for (int c3 = 0; c3 < 3; c3++) {
+      for (long long x = 0; x < n; x++) {
+        if (L.precision == 0) ((double *)buf.data())[x] = src[c3][x];
+        else ((float *)buf.data())[x] = (float)src[c3][x];
+      }
+      CK(cudaMemcpy((char *)L.uw + c3 * (size_t)L.npad * es, buf.data(), (size_t)n * es,
+                    cudaMemcpyHostToDevice));
+    }
+  }
+  L.generation++;
+  return 0;
+}
+
+int slbc_put_pops(slbc_lattice *h, const double *a) {
+  Lattice &L = h->L;
+  if (ensure_staging(L, L.nnodes, 15)) return 1;
+  const long long chunk = L.staging_nodes / 15;
+  for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
+    const long long n = std::min(chunk, L.nnodes - x0);
+    CK(cudaMemcpyAsync(L.staging, a + 15 * x0, (size_t)(15 * n) * sizeof(double),
+                       cudaMemcpyHostToDevice, L.stream));
+    CK(DISPATCH(L, launch_put, L, L.staging, x0, n));
+  }
+  CK(cudaStreamSynchronize(L.stream));
+  L.layout = SLBC_LAYOUT_N;
+  return 0;
+}
+
+int slbc_get_pops(slbc_lattice *h, double *a) {
+  Lattice &L = h->L;
+  if (ensure_staging(L, L.nnodes, 15)) return 1;
+  const long long chunk = L.staging_nodes / 15;
+  for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
+    const long long n = std::min(chunk, L.nnodes - x0);
+    CK(DISPATCH(L, launch_get, L, L.staging, x0, n));
+    CK(cudaMemcpyAsync(a + 15 * x0, L.staging, (size_t)(15 * n) * sizeof(double),
+                       cudaMemcpyDeviceToHost, L.stream));
+    CK(cudaStreamSynchronize(L.stream));
+  }
+  return 0;
+}
+
+int slbc_step(slbc_lattice *h, int n, int use_graph) {
+  Lattice &L = h->L;
+  if (to_aa(L)) return 1;
+  int done = 0;
+  if (use_graph && n >= 2 * 2 * kGraphPairs) {
+    if (L.layout == SLBC_LAYOUT_C1) { if (one_step(L)) return 1; done++; }
+    if (ensure_graph(L)) return 1;
+    while (n - done >= L.graph_steps) {
+      CK(cudaGraphLaunch(L.graph, L.stream));
+      count_launch(L.graph_steps);
+      done += L.graph_steps;
+    }
+    // the graph starts and ends in C0
+  }
+  for (; done < n; done++)
+    if (one_step(L)) return 1;
+  return 0;
+}
+
+int slbc_force_step(slbc_lattice *h) {
+  Lattice &L = h->L;
+  if (to_aa(L)) return 1;
+  CK(DISPATCH(L, launch_force, L));
+  return one_step(L);
+}
+
+int slbc_bbl(slbc_lattice *h, int with_force) {
+  Lattice &L = h->L;
+  if (to_natural(L)) return 1;
+  CK(DISPATCH(L, launch_bbl, L, with_force));
+  return 0;
+}
+
+int slbc_propagate(slbc_lattice *h) {
+  Lattice &L = h->L;
+  if (to_natural(L)) return 1;
+  if (ensure_scratch(L)) return 1;
+  CK(DISPATCH(L, launch_propagate, L));
+  std::swap(L.pop, L.scratch);
+  L.generation++;  // captured graphs hold the old buffer
+  return 0;
+}
+
+int slbc_collide(slbc_lattice *h) {
+  Lattice &L = h->L;
+  if (to_natural(L)) return 1;
+  CK(DISPATCH(L, launch_collide, L));
+  return 0;
+}
+
+int slbc_zero_force(slbc_lattice *h) {
+  Lattice &L = h->L;
+  if (L.nbnd) CK(cudaMemsetAsync(L.bnd_f, 0, 3 * (size_t)L.nbnd * sizeof(double), L.stream));
+  return 0;
+}
+
+int slbc_scale_force(slbc_lattice *h, double fac) {
+  Lattice &L = h->L;
+  if (!L.nbnd) return 0;
+  k_scale<<<blocks_for(3 * L.nbnd, 256), 256, 0, L.stream>>>(L.bnd_f, 3 * L.nbnd, fac);
+  count_launch();
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int slbc_get_force(slbc_lattice *h, double *f3) {
+  Lattice &L = h->L;
+  if (!L.nbnd) return 0;
+  std::vector<double> tmp(3 * (size_t)L.nbnd);
+  CK(cudaMemcpyAsync(tmp.data(), L.bnd_f, 3 * (size_t)L.nbnd * sizeof(double),
+                     cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  for (long long e = 0; e < L.nbnd; e++) {
+    f3[3 * e] = tmp[e];
+    f3[3 * e + 1] = tmp[L.nbnd + e];
+    f3[3 * e + 2] = tmp[2 * L.nbnd + e];
+  }
+  return 0;
+}
+
+int slbc_vsum(slbc_lattice *h, double fac, const double *psi, double out[5]) {
+  Lattice &L = h->L;
+  const int nb = reduction_blocks(L);
+  if (ensure_partials(L, 5 * nb + 8)) return 1;
+  double *dpsi = nullptr;
+  if (psi) {
+    CK(cudaMallocAsync(&dpsi, (size_t)L.nnodes * sizeof(double), L.stream));
+    CK(cudaMemcpyAsync(dpsi, psi, (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+  }
+  CK(DISPATCH(L, launch_vsum, L, fac, dpsi, L.partials, nb));
+  k_final_sum<<<1, 32, 0, L.stream>>>(L.partials, nb, 5, L.partials + 5 * nb);
+  count_launch();
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(L.host_out, L.partials + 5 * nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  if (dpsi) CK(cudaFreeAsync(dpsi, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  for (int c = 0; c < 5; c++) out[c] = L.host_out[c];
+  return 0;
+}
+
+int slbc_distribf(slbc_lattice *h, const double *pos, double *ft) {
+  Lattice &L = h->L;
+  if (L.nobj == 0) return 0;
+  CK(cudaMemcpyAsync(L.obj_pos, pos, 3 * (size_t)L.nobj * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+  if (L.npiece > 0) {
+    k_distrib_piece<<<L.npiece, 256, 0, L.stream>>>(L.bnd_node, L.bnd_f, L.nbnd, L.piece_obj,
+                                                   L.piece_lo, L.piece_hi, L.obj_pos, L.esj,
+                                                   L.esk, L.piece_sum);
+    count_launch();
+    CK(cudaGetLastError());
+  }
+  const int *first = (const int *)(L.obj_ft + 6 * L.nobj);
+  k_distrib_obj<<<blocks_for(L.nobj, 128), 128, 0, L.stream>>>(first, first + L.nobj, L.piece_sum,
+                                                               L.nobj, L.obj_ft);
+  count_launch();
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ft, L.obj_ft, 6 * (size_t)L.nobj * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  return 0;
+}
+
+int slbc_set_velocity(slbc_lattice *h, const double *rho, const double *ux, const double *uy,
+                      const double *uz, int skip_solid) {
+  Lattice &L = h->L;
+  if (ensure_staging(L, L.nnodes, 4)) return 1;
+  const long long chunk = L.staging_nodes / 4;
+  std::vector<double> buf((size_t)(4 * std::min(chunk, L.nnodes)));
+  for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
+    const long long n = std::min(chunk, L.nnodes - x0);
+    for (long long e = 0; e < n; e++) {
+      buf[4 * e] = rho ? rho[x0 + e] : 0.0;
+      buf[4 * e + 1] = ux[x0 + e]; buf[4 * e + 2] = uy[x0 + e]; buf[4 * e + 3] = uz[x0 + e];
+    }
+    CK(cudaMemcpyAsync(L.staging, buf.data(), (size_t)(4 * n) * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+    CK(DISPATCH(L, launch_setvel, L, L.staging, x0, n, rho != nullptr, skip_solid));
+    CK(cudaStreamSynchronize(L.stream));
+  }
+  L.layout = SLBC_LAYOUT_N;
+  return 0;
+}
+
+// ---- moment propagation ----------------------------------------------------
+
+int slbc_mp_create(slbc_lattice *h, slbc_tracer **out, int use_f64) {
+  Lattice &L = h->L;
+  *out = nullptr;
+  slbc_tracer *t = new slbc_tracer();
+  t->h = h; t->f64 = use_f64 ? 1 : 0;
+  const size_t es = use_f64 ? 8 : 4;
+  cudaError_t e = cudaMalloc(&t->p, (size_t)L.nnodes * es);
+  if (e == cudaSuccess) e = cudaMalloc(&t->p2, (size_t)L.nnodes * es);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->p, 0, (size_t)L.nnodes * es, L.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->p2, 0, (size_t)L.nnodes * es, L.stream);
+  if (e == cudaSuccess && !L.mp_rho64) {
+    e = cudaMalloc(&L.mp_rho64, (size_t)L.nnodes * sizeof(double));
+    if (e == cudaSuccess) {
+      // rho = rho0 until the first snapshot (reference src/mpmisc.c:50-52)
+      std::vector<double> r0((size_t)L.nnodes, L.par.rho0);
+      e = cudaMemcpy(L.mp_rho64, r0.data(), (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice);
+    }
+  }
+  if (e == cudaSuccess && !use_f64 && !L.mp_rho32) {
+    e = cudaMalloc(&L.mp_rho32, (size_t)L.nnodes * sizeof(float));
+    if (e == cudaSuccess) {
+      k_convert<float, double><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>(L.mp_rho32, L.mp_rho64, L.nnodes);
+      count_launch();
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  if (e != cudaSuccess) {
+    slbc_mp_destroy(t);
+    return fail("slbc_mp_create", e);
+  }
+  *out = t;
+  return 0;
+}
+
+void slbc_mp_destroy(slbc_tracer *t) {
+  if (!t) return;
+  if (t->h) cudaStreamSynchronize(t->h->L.stream);
+  if (t->p) cudaFree(t->p);
+  if (t->p2) cudaFree(t->p2);
+  if (t->objstate) cudaFree(t->objstate);
+  delete t;
+}
+
+int slbc_mp_rhoinit(slbc_lattice *h) {
+  Lattice &L = h->L;
+  if (!L.mp_rho64) CK(cudaMalloc(&L.mp_rho64, (size_t)L.nnodes * sizeof(double)));
+  CK(DISPATCH(L, launch_mp_rhoinit, L));
+  return 0;
+}
+
+int slbc_mp_get_rho(slbc_lattice *h, double *rho) {
+  Lattice &L = h->L;
+  if (!L.mp_rho64) return fail_msg("slbc_mp_get_rho: no density snapshot");
+  CK(cudaMemcpyAsync(rho, L.mp_rho64, (size_t)L.nnodes * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  return 0;
+}
+
+int slbc_mp_put(slbc_tracer *t, const double *p) {
+  Lattice &L = t->h->L;
+  if (t->f64) {
+    CK(cudaMemcpyAsync(t->p, p, (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+  } else {
+    std::vector<float> buf((size_t)L.nnodes);
+    for (long long x = 0; x < L.nnodes; x++) buf[x] = (float)p[x];
+    CK(cudaMemcpyAsync(t->p, buf.data(), (size_t)L.nnodes * sizeof(float), cudaMemcpyHostToDevice, L.stream));
+  }
+  CK(cudaStreamSynchronize(L.stream));
+  return 0;
+}
+
+int slbc_mp_get(slbc_tracer *t, double *p) {
+  Lattice &L = t->h->L;
+  if (t->f64) {
+    CK(cudaMemcpyAsync(p, t->p, (size_t)L.nnodes * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+    CK(cudaStreamSynchronize(L.stream));
+  } else {
+    std::vector<float> buf((size_t)L.nnodes);
+    CK(cudaMemcpyAsync(buf.data(), t->p, (size_t)L.nnodes * sizeof(float), cudaMemcpyDeviceToHost, L.stream));
+    CK(cudaStreamSynchronize(L.stream));
+    for (long long x = 0; x < L.nnodes; x++) p[x] = buf[x];
+  }
+  return 0;
+}
+
+int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
+                 const double *objstate, int nobj) {
+  Lattice &L = t->h->L;
+  if (!L.mp_rho64) return fail_msg("slbc_mp_step: density snapshot missing");
+  if (!t->f64 && !L.mp_rho32) return fail_msg("slbc_mp_step: FP32 density snapshot missing");
+  if (moving) {
+    if (nobj > t->objstate_cap) {
+      if (t->objstate) { cudaStreamSynchronize(L.stream); cudaFree(t->objstate); }
+      CK(cudaMalloc(&t->objstate, 9 * (size_t)nobj * sizeof(double)));
+      t->objstate_cap = nobj;
+    }
+    if (nobj > 0)
+      CK(cudaMemcpyAsync(t->objstate, objstate, 9 * (size_t)nobj * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+  }
+  for (int s = 0; s < n; s++) {
+    CK(DISPATCH(L, launch_mp_step, L, t->p, t->p2, t->f64, alpha, adprob, moving, t->objstate));
+    std::swap(t->p, t->p2);
+  }
+  return 0;
+}
+
+static int mp_reduce(slbc_tracer *t, int axis, double out[5]) {
+  Lattice &L = t->h->L;
+  const int nb = 152 * 4;
+  if (ensure_partials(L, 5 * nb + 8)) return 1;
+  if (t->f64)
+    k_mp_sums<double><<<nb, kReduceThreads, 0, L.stream>>>((const double *)t->p, L.flags, L.ads, L.nnodes, L.esj, L.esk, axis, L.partials);
+  else
+    k_mp_sums<float><<<nb, kReduceThreads, 0, L.stream>>>((const float *)t->p, L.flags, L.ads, L.nnodes, L.esj, L.esk, axis, L.partials);
+  count_launch();
+  CK(cudaGetLastError());
+  k_final_sum<<<1, 32, 0, L.stream>>>(L.partials, nb, 5, L.partials + 5 * nb);
+  count_launch();
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(L.host_out, L.partials + 5 * nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  for (int c = 0; c < 5; c++) out[c] = L.host_out[c];
+  return 0;
+}
+
+int slbc_mp_sums(slbc_tracer *t, int axis, double out[5]) { return mp_reduce(t, axis, out); }
+
+int slbc_mp_minmax(slbc_tracer *t, double out[2]) {
+  Lattice &L = t->h->L;
+  const int nb = 152 * 2;
+  if (ensure_partials(L, 2 * nb + 8)) return 1;
+  if (t->f64) k_mp_minmax<double><<<nb, 256, 0, L.stream>>>((const double *)t->p, L.flags, L.nnodes, L.partials);
+  else k_mp_minmax<float><<<nb, 256, 0, L.stream>>>((const float *)t->p, L.flags, L.nnodes, L.partials);
+  count_launch();
+  CK(cudaGetLastError());
+  std::vector<double> part(2 * nb);
+  CK(cudaMemcpyAsync(part.data(), L.partials, 2 * nb * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  double lo = 1e300, hi = -1e300;
+  for (int b = 0; b < nb; b++) { lo = std::min(lo, part[2 * b]); hi = std::max(hi, part[2 * b + 1]); }
+  out[0] = lo; out[1] = hi;
+  return 0;
+}
+
+int slbc_mp_fill(slbc_tracer *t, int kind, const double *geo, double value) {
+  Lattice &L = t->h->L;
+  double g[6] = {0, 0, 0, 0, 0, 0};
+  const int ng = kind == 1 ? 6 : kind == 2 ? 2 : kind == 3 ? 4 : kind == 4 ? 5 : 0;
+  for (int c = 0; c < ng; c++) g[c] = geo[c];
+  if (t->f64)
+    k_mp_fill<double><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((double *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value);
+  else
+    k_mp_fill<float><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((float *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value);
+  count_launch();
+  CK(cudaGetLastError());
+  return 0;
+}
+
+static int mp_misc(slbc_tracer *t, const slbc_tracer *src, int op, double fac) {
+  Lattice &L = t->h->L;
+  if (op == 2 && src->f64 != t->f64) return fail_msg("slbc_mp_add: tracers differ in precision");
+  if (t->f64)
+    k_mp_misc<double><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((double *)t->p, src ? (const double *)src->p : nullptr, L.flags, L.ads, L.nnodes, op, fac);
+  else
+    k_mp_misc<float><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((float *)t->p, src ? (const float *)src->p : nullptr, L.flags, L.ads, L.nnodes, op, fac);
+  count_launch();
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int slbc_mp_scale(slbc_tracer *t, double fac) { return mp_misc(t, nullptr, 0, fac); }
+int slbc_mp_zero_ads(slbc_tracer *t) { return t->h->L.ads ? mp_misc(t, nullptr, 1, 0.0) : 0; }
+int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src) { return mp_misc(dst, src, 2, 0.0); }
+
+}  // extern "C"

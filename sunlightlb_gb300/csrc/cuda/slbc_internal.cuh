@@ -1,0 +1,155 @@
+// Internal definitions shared by the CUDA translation units of the GB300
+// SunlightLB device layer: the D3Q15 link table, the device state of one
+// lattice, and the per-precision launcher interface.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "slb_device.h"
+
+namespace slbc {
+
+// ---------------------------------------------------------------------------
+// D3Q15 link table (reference src/lbmisc.c:87-104):
+//   q  : 0  1  2  3  4  5  6  7  8  9 10 11 12 13 14
+//   cx : 0  1 -1  0  0  0  0  1 -1  1 -1  1 -1  1 -1
+//   cy : 0  0  0  1 -1  0  0  1  1 -1 -1  1  1 -1 -1
+//   cz : 0  0  0  0  0  1 -1  1  1  1  1 -1 -1 -1 -1
+//   w  : 16 8  8  8  8  8  8  1  1  1  1  1  1  1  1
+// Written as constexpr functions so they fold to immediates in unrolled
+// device loops and still work for run-time q.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int CX(int q) {
+  return (q == 1 || q == 7 || q == 9 || q == 11 || q == 13) ? 1
+       : (q == 2 || q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int CY(int q) {
+  return (q == 3 || q == 7 || q == 8 || q == 11 || q == 12) ? 1
+       : (q == 4 || q == 9 || q == 10 || q == 13 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int CZ(int q) {
+  return (q == 5 || q == 7 || q == 8 || q == 9 || q == 10) ? 1
+       : (q == 6 || q == 11 || q == 12 || q == 13 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int OPP(int q) {
+  return q == 0 ? 0 : (q <= 6 ? ((q & 1) ? q + 1 : q - 1) : 21 - q);
+}
+
+// Per-node flag word: bit 15 = solid node; bit q (1..14) = the link between
+// the node x and its upstream neighbour x - c_q joins a fluid and a solid
+// node (a bounce-back link).  The bit serves the population arriving along
+// q and, equally, the population leaving along opp(q).
+constexpr uint16_t FLAG_SOLID = 0x8000u;
+constexpr uint16_t FLAG_LINKS = 0x7FFEu;
+
+// Device state of one lattice.
+struct Lattice {
+  int esi = 0, esj = 0, esk = 0;
+  int precision = 0;          // 0 FP64, 1 FP32, 2 BF16
+  long long nnodes = 0;
+  long long npad = 0;         // stride between population arrays (elements)
+  void *pop = nullptr;        // 15 * npad elements
+  void *scratch = nullptr;    // second population buffer (separate phases)
+  uint16_t *flags = nullptr;  // per node
+  int layout = SLBC_LAYOUT_N;
+  // geometry
+  int nobj = 0;
+  long long nbnd = 0;
+  int *bnd_node = nullptr;    // solid boundary nodes, sorted (object, node)
+  int *bnd_obj = nullptr;
+  double *bnd_f = nullptr;    // 3 * nbnd node forces (x block, y block, z block)
+  int npiece = 0;             // distribf work pieces
+  int *piece_obj = nullptr, *piece_lo = nullptr, *piece_hi = nullptr;
+  double *piece_sum = nullptr;  // 6 * npiece
+  double *obj_pos = nullptr;    // 3 * nobj
+  double *obj_ft = nullptr;     // 6 * nobj
+  unsigned char *ads = nullptr; // adsorption byte per node
+  int *objidx = nullptr;        // object index per node (-1 fluid)
+  // parameters
+  slbc_params par{};
+  int bf_uniform = 1;
+  double bf_const[3] = {0.0, 0.0, 0.0};
+  void *bf = nullptr;         // 3 * npad of the population type, when not uniform
+  void *uw = nullptr;         // 3 * npad of the population type: wall velocity
+  // reductions
+  double *partials = nullptr;
+  int npartials = 0;
+  double *host_out = nullptr; // pinned, small
+  // staging for host transfers
+  double *staging = nullptr;
+  long long staging_nodes = 0;
+  // moment propagation: density snapshot (FP64, and FP32 for FP32 tracers)
+  double *mp_rho64 = nullptr;
+  float *mp_rho32 = nullptr;
+  // BF16 variant: reference moments (drho, ru) per node in FP32
+  float *ref_mom = nullptr;
+  double bf16_scale = 1.0;
+  // execution
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  unsigned long long generation = 1;  // bumped when anything the step reads changes
+  unsigned long long graph_generation = 0;
+  int block_k = 128;          // threads along k (autotuned)
+};
+
+// Arguments shared by the population kernels.
+template <typename T>
+struct PopArgs {
+  T *pop;
+  long long npad;
+  const uint16_t *flags;
+  int esi, esj, esk;
+};
+
+template <typename T>
+struct StepArgs {
+  PopArgs<T> p;
+  T omega, comega, rho0;
+  int stokes, skip_solid, moving;
+  int bf_uniform;
+  T bfx, bfy, bfz;
+  const T *bf;   // 3 * npad when not uniform
+  const T *uw;   // 3 * npad wall velocities when moving
+};
+
+struct ForceArgs {
+  long long nbnd;
+  const int *bnd_node;
+  double *f;     // 3 * nbnd
+};
+
+// Per-precision launchers (defined in slbc_f64.cu / slbc_f32.cu).
+#define SLBC_DECLARE_LAUNCHERS(SUFFIX)                                          \
+  cudaError_t launch_step_##SUFFIX(Lattice &L, int odd);                        \
+  cudaError_t launch_force_##SUFFIX(Lattice &L);                                \
+  cudaError_t launch_vsum_##SUFFIX(Lattice &L, double fac, const double *psi,   \
+                                   double *partials, int nblocks);              \
+  cudaError_t launch_put_##SUFFIX(Lattice &L, const double *stage,              \
+                                  long long x0, long long n);                   \
+  cudaError_t launch_get_##SUFFIX(Lattice &L, double *stage, long long x0,      \
+                                  long long n);                                 \
+  cudaError_t launch_swap_##SUFFIX(Lattice &L);                                 \
+  cudaError_t launch_to_natural_##SUFFIX(Lattice &L);                           \
+  cudaError_t launch_bbl_##SUFFIX(Lattice &L, int with_force);                  \
+  cudaError_t launch_propagate_##SUFFIX(Lattice &L);                            \
+  cudaError_t launch_collide_##SUFFIX(Lattice &L);                              \
+  cudaError_t launch_setvel_##SUFFIX(Lattice &L, const double *stage,           \
+                                     long long x0, long long n, int has_rho,    \
+                                     int skip_solid);                           \
+  cudaError_t launch_mp_rhoinit_##SUFFIX(Lattice &L);                           \
+  cudaError_t launch_mp_step_##SUFFIX(Lattice &L, const void *p_in, void *p_out, \
+                                      int tp_f64, double alpha, double adprob,  \
+                                      int moving, const double *objstate);
+
+SLBC_DECLARE_LAUNCHERS(f64)
+SLBC_DECLARE_LAUNCHERS(f32)
+
+// Launch bookkeeping (defined in slbc_core.cu)
+void count_launch(int n = 1);
+int reduction_blocks(const Lattice &L);
+constexpr int kReduceThreads = 256;
+
+}  // namespace slbc

@@ -1,0 +1,468 @@
+// Population kernels of the GB300 SunlightLB device layer, templated on the
+// population type T.  Included once per precision (slbc_f64.cu compiles it
+// with FMA contraction off so FP64 results equal the reference bit for bit;
+// slbc_f32.cu compiles it with FMA on).
+//
+// Update scheme.  The reference step (src/lbkernel.c:49-51) is link
+// bounce-back (swap a_q(solid) <-> a_opp(q)(fluid) on every solid-fluid link,
+// plus a wall term for moving objects), periodic streaming, then collision.
+// The swaps of different links touch disjoint slots, so the step is exactly
+// this pull rule at every node x and population q:
+//   link x <- x - c_q joins fluid and solid:  a'_q(x) = a_opp(q)(x) +- wall
+//   otherwise:                                a'_q(x) = a_q(x - c_q)
+// followed by the local collision.  It is applied in place with the AA
+// pattern: an odd step reads C0 (post-collision values kept at the node in
+// reversed slots), pulls from the neighbours, collides and pushes to the
+// neighbours (C1); an even step reads C1 locally, collides and writes back
+// reversed (C0).  Bounce-back values are stored raw and the wall term is
+// added when they are read, so C0 and C1 are both exact permutations of the
+// reference's post-collision array.  Each thread reads exactly the slots it
+// writes, so the in-place update has no races.
+#pragma once
+
+#include "slbc_internal.cuh"
+
+namespace slbc {
+
+// Periodic neighbourhood of node (i,j,k).
+struct Nbr {
+  int I[3], J[3], K[3];
+  int esk;
+  __device__ __forceinline__ int at(int dx, int dy, int dz) const {
+    return (I[dx + 1] + J[dy + 1]) * esk + K[dz + 1];
+  }
+};
+
+__device__ __forceinline__ Nbr make_nbr(int i, int j, int k, int esi, int esj, int esk) {
+  Nbr n;
+  const int im = i == 0 ? esi - 1 : i - 1, ip = i == esi - 1 ? 0 : i + 1;
+  const int jm = j == 0 ? esj - 1 : j - 1, jp = j == esj - 1 ? 0 : j + 1;
+  const int km = k == 0 ? esk - 1 : k - 1, kp = k == esk - 1 ? 0 : k + 1;
+  n.I[0] = im * esj; n.I[1] = i * esj; n.I[2] = ip * esj;
+  n.J[0] = jm; n.J[1] = j; n.J[2] = jp;
+  n.K[0] = km; n.K[1] = k; n.K[2] = kp;
+  n.esk = esk;
+  return n;
+}
+
+__device__ __forceinline__ void decode(int x, int esj, int esk, int &i, int &j, int &k) {
+  k = x % esk;
+  const int r = x / esk;
+  j = r % esj;
+  i = r / esj;
+}
+
+// Moving-wall momentum term of link q for a solid node whose wall velocity
+// (times rho0/12) is u: reference src/lbkernel.c:360-446, same evaluation.
+template <typename R>
+__device__ __forceinline__ R link_term(int q, R ux, R uy, R uz) {
+  switch (q) {
+    case 1: return R(8.0) * ux;
+    case 2: return R(-8.0) * ux;
+    case 3: return R(8.0) * uy;
+    case 4: return R(-8.0) * uy;
+    case 5: return R(8.0) * uz;
+    case 6: return R(-8.0) * uz;
+    case 7: return (ux + uy) + uz;
+    case 8: return (-ux + uy) + uz;
+    case 9: return (ux - uy) + uz;
+    case 10: return (-ux - uy) + uz;
+    case 11: return (ux + uy) - uz;
+    case 12: return (-ux + uy) - uz;
+    case 13: return (ux - uy) - uz;
+    default: return (-ux - uy) - uz;
+  }
+}
+
+// Rebuild the 15 populations from density deviation, momentum and stress:
+// reference src/lbkernel.c:838-865, same evaluation order.
+template <typename T, bool EXACT>
+__device__ __forceinline__ void rebuild(T (&t)[15], T drho, T rux, T ruy, T ruz, T sxx,
+                                        T syy, T szz, T sxy, T sxz, T syz) {
+  const T dbybc2 = T(1.0 / 24.0), dd2bybc4 = T(1.0 / 8.0);
+  const T fdd2bybc4 = T(4.0) * dd2bybc4, edbybc2 = T(8.0) * dbybc2;
+  T rhobyb, trsby3;
+  if (EXACT) {
+    rhobyb = drho / T(72.0);
+    trsby3 = (sxx + syy + szz) / T(3.0);
+  } else {
+    rhobyb = drho * T(1.0 / 72.0);
+    trsby3 = (sxx + syy + szz) * T(1.0 / 3.0);
+  }
+  const T erhobyb = T(8.0) * rhobyb;
+  T ru, st;
+  t[0] = T(2.0) * erhobyb - T(2.0) * fdd2bybc4 * trsby3;
+  ru = edbybc2 * rux; st = fdd2bybc4 * (sxx - trsby3);
+  t[1] = erhobyb + ru + st; t[2] = erhobyb - ru + st;
+  ru = edbybc2 * ruy; st = fdd2bybc4 * (syy - trsby3);
+  t[3] = erhobyb + ru + st; t[4] = erhobyb - ru + st;
+  ru = edbybc2 * ruz; st = fdd2bybc4 * (szz - trsby3);
+  t[5] = erhobyb + ru + st; t[6] = erhobyb - ru + st;
+  ru = dbybc2 * (rux + ruy + ruz); st = dd2bybc4 * (trsby3 + sxy + sxz + syz);
+  t[7] = rhobyb + ru + st; t[14] = rhobyb - ru + st;
+  ru = dbybc2 * (rux - ruy - ruz); st = dd2bybc4 * (trsby3 - sxy - sxz + syz);
+  t[8] = rhobyb - ru + st; t[13] = rhobyb + ru + st;
+  ru = dbybc2 * (rux - ruy + ruz); st = dd2bybc4 * (trsby3 - sxy + sxz - syz);
+  t[9] = rhobyb + ru + st; t[12] = rhobyb - ru + st;
+  ru = dbybc2 * (rux + ruy - ruz); st = dd2bybc4 * (trsby3 + sxy - sxz - syz);
+  t[10] = rhobyb - ru + st; t[11] = rhobyb + ru + st;
+}
+
+// Collision of one node: reference src/lbkernel.c:805-865.
+template <typename T, bool EXACT>
+__device__ __forceinline__ void collide(T (&t)[15], T omega, T comega, T rho0, int stokes,
+                                        bool fluid, T bx, T by, T bz) {
+  const T twoby3 = T(2.0 / 3.0);
+  const T p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
+  const T lo_sum = t[7] + t[8] + t[9] + t[10], hi_sum = t[11] + t[12] + t[13] + t[14];
+  const T lo_x = t[7] - t[8] + t[9] - t[10], hi_x = t[11] - t[12] + t[13] - t[14];
+  const T lo_y = t[7] + t[8] - t[9] - t[10], hi_y = t[11] + t[12] - t[13] - t[14];
+  const T lo_xy = t[7] - t[8] - t[9] + t[10], hi_xy = t[11] - t[12] - t[13] + t[14];
+  const T p06 = t[0] + p12 + p34 + p56;
+  const T drho = p06 + (lo_sum + hi_sum);
+  T rux = t[1] - t[2] + lo_x + hi_x;
+  T ruy = t[3] - t[4] + lo_y + hi_y;
+  T ruz = t[5] - t[6] + lo_sum - hi_sum;
+  if (fluid) { rux += bx; ruy += by; ruz += bz; }
+  const T sdiag = twoby3 * drho - p06;
+  T sxx = sdiag + p12, syy = sdiag + p34, szz = sdiag + p56;
+  T sxy = lo_xy + hi_xy, sxz = lo_x - hi_x, syz = lo_y - hi_y;
+  if (stokes) {
+    sxx = comega * sxx; sxy = comega * sxy; sxz = comega * sxz;
+    syy = comega * syy; syz = comega * syz; szz = comega * szz;
+  } else {
+    const T obyr = omega / (rho0 + drho);
+    sxx = comega * sxx + obyr * rux * rux;
+    sxy = comega * sxy + obyr * rux * ruy;
+    sxz = comega * sxz + obyr * rux * ruz;
+    syy = comega * syy + obyr * ruy * ruy;
+    syz = comega * syz + obyr * ruy * ruz;
+    szz = comega * szz + obyr * ruz * ruz;
+  }
+  rebuild<T, EXACT>(t, drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
+}
+
+// Add the moving-wall term to every population that arrived over a
+// bounce-back link (bits of fl).  Fluid node: the wall velocity is that of
+// the solid upstream node x - c_q and the term is added; solid node: its own
+// wall velocity, the term of the opposite link is subtracted.
+template <typename T>
+__device__ __forceinline__ void apply_wall(T (&t)[15], uint16_t fl, bool solid, const Nbr &nb,
+                                           int x, const T *uw, long long S) {
+#pragma unroll
+  for (int q = 1; q < 15; q++) {
+    if (!((fl >> q) & 1)) continue;
+    if (solid) {
+      t[q] = t[q] - link_term<T>(OPP(q), uw[x], uw[S + x], uw[2 * S + x]);
+    } else {
+      const int y = nb.at(-CX(q), -CY(q), -CZ(q));
+      t[q] = t[q] + link_term<T>(q, uw[y], uw[S + y], uw[2 * S + y]);
+    }
+  }
+}
+
+// One fused update step (bounce-back + streaming + collision) of every node.
+// ODD = false: C1 -> C0 (local), ODD = true: C0 -> C1 (pull and push).
+// Grid: (ceil(esk/blockDim.x), esj, esi).
+template <typename T, bool ODD, bool EXACT>
+__global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, i = blockIdx.z;
+  const int esk = a.p.esk;
+  if (k >= esk) return;
+  const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, esk);
+  const int x = nb.at(0, 0, 0);
+  const uint16_t fl = __ldg(a.p.flags + x);
+  const bool solid = (fl & FLAG_SOLID) != 0;
+  T *__restrict__ P = a.p.pop;
+  const long long S = a.p.npad;
+  T t[15];
+  if (!ODD) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
+  } else {
+    t[0] = P[x];
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> q) & 1;
+      const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+      const int slot = bnd ? q : OPP(q);
+      t[q] = P[slot * S + src];
+    }
+  }
+  if (a.moving && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
+  if (!(a.skip_solid && solid)) {
+    T bx = a.bfx, by = a.bfy, bz = a.bfz;
+    if (!a.bf_uniform) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
+    collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
+  }
+  if (!ODD) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
+  } else {
+    P[x] = t[0];
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> OPP(q)) & 1;
+      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+      const int slot = bnd ? OPP(q) : q;
+      P[slot * S + dst] = t[q];
+    }
+  }
+}
+
+// Post-collision population q of node x in a given layout (see slb_device.h).
+template <typename T>
+__device__ __forceinline__ T post_value(const T *P, long long S, int layout, int q, int x,
+                                        uint16_t fl, const Nbr &nb) {
+  if (layout == SLBC_LAYOUT_N) return P[q * S + x];
+  if (layout == SLBC_LAYOUT_C0 || q == 0) return P[OPP(q) * S + x];
+  if ((fl >> OPP(q)) & 1) return P[OPP(q) * S + x];
+  return P[q * S + nb.at(CX(q), CY(q), CZ(q))];
+}
+
+// Node forces of one bblforce (reference src/lbkernel.c:179-321 stationary,
+// 464-618 moving) over the solid boundary nodes, accumulated in link order
+// into f (x, y, z blocks of nbnd), in FP64.  Reads the post-collision
+// state; the links of a solid node s are those whose far end is fluid.
+template <typename T>
+__global__ void k_force(PopArgs<T> p, int layout, int moving, const T *uw, ForceArgs f) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= f.nbnd) return;
+  const int s = f.bnd_node[e];
+  int i, j, k;
+  decode(s, p.esj, p.esk, i, j, k);
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const uint16_t fl = p.flags[s];
+  const T *P = p.pop;
+  const long long S = p.npad;
+  double fx = f.f[e], fy = f.f[f.nbnd + e], fz = f.f[2 * f.nbnd + e];
+  double ux = 0.0, uy = 0.0, uz = 0.0;
+  if (moving) { ux = (double)uw[s]; uy = (double)uw[S + s]; uz = (double)uw[2 * S + s]; }
+#pragma unroll
+  for (int q = 1; q < 15; q++) {
+    if (!((fl >> OPP(q)) & 1)) continue;
+    const int n = nb.at(CX(q), CY(q), CZ(q));
+    double av, bv;
+    if (layout == SLBC_LAYOUT_N) { av = (double)P[q * S + s]; bv = (double)P[OPP(q) * S + n]; }
+    else { av = (double)P[OPP(q) * S + s]; bv = (double)P[q * S + n]; }
+    const double dp = moving ? 2.0 * (av - bv - link_term<double>(q, ux, uy, uz)) : 2.0 * (av - bv);
+    if (CX(q) > 0) fx += dp; else if (CX(q) < 0) fx -= dp;
+    if (CY(q) > 0) fy += dp; else if (CY(q) < 0) fy -= dp;
+    if (CZ(q) > 0) fz += dp; else if (CZ(q) < 0) fz -= dp;
+  }
+  f.f[e] = fx; f.f[f.nbnd + e] = fy; f.f[2 * f.nbnd + e] = fz;
+}
+
+// Deterministic block reduction of NV doubles; thread 0 gets the totals.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[32][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < NV; c++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < NV; c++) sh[warp][c] = v[c];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; c++) v[c] = lane < nw ? sh[lane][c] : 0.0;
+#pragma unroll
+    for (int c = 0; c < NV; c++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+  }
+}
+
+// Velocity sums of accvmean (reference src/lbmeasure.c:78-97) per block:
+// rows (i,j) are dealt to blocks round-robin, threads stride along k.
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads)
+k_vsum(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double b0, double b1,
+       double b2, const T *bf, const double *psi, double *partials) {
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const long long rows = (long long)p.esi * p.esj;
+  const T *P = p.pop;
+  const long long S = p.npad;
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int i = (int)(r / p.esj), j = (int)(r % p.esj);
+    for (int k = threadIdx.x; k < p.esk; k += blockDim.x) {
+      const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+      const int x = nb.at(0, 0, 0);
+      const uint16_t fl = p.flags[x];
+      if (fl & FLAG_SOLID) continue;
+      double t[15];
+#pragma unroll
+      for (int q = 0; q < 15; q++) t[q] = (double)post_value<T>(P, S, layout, q, x, fl, nb);
+      double bx = b0, by = b1, bz = b2;
+      if (!bf_uniform) { bx = (double)bf[x]; by = (double)bf[S + x]; bz = (double)bf[2 * S + x]; }
+      const double rho = rho0 + t[0] + t[1] + t[2] + t[3] + t[4] + t[5] + t[6] + t[7] + t[8] +
+                         t[9] + t[10] + t[11] + t[12] + t[13] + t[14];
+      const double ux = (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14] + fac * bx) / rho;
+      const double uy = (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14] + fac * by) / rho;
+      const double uz = (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14] + fac * bz) / rho;
+      double w = 1.0;
+      if (psi) { w = psi[x]; w = w * w; }
+      v[0] += w * ux; v[1] += w * uy; v[2] += w * uz; v[3] += w; v[4] += 1.0;
+    }
+  }
+  block_sum<5>(v);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int c = 0; c < 5; c++) partials[5 * blockIdx.x + c] = v[c];
+}
+
+// Host AoS staging (FP64, a[15*x + q]) -> layout N.
+template <typename T>
+__global__ void k_put(PopArgs<T> p, const double *stage, long long x0, long long n) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const long long x = x0 + e;
+#pragma unroll
+  for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = (T)stage[15 * e + q];
+}
+
+// Any layout -> host AoS staging of the reference's array.
+template <typename T>
+__global__ void k_get(PopArgs<T> p, int layout, double *stage, long long x0, long long n) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int x = (int)(x0 + e);
+  int i, j, k;
+  decode(x, p.esj, p.esk, i, j, k);
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const uint16_t fl = p.flags[x];
+#pragma unroll
+  for (int q = 0; q < 15; q++) stage[15 * e + q] = (double)post_value<T>(p.pop, p.npad, layout, q, x, fl, nb);
+}
+
+// N <-> C0: swap the slots of opposite populations at every node.
+template <typename T>
+__global__ void k_swap(PopArgs<T> p, long long n) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  T *P = p.pop;
+  const long long S = p.npad;
+#pragma unroll
+  for (int q = 1; q < 15; q++) {
+    if (OPP(q) < q) continue;
+    const T a = P[q * S + x], b = P[OPP(q) * S + x];
+    P[q * S + x] = b; P[OPP(q) * S + x] = a;
+  }
+}
+
+// C1 -> N (out of place into dst).
+template <typename T>
+__global__ void k_c1_to_n(PopArgs<T> p, T *dst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, i = blockIdx.z;
+  if (k >= p.esk) return;
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const int x = nb.at(0, 0, 0);
+  const uint16_t fl = p.flags[x];
+#pragma unroll
+  for (int q = 0; q < 15; q++) dst[q * p.npad + x] = post_value<T>(p.pop, p.npad, SLBC_LAYOUT_C1, q, x, fl, nb);
+}
+
+// Separate bounce-back on layout N (reference src/lbkernel.c:58-618): every
+// solid boundary node swaps each of its fluid links; optional force.
+template <typename T>
+__global__ void k_bbl_n(PopArgs<T> p, int moving, const T *uw, int with_force, ForceArgs f) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= f.nbnd) return;
+  const int s = f.bnd_node[e];
+  int i, j, k;
+  decode(s, p.esj, p.esk, i, j, k);
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const uint16_t fl = p.flags[s];
+  T *P = p.pop;
+  const long long S = p.npad;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (with_force) { fx = f.f[e]; fy = f.f[f.nbnd + e]; fz = f.f[2 * f.nbnd + e]; }
+#pragma unroll
+  for (int q = 1; q < 15; q++) {
+    if (!((fl >> OPP(q)) & 1)) continue;
+    const int n = nb.at(CX(q), CY(q), CZ(q));
+    const T av = P[q * S + s], bv = P[OPP(q) * S + n];
+    double dp;
+    if (moving) {
+      const T term = link_term<T>(q, uw[s], uw[S + s], uw[2 * S + s]);
+      P[OPP(q) * S + n] = av - term; P[q * S + s] = bv + term;
+      dp = 2.0 * ((double)av - (double)bv - (double)term);
+    } else {
+      P[q * S + s] = bv; P[OPP(q) * S + n] = av;
+      dp = 2.0 * ((double)av - (double)bv);
+    }
+    if (CX(q) > 0) fx += dp; else if (CX(q) < 0) fx -= dp;
+    if (CY(q) > 0) fy += dp; else if (CY(q) < 0) fy -= dp;
+    if (CZ(q) > 0) fz += dp; else if (CZ(q) < 0) fz -= dp;
+  }
+  if (with_force) { f.f[e] = fx; f.f[f.nbnd + e] = fy; f.f[2 * f.nbnd + e] = fz; }
+}
+
+// Separate streaming on layout N, out of place: dst[q][x] = pop[q][x - c_q]
+// (reference src/lbkernel.c:623-762).
+template <typename T>
+__global__ void k_propagate_n(PopArgs<T> p, T *dst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y, i = blockIdx.z;
+  if (k >= p.esk) return;
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const int x = nb.at(0, 0, 0);
+#pragma unroll
+  for (int q = 0; q < 15; q++) dst[q * p.npad + x] = p.pop[q * p.npad + nb.at(-CX(q), -CY(q), -CZ(q))];
+}
+
+// Separate collision on layout N (reference src/lbkernel.c:769-877).
+template <typename T, bool EXACT>
+__global__ void k_collide_n(StepArgs<T> a) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)a.p.esi * a.p.esj * a.p.esk;
+  if (x >= n) return;
+  const bool solid = (a.p.flags[x] & FLAG_SOLID) != 0;
+  if (a.skip_solid && solid) return;
+  T *P = a.p.pop;
+  const long long S = a.p.npad;
+  T t[15];
+#pragma unroll
+  for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
+  T bx = a.bfx, by = a.bfy, bz = a.bfz;
+  if (!a.bf_uniform) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
+  collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
+#pragma unroll
+  for (int q = 0; q < 15; q++) P[q * S + x] = t[q];
+}
+
+// Populations from (rho, u): the rebuild of lbloadvel (reference
+// src/lbstore.c:352-399).  stage holds 4 doubles per node (rho, ux, uy, uz,
+// velocities already rescaled); layout N.
+template <typename T, bool EXACT>
+__global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long long n, int has_rho,
+                         double rho0, int stokes, int skip_solid) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const long long x = x0 + e;
+  const T r = has_rho ? (T)stage[4 * e] : (T)rho0;
+  const T vx = (T)stage[4 * e + 1], vy = (T)stage[4 * e + 2], vz = (T)stage[4 * e + 3];
+  T t[15];
+  if (skip_solid && (p.flags[x] & FLAG_SOLID)) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) t[q] = T(0);
+  } else {
+    const T drho = r - (T)rho0, rux = r * vx, ruy = r * vy, ruz = r * vz;
+    T sxx = T(0), syy = T(0), szz = T(0), sxy = T(0), sxz = T(0), syz = T(0);
+    if (!stokes) {
+      sxx = vx * rux; sxy = vx * ruy; sxz = vx * ruz;
+      syy = vy * ruy; syz = vy * ruz; szz = vz * ruz;
+    }
+    rebuild<T, EXACT>(t, drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
+  }
+#pragma unroll
+  for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = t[q];
+}
+
+}  // namespace slbc

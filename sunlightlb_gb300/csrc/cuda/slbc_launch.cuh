@@ -1,0 +1,156 @@
+// Launchers of the population kernels for one population type.  Included by
+// slbc_f64.cu and slbc_f32.cu after defining SLBC_T (the type), SLBC_SUFFIX
+// (f64 / f32) and SLBC_EXACT (follow the reference's division forms).
+#pragma once
+
+#include "slbc_kernels.cuh"
+#include "slbc_mp.cuh"
+
+#define SLBC_CAT2(a, b) a##_##b
+#define SLBC_CAT(a, b) SLBC_CAT2(a, b)
+#define SLBC_FN(name) SLBC_CAT(name, SLBC_SUFFIX)
+
+namespace slbc {
+
+using T_ = SLBC_T;
+
+static PopArgs<T_> pop_args(Lattice &L) {
+  PopArgs<T_> p;
+  p.pop = (T_ *)L.pop;
+  p.npad = L.npad;
+  p.flags = L.flags;
+  p.esi = L.esi; p.esj = L.esj; p.esk = L.esk;
+  return p;
+}
+
+static StepArgs<T_> step_args(Lattice &L) {
+  StepArgs<T_> a;
+  a.p = pop_args(L);
+  const double omega = 1.0 / L.par.tau;
+  a.omega = (T_)omega;
+  a.comega = (T_)(1.0 - omega);
+  a.rho0 = (T_)L.par.rho0;
+  a.stokes = L.par.stokes_flow;
+  a.skip_solid = L.par.skip_solid;
+  a.moving = L.par.objects_moving && L.uw != nullptr;
+  a.bf_uniform = L.bf_uniform;
+  a.bfx = (T_)L.bf_const[0]; a.bfy = (T_)L.bf_const[1]; a.bfz = (T_)L.bf_const[2];
+  a.bf = (const T_ *)L.bf;
+  a.uw = (const T_ *)L.uw;
+  return a;
+}
+
+static dim3 row_grid(const Lattice &L, int bx) {
+  return dim3((unsigned)((L.esk + bx - 1) / bx), (unsigned)L.esj, (unsigned)L.esi);
+}
+
+static int flat_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+cudaError_t SLBC_FN(launch_step)(Lattice &L, int odd) {
+  const int bx = L.esk >= L.block_k ? L.block_k : (L.esk >= 64 ? 64 : 32);
+  StepArgs<T_> a = step_args(L);
+  if (odd) k_step<T_, true, SLBC_EXACT><<<row_grid(L, bx), bx, 0, L.stream>>>(a);
+  else k_step<T_, false, SLBC_EXACT><<<row_grid(L, bx), bx, 0, L.stream>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_force)(Lattice &L) {
+  if (L.nbnd == 0) return cudaSuccess;
+  ForceArgs f{L.nbnd, L.bnd_node, L.bnd_f};
+  const int bs = 128;
+  const int moving = L.par.objects_moving && L.uw != nullptr;
+  k_force<T_><<<flat_blocks(L.nbnd, bs), bs, 0, L.stream>>>(pop_args(L), L.layout, moving,
+                                                           (const T_ *)L.uw, f);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_vsum)(Lattice &L, double fac, const double *psi, double *partials,
+                                 int nblocks) {
+  k_vsum<T_><<<nblocks, kReduceThreads, 0, L.stream>>>(
+      pop_args(L), L.layout, L.par.rho0, fac, L.bf_uniform, L.bf_const[0], L.bf_const[1],
+      L.bf_const[2], (const T_ *)L.bf, psi, partials);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_put)(Lattice &L, const double *stage, long long x0, long long n) {
+  k_put<T_><<<flat_blocks(n, 256), 256, 0, L.stream>>>(pop_args(L), stage, x0, n);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_get)(Lattice &L, double *stage, long long x0, long long n) {
+  k_get<T_><<<flat_blocks(n, 256), 256, 0, L.stream>>>(pop_args(L), L.layout, stage, x0, n);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_swap)(Lattice &L) {
+  k_swap<T_><<<flat_blocks(L.nnodes, 256), 256, 0, L.stream>>>(pop_args(L), L.nnodes);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_to_natural)(Lattice &L) {
+  const int bx = L.esk >= 128 ? 128 : 32;
+  k_c1_to_n<T_><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), (T_ *)L.scratch);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_bbl)(Lattice &L, int with_force) {
+  if (L.nbnd == 0) return cudaSuccess;
+  ForceArgs f{L.nbnd, L.bnd_node, L.bnd_f};
+  const int moving = L.par.objects_moving && L.uw != nullptr;
+  k_bbl_n<T_><<<flat_blocks(L.nbnd, 128), 128, 0, L.stream>>>(pop_args(L), moving,
+                                                              (const T_ *)L.uw, with_force, f);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_propagate)(Lattice &L) {
+  const int bx = L.esk >= 128 ? 128 : 32;
+  k_propagate_n<T_><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), (T_ *)L.scratch);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_collide)(Lattice &L) {
+  k_collide_n<T_, SLBC_EXACT><<<flat_blocks(L.nnodes, 256), 256, 0, L.stream>>>(step_args(L));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_setvel)(Lattice &L, const double *stage, long long x0, long long n,
+                                   int has_rho, int skip_solid) {
+  k_setvel<T_, SLBC_EXACT><<<flat_blocks(n, 256), 256, 0, L.stream>>>(
+      pop_args(L), stage, x0, n, has_rho, L.par.rho0, L.par.stokes_flow, skip_solid);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_mp_rhoinit)(Lattice &L) {
+  k_mp_rhoinit<T_><<<flat_blocks(L.nnodes, 256), 256, 0, L.stream>>>(
+      pop_args(L), L.layout, L.par.rho0, L.mp_rho64, L.mp_rho32);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, int tp_f64,
+                                    double alpha, double adprob, int moving,
+                                    const double *objstate) {
+  const int bx = L.esk >= 128 ? 128 : (L.esk >= 64 ? 64 : 32);
+  MpArgs m;
+  m.p_in = p_in; m.p_out = p_out;
+  m.rho = tp_f64 ? (const void *)L.mp_rho64 : (const void *)L.mp_rho32;
+  m.ads = L.ads; m.objidx = L.objidx; m.objstate = objstate; m.moving = moving;
+  m.alpha = alpha; m.adprob = adprob; m.rho0 = L.par.rho0;
+  if (tp_f64) k_mp_step<T_, double><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), L.layout, m);
+  else k_mp_step<T_, float><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), L.layout, m);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace slbc

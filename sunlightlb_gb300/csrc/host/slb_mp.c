@@ -1,0 +1,395 @@
+/*
+ * Moment propagation (host side of reference src/mpkernel.c, src/mpmisc.c,
+ * src/mpobjs.c, src/mpads.c).  The tracer field p of every MPSys and the
+ * lattice's density snapshot live on the GPU; mp->p and lb->rho are host
+ * mirrors (mppull / mppush keep them coherent for drivers that touch them).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include "slb_private.h"
+
+#define ADSORB 0x4000
+
+static mp_priv *mpstate(MPSys mp) { return (mp_priv *)mp->priv; }
+
+static void mptrace(MPSys mp, const char *what) {
+  if (slb_verbosity & TRACE_ROUTINE_EXITS) printf("MP '%s' %i : %s done\n", mp->name, mp->step, what);
+}
+
+/* device tracer of mp, created on first use; uploads a host-written p */
+static slbc_tracer *tracer(MPSys mp) {
+  mp_priv *st = mpstate(mp);
+  slbc_lattice *d = slb_device(mp->lb);
+  if (st->dev == NULL) {
+    st->use_f64 = mp->precision == SLB_FP32 ? 0 : 1;
+    slb_check(slbc_mp_create(d, &st->dev, st->use_f64), "tracer set-up");
+    st->p_sent = 0;
+  }
+  if (st->p_sent != st->p_gen) {
+    slb_check(slbc_mp_put(st->dev, mp->p), "tracer upload");
+    st->p_sent = st->p_gen;
+  }
+  return st->dev;
+}
+
+static void p_changed(MPSys mp) { mpstate(mp)->host_p_valid = 0; }
+
+/* appended: host mirror mp->p <-> device */
+void mppull(MPSys mp) {
+  mp_priv *st = mpstate(mp);
+  if (st->dev == NULL || st->host_p_valid) return;
+  slb_check(slbc_mp_get(st->dev, mp->p), "tracer download");
+  st->host_p_valid = 1;
+}
+void mppush(MPSys mp) {
+  mp_priv *st = mpstate(mp);
+  st->p_gen++;
+  st->host_p_valid = 1;
+}
+
+/* reference src/mpmisc.c:38-59.  alpha starts at 0 (the reference leaves it
+ * unset); adprob = 1 gives the reference's adsorption. */
+MPSys newmp(LBSys lb, char *name) {
+  long x;
+  MPSys mp = (MPSys)calloc(1, sizeof(MPSys_type));
+  mp_priv *st = (mp_priv *)calloc(1, sizeof(mp_priv));
+  if (mp == NULL || st == NULL) error("No room for mpsys structure\n");
+  mp->lb = lb;
+  mp->p = (LBReal *)calloc((size_t)lb->nnodes, sizeof(LBReal));
+  mp->newp = (LBReal *)calloc(1, sizeof(LBReal));  /* unused: the update gathers */
+  free(lb->rho);
+  lb->rho = (LBReal *)malloc((size_t)lb->nnodes * sizeof(LBReal));
+  if (mp->p == NULL || lb->rho == NULL) error("No room at the inn");
+  for (x = 0; x < lb->nnodes; x++) lb->rho[x] = lb->rho0;
+  mp->objects_moving = lb->objects_moving;
+  mp->to_be_initialised = 1;
+  mp->adprob = 1.0;
+  mp->precision = lb->precision;
+  st->host_p_valid = 1;
+  mp->priv = st;
+  slb_state(lb)->host_rho_valid = 1;
+  if (myscmp("null", name)) mp->name = NULL; else mp->name = mycopy(name);
+  printf("MP '%s' initialised for %i * %i * %i lattice\n", mp->name, lb->esi, lb->esj, lb->esk);
+  return mp;
+}
+
+void freemp(MPSys mp) {
+  if (mp == NULL) return;
+  if (mpstate(mp)->dev) slbc_mp_destroy(mpstate(mp)->dev);
+  free(mp->priv); free(mp->p); free(mp->newp); free(mp->name); free(mp);
+}
+
+/* reference src/mpmisc.c:64-79 */
+void mprhoinit(MPSys mp) {
+  slbc_lattice *d = slb_device(mp->lb);
+  tracer(mp);  /* makes sure the snapshot buffers exist */
+  slb_check(slbc_mp_rhoinit(d), "density snapshot");
+  slb_state(mp->lb)->host_rho_valid = 0;
+  mptrace(mp, "mprhoinit");
+}
+
+/* reference src/mpmisc.c:83-99 */
+void mpinit(MPSys mp) {
+  mp_priv *st = mpstate(mp);
+  mprhoinit(mp);
+  memset(mp->p, 0, (size_t)mp->lb->nnodes * sizeof(LBReal));
+  st->p_gen++;
+  st->host_p_valid = 1;
+  tracer(mp);
+  mp->step = 0;
+  mp->to_be_initialised = 0;
+  printf("MP '%s' initialised and ready to go.\n", mp->name);
+  mptrace(mp, "mpinit");
+}
+
+/* reference src/mpmisc.c:104-114 */
+void mpwrpars(MPSys mp) {
+  LBReal d = (1.0 - mp->alpha) / 6.0;
+  printf("\nMP '%s' parameter list\n\n", mp->name);
+  printf(" | LB size  = %i * %i * %i = %i\n", mp->lb->esi, mp->lb->esj, mp->lb->esk, mp->lb->nnodes);
+  printf(" | alpha, D = %0.4f %0.6f\n", mp->alpha, d);
+  printf(mp->objects_moving ? " | Objects allowed to move\n" : " | All objects are stationary\n");
+  printf("\n");
+}
+
+/* reference src/mpkernel.c:33-43 */
+void mpstep(MPSys mp) {
+  slbc_tracer *t;
+  double *state = NULL;
+  int nobj = 0;
+  if (mp->to_be_initialised) mpinit(mp);
+  t = tracer(mp);
+  if (mp->lb->status != POST_COLLIDE) {
+    printf("Moment propagation apparently out of position\n");
+    wrstatus(mp->lb, stdout);
+  }
+  if (mp->objects_moving) {
+    slb_priv *ls = slb_state(mp->lb);
+    int o;
+    nobj = ls->nobj;
+    state = (double *)malloc(9 * (size_t)(nobj + 1) * sizeof(double));
+    if (state == NULL) error("No room for object table");
+    for (o = 0; o < nobj; o++) {
+      LBObj p = ls->objs[o];
+      double *s = state + 9 * o;
+      s[0] = p->posx; s[1] = p->posy; s[2] = p->posz;
+      s[3] = p->velx; s[4] = p->vely; s[5] = p->velz;
+      s[6] = p->angx; s[7] = p->angy; s[8] = p->angz;
+    }
+  }
+  slb_check(slbc_mp_step(t, 1, mp->alpha, mp->adprob, mp->objects_moving, state, nobj), "tracer update");
+  free(state);
+  p_changed(mp);
+#ifdef SIGNAL
+  if (slb_signal_flag) sighandle(mp->lb);
+#endif
+  mp->step += 1;
+  mptrace(mp, "mpdo");
+}
+
+static void sums(MPSys mp, int axis, double out[5]) {
+  slb_check(slbc_mp_sums(tracer(mp), axis, out), "tracer sums");
+}
+
+/* reference src/mpmisc.c:121-136 */
+void mpcheck(MPSys mp) {
+  double s[5];
+  sums(mp, -1, s);
+  printf("MP '%s' %i : fluid + solid scalar = %10.6f + %10.6f = %10.6f\n", mp->name, mp->step, s[0], s[1], s[0] + s[1]);
+  mptrace(mp, "mpcheck");
+}
+
+/* appended: tracer totals, which = "fluid", "solid", "adsorbed" or "all" */
+LBReal mptotal(MPSys mp, char *which) {
+  double s[5];
+  sums(mp, -1, s);
+  if (which[0] == 'f') return s[0];
+  if (which[0] == 's') return s[1];
+  if (which[0] == 'a' && which[1] == 'd') return s[2];
+  return s[0] + s[1];
+}
+
+/* reference src/mpmisc.c:142-158 */
+LBReal mpmean(MPSys mp) {
+  double s[5];
+  LBReal pmean;
+  sums(mp, -1, s);
+  pmean = s[0] / (LBReal)(countfluid(mp->lb));
+  if (slb_verbosity & TRACE_ROUTINE_EXITS)
+    printf("MP '%s' %i : mpnorm done, ptot = %f, pmean = %f\n", mp->name, mp->step, s[0], pmean);
+  return pmean;
+}
+
+/* reference src/mpmisc.c:164-208 (0 when there is no fluid node) */
+static LBReal extreme(MPSys mp, int want_max) {
+  double mm[2];
+  if (countfluid(mp->lb) == 0) return 0.0;
+  slb_check(slbc_mp_minmax(tracer(mp), mm), "tracer extremes");
+  return want_max ? mm[1] : mm[0];
+}
+LBReal mpmax(MPSys mp) { return extreme(mp, 1); }
+LBReal mpmin(MPSys mp) { return extreme(mp, 0); }
+
+/* reference src/mpmisc.c:214-225 */
+void mprescale(MPSys mp, LBReal fac) {
+  slb_check(slbc_mp_scale(tracer(mp), fac), "tracer rescale");
+  p_changed(mp);
+  mptrace(mp, "mprescale");
+}
+
+/* reference src/mpmisc.c:233-246 */
+void mpcopy(MPSys mp, MPSys dest) {
+  slbc_tracer *src = tracer(mp);
+  slb_check(slbc_mp_add(tracer(dest), src), "tracer copy");
+  p_changed(dest);
+  mptrace(mp, "mpcopy");
+}
+
+/* reference src/mpmisc.c:466-499 */
+LBReal mpspread(MPSys mp, char *dirn) {
+  double s[5];
+  int axis;
+  LBReal tot, mean, var = 0.0;
+  switch (dirn[0]) {
+    case 'x': case 'i': axis = 0; break;
+    case 'y': case 'j': axis = 1; break;
+    case 'z': case 'k': axis = 2; break;
+    default: printf("Unrecognised direction for measuring spread\n"); return -1.0;
+  }
+  sums(mp, axis, s);
+  tot = s[0]; mean = s[3]; var = s[4];
+  if (tot > 0.0) { mean = mean / tot; var = var / tot - mean * mean; }
+  mptrace(mp, "mpspread");
+  return var;
+}
+
+/* ---- tracer injection: reference src/mpobjs.c ---------------------------- */
+
+static void fill(MPSys mp, int kind, const double *geo, LBReal pval) {
+  slb_check(slbc_mp_fill(tracer(mp), kind, geo, pval), "tracer injection");
+  p_changed(mp);
+}
+
+void mpall(MPSys mp, LBReal pval) {
+  fill(mp, 0, NULL, pval);
+  if (slb_verbosity & MP_OBJECT_DETAILS)
+    printf("Diffusing material slab inserted everywhere, %i sites set\n", countfluid(mp->lb));
+  mptrace(mp, "mpall");
+}
+
+void mpslab(MPSys mp, LBReal x1, LBReal x2, LBReal y1, LBReal y2, LBReal z1, LBReal z2, LBReal pval) {
+  double g[6];
+  g[0] = x1; g[1] = x2; g[2] = y1; g[3] = y2; g[4] = z1; g[5] = z2;
+  fill(mp, 1, g, pval);
+  mptrace(mp, "mpslab");
+}
+
+void mpwall(MPSys mp, char *type, int wallpos, LBReal pval) {
+  double g[2];
+  int lim;
+  switch (type[0]) {
+    case 'x': case 'i': g[0] = 0; lim = mp->lb->esi; break;
+    case 'y': case 'j': g[0] = 1; lim = mp->lb->esj; break;
+    case 'z': case 'k': g[0] = 2; lim = mp->lb->esk; break;
+    default: printf("Unrecognised direction for walls\n"); return;
+  }
+  if (wallpos < 0 || wallpos > lim - 1) { printf("wallpos out of range\n"); return; }
+  g[1] = wallpos;
+  fill(mp, 2, g, pval);
+  mptrace(mp, "mpwall");
+}
+
+void mpsph(MPSys mp, LBReal rad, LBReal ox, LBReal oy, LBReal oz, LBReal pval) {
+  double g[4];
+  g[0] = rad; g[1] = ox; g[2] = oy; g[3] = oz;
+  fill(mp, 3, g, pval);
+  mptrace(mp, "mpsph");
+}
+
+void mpcyl(MPSys mp, char *type, LBReal rad, LBReal a, LBReal b, LBReal pval) {
+  double g[5];
+  switch (type[0]) {
+    case 'x': case 'i': g[0] = 0; break;
+    case 'y': case 'j': g[0] = 1; break;
+    case 'z': case 'k': g[0] = 2; break;
+    default: error("Unrecognised cylinder direction"); return;
+  }
+  g[1] = type[1] != '\0' ? 1.0 : 0.0; g[2] = rad; g[3] = a; g[4] = b;
+  fill(mp, 4, g, pval);
+  mptrace(mp, "mpcyl");
+}
+
+/* reference src/mpobjs.c:233-261: a node list is read on the host, the
+ * field is updated there and sent back. */
+void mplist(MPSys mp, char *file, LBReal pval) {
+  int i, j, k;
+  FILE *fp;
+  LBSys lb = mp->lb;
+  if ((fp = fopen(file, "r")) == NULL) { printf("mpsubs: %s could not be opened\n", file); return; }
+  mppull(mp);
+  while (fscanf(fp, "%i%i%i", &i, &j, &k) == 3) {
+    long x = slb_node(lb, i, j, k);
+    if (x < 0 || x >= lb->nnodes) continue;
+    if (lb->obj[x] == NULL) mp->p[x] = pval;
+  }
+  fclose(fp);
+  mppush(mp);
+  mptrace(mp, "mplist");
+}
+
+/* ---- adsorption sites: reference src/mpads.c ------------------------------ */
+
+void adall(MPSys mp) {
+  long x;
+  int ns = 0;
+  for (x = 0; x < mp->lb->nnodes; x++)
+    if (mp->lb->mask[x] != 0) { mp->lb->mask[x] |= ADSORB; ns++; }
+  slb_mark_ads(mp->lb);
+  printf("All nodes are adsorption sites, %i sites set\n", ns);
+  mptrace(mp, "adall");
+}
+
+void adnone(MPSys mp) {
+  long x;
+  int ns = 0;
+  for (x = 0; x < mp->lb->nnodes; x++)
+    if (mp->lb->mask[x] & ADSORB) { mp->lb->mask[x] &= ~ADSORB; ns++; }
+  slb_mark_ads(mp->lb);
+  printf("Reset %i adsorption sites to non-adsorbing sites\n", ns);
+  mptrace(mp, "adnone");
+}
+
+void adslab(MPSys mp, LBReal x1, LBReal x2, LBReal y1, LBReal y2, LBReal z1, LBReal z2) {
+  LBSys lb = mp->lb;
+  int i, j, k, ns = 0;
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++)
+    if (i > x1 && i < x2 && j > y1 && j < y2 && k > z1 && k < z2) {
+      long x = slb_node(lb, i, j, k);
+      if (lb->mask[x] != 0) { lb->mask[x] |= ADSORB; ns++; }
+    }
+  slb_mark_ads(lb);
+  printf("Adsorption site slab from %5.2f %5.2f %5.2f to %5.2f %5.2f %5.2f, %i sites set\n", x1, y1, z1, x2, y2, z2, ns);
+  mptrace(mp, "adslab");
+}
+
+void adsph(MPSys mp, LBReal rad, LBReal ox, LBReal oy, LBReal oz) {
+  LBSys lb = mp->lb;
+  int i, j, k, ns = 0;
+  LBReal radsq = rad * rad;
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    LBReal rsq = (i - ox) * (i - ox) + (j - oy) * (j - oy) + (k - oz) * (k - oz);
+    long x = slb_node(lb, i, j, k);
+    if (rsq < radsq && lb->mask[x] != 0) { lb->mask[x] |= ADSORB; ns++; }
+  }
+  slb_mark_ads(lb);
+  printf("Adsorption site sphere, radius %5.2f at %5.2f %5.2f %5.2f, %i sites set\n", rad, ox, oy, oz, ns);
+  mptrace(mp, "adsph");
+}
+
+void adcyl(MPSys mp, char *type, LBReal rad, LBReal a, LBReal b) {
+  LBSys lb = mp->lb;
+  int i, j, k, ns = 0, within;
+  LBReal rsq = 0.0, radsq = rad * rad;
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    long x = slb_node(lb, i, j, k);
+    switch (type[0]) {
+      case 'x': case 'i': rsq = (j - a) * (j - a) + (k - b) * (k - b); break;
+      case 'y': case 'j': rsq = (i - a) * (i - a) + (k - b) * (k - b); break;
+      case 'z': case 'k': rsq = (i - a) * (i - a) + (j - b) * (j - b); break;
+      default: error("Unrecognised cylinder direction");
+    }
+    within = (rsq < radsq);
+    if (type[1] != '\0') within = !within;
+    if (within && lb->mask[x] != 0) { lb->mask[x] |= ADSORB; ns++; }
+  }
+  slb_mark_ads(lb);
+  printf(type[1] == '\0' ? "Adsorbtion site cylinder, \n" : "Adsorbtion site cylindrical hole, \n");
+  printf("radius %5.2f, axis %5.2f %5.2f along %c, %i sites set\n", rad, a, b, type[0], ns);
+  mptrace(mp, "adcyl");
+}
+
+/* reference src/mpads.c:149-172 */
+LBReal adtotal(MPSys mp, char *adtfile, int imult) {
+  static int nadt = 0;
+  double s[5];
+  LBReal ptot;
+  sums(mp, -1, s);
+  ptot = s[2];
+  if (!myscmp("null", adtfile)) {
+    FILE *fp = fopen(adtfile, nadt == 0 ? "w" : "a");
+    if (fp == NULL) printf("adtotal: %s could not be opened to write/append data\n", adtfile);
+    else { fprintf(fp, "%8i %f\n", nadt * imult, ptot); fclose(fp); }
+  }
+  nadt++;
+  mptrace(mp, "adtotal");
+  return ptot;
+}
+
+/* reference src/mpads.c:177-186 */
+void adzero(MPSys mp) {
+  slb_check(slbc_mp_zero_ads(tracer(mp)), "adsorbed reset");
+  p_changed(mp);
+  mptrace(mp, "adzero");
+}

@@ -1,0 +1,150 @@
+"""GPU parity of the lattice Boltzmann update path against the CPU oracle.
+
+FP64 populations must equal the oracle's bit for bit (the oracle itself
+equals a strict build of the reference bit for bit, see test_oracle.py).
+Reductions (mean flow, object force and torque) are summed in a different
+order on the GPU, so they are compared to 1e-12 relative to their scale.
+FP32 populations are compared to the FP64 oracle at the tolerances written
+in each test.
+"""
+
+import numpy as np
+import pytest
+
+from scenarios import couette, objects_ft, two_spheres
+
+pytestmark = pytest.mark.gpu
+
+RED_TOL = 1e-12  # FP64 reductions: relative to the largest component
+
+
+def close(a, b, tol):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() <= tol * scale
+
+
+CASES = {
+    "stokes": dict(),
+    "navier_stokes": dict(stokes=0, tau=0.62),
+    "skip_solid": dict(skip=1),
+    "moving": dict(moving=1),
+    "moving_ns_skip": dict(moving=1, stokes=0, skip=1, tau=0.6),
+    "odd_steps": dict(steps=31),
+    "thin_x": dict(dims=(2, 9, 11)),
+    "thin_xy": dict(dims=(1, 2, 13), moving=1),
+    "small": dict(dims=(3, 3, 3), steps=7),
+    "ragged": dict(dims=(7, 13, 33), steps=12),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_bit_exact(gpu, orc, name):
+    cfg = CASES[name]
+    lg = two_spheres(gpu, **cfg)
+    lo = two_spheres(orc, **cfg)
+    pg, po = lg.pops(), lo.pops()
+    assert np.array_equal(pg, po), f"max |diff| = {np.abs(pg - po).max():.3e}"
+    assert lg.step == lo.step and lg.status == lo.status
+    vg = [lg.vmeanx, lg.vmeany, lg.vmeanz]
+    vo = [lo.vmeanx, lo.vmeany, lo.vmeanz]
+    assert close(vg, vo, RED_TOL), (vg, vo)
+    assert close(objects_ft(lg)[:, :3], objects_ft(lo)[:, :3], RED_TOL)
+    assert close(objects_ft(lg)[:, 3:], objects_ft(lo)[:, 3:], RED_TOL)
+    # node forces of the last measurement
+    for f in ("fx", "fy", "fz"):
+        assert close(lg.array(f), lo.array(f), RED_TOL)
+
+
+def test_graph_steps_equal_single_steps(gpu):
+    a = two_spheres(gpu, steps=260, use_steps=False, measure=False)
+    b = two_spheres(gpu, steps=260, use_steps=True, measure=False)
+    assert np.array_equal(a.pops(), b.pops())
+    assert a.step == b.step == 260
+
+
+def test_separate_phases(gpu, orc):
+    """bbl / propagate / collide called one by one, mixed with lbstep and
+    bblforce, as a driver of the reference may do."""
+    out = []
+    for L in (gpu, orc):
+        lb = two_spheres(L, steps=5, measure=False, moving=1)
+        L.bbl(lb); L.propagate(lb); L.collide(lb)
+        L.lbstep(lb)
+        L.zeroforce(lb)
+        L.bblforce(lb); L.propagate(lb)
+        L.accvmean(lb, 1.0)
+        L.collide(lb)
+        L.lbstep(lb)
+        L.normforce(lb, 0.5)
+        L.distribf(lb)
+        out.append((lb.pops(), lb.vmeanx, objects_ft(lb), lb.array("fx").copy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert abs(out[0][1] - out[1][1]) <= RED_TOL * abs(out[1][1])
+    assert close(out[0][2], out[1][2], RED_TOL)
+    assert close(out[0][3], out[1][3], RED_TOL)
+
+
+def test_psi_weighted_mean(gpu, orc):
+    vg = two_spheres(gpu, psi=True, steps=9)
+    vo = two_spheres(orc, psi=True, steps=9)
+    assert close([vg.vmeanx, vg.vmeany], [vo.vmeanx, vo.vmeany], RED_TOL)
+
+
+def test_nonuniform_body_force(gpu, orc):
+    out = []
+    for L in (gpu, orc):
+        lb = two_spheres(L, steps=0, measure=False)
+        bx = lb.array("bx")
+        bx[: lb.nnodes // 3] *= 3.0
+        L.lbpush(lb)
+        for _ in range(11):
+            L.lbstep(lb)
+        L.measure(lb)
+        out.append((lb.pops(), lb.vmeanx))
+    assert np.array_equal(out[0][0], out[1][0])
+
+
+def test_warm_start_from_velocity(gpu, orc):
+    out = []
+    for L in (gpu, orc):
+        lb = two_spheres(L, steps=0, measure=False, stokes=0, tau=0.7)
+        n = lb.nnodes
+        x = np.arange(n, dtype=float)
+        rho = 72.0 + 1e-3 * np.sin(x)
+        ux, uy, uz = 1e-3 * np.cos(x), 2e-4 * np.sin(0.3 * x), -1e-4 * np.ones(n)
+        L.lbsetvel(lb, rho, ux, uy, uz)
+        L.lbsteps(lb, 4)
+        out.append(lb.pops())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_couette_wall_force_exact(gpu):
+    """Planar Couette flow: wall force 2 eta (v1 - v2)/h, exact in LB
+    (examples/planar_couette.pl; needs vspread, which the example omits)."""
+    lb, w1, w2, expect = couette(gpu, steps=4000)
+    assert abs(abs(w1.frcx) - expect) < 1e-9 * expect
+    assert abs(abs(w2.frcx) - expect) < 1e-9 * expect
+    assert w1.frcx * w2.frcx < 0
+
+
+def test_fp32_close_to_fp64(gpu, orc):
+    """FP32 populations with FP32 collision, FP64 reductions: mean flow and
+    drag within 1e-4 relative of the FP64 oracle after 200 steps."""
+    lg = two_spheres(gpu, steps=200, precision=1)
+    lo = two_spheres(orc, steps=200)
+    assert abs(lg.vmeanx - lo.vmeanx) <= 1e-4 * abs(lo.vmeanx)
+    assert close(objects_ft(lg)[:, :3], objects_ft(lo)[:, :3], 1e-4)
+    pg, po = lg.pops(), lo.pops()
+    assert np.abs(pg - po).max() <= 1e-4 * np.abs(po).max()
+
+
+def test_precision_switch_keeps_state(gpu):
+    lb = two_spheres(gpu, steps=20, measure=False)
+    before = lb.pops()
+    lb.precision = 1
+    gpu.lbstep(lb)
+    lb.precision = 0
+    after = lb.pops()
+    assert np.abs(after - before).max() < 1e-3 * np.abs(before).max()
