@@ -107,6 +107,19 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.samples)}
 
 
+def aggregate(total_ms, nodes, steps, world, dist=None, device=None):
+    """Replica throughput over ranks: every rank advanced its own lattice of
+    `nodes` nodes by `steps` steps in total_ms; the job's time is the
+    slowest rank's.  Returns (MLUPS of the whole job, ms per step)."""
+    if world > 1 and dist is not None:
+        import torch
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / steps
+    return world * nodes / (ms_per_step * 1e-3) / 1e6, ms_per_step
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -178,13 +191,10 @@ def run_mine(args):
     launches = L.lbkernelcount() - k0
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
+    value, ms_per_step = aggregate(total_ms, nodes, args.steps, world,
+                                   torch.distributed if world > 1 else None, "cuda")
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
         torch.distributed.barrier()
-    ms_per_step = total_ms / args.steps
-    value = world * nodes / (ms_per_step * 1e-3) / 1e6
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE[precision] * nodes / (ms_per_step * 1e-3) / 1e9
 
@@ -231,8 +241,7 @@ def run_e2e(L, precision, spheres, solid, args):
     lb = build_lattice(L, precision, spheres, solid)
     n = lb.nnodes
     intervals = max(1, args.e2e_intervals)
-    a_host = lb.array("a") if lb.a else None
-    lb_a = L.lbpull(lb)  # allocates the host mirror (zero populations)
+    L.lbpull(lb)  # allocates the host mirror (zero populations)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     L.lbpush(lb)

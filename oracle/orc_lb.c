@@ -723,6 +723,86 @@ void lbloadvel(LBSys lb, char *loadfile, char *type) {
   free(r); free(vx); free(vy); free(vz);
 }
 
+
+/* ------------------------------------------------------------------------
+ * moment checkpoint: reference src/lbstore.c:36-218.  drho and the momenta
+ * are LBStoreReal (float) variables in the reference, so the stress uses the
+ * rounded drho and some of the rebuild sums run in float; kept here.
+ * ---------------------------------------------------------------------- */
+void lbsave(LBSys lb, char *savefile) {
+  long n;
+  FILE *fp;
+  const LBReal twoby3 = 2.0 / 3.0;
+  if ((fp = fopen(savefile, "wb")) == NULL) { printf("savefile: %s could not be opened\n", savefile); return; }
+  bbl(lb); propagate(lb);
+  for (n = 0; n < lb->nnodes; n++) {
+    const LBReal *t = lb->a + 15 * n;
+    LBReal p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
+    LBReal lo_sum = t[7] + t[8] + t[9] + t[10], hi_sum = t[11] + t[12] + t[13] + t[14];
+    LBReal lo_x = t[7] - t[8] + t[9] - t[10], hi_x = t[11] - t[12] + t[13] - t[14];
+    LBReal lo_y = t[7] + t[8] - t[9] - t[10], hi_y = t[11] + t[12] - t[13] - t[14];
+    LBReal lo_xy = t[7] - t[8] - t[9] + t[10], hi_xy = t[11] - t[12] - t[13] + t[14];
+    LBReal p06 = t[0] + p12 + p34 + p56, sd;
+    LBStoreReal m[10];
+    m[0] = p06 + (lo_sum + hi_sum);
+    m[1] = t[1] - t[2] + lo_x + hi_x;
+    m[2] = t[3] - t[4] + lo_y + hi_y;
+    m[3] = t[5] - t[6] + lo_sum - hi_sum;
+    sd = twoby3 * m[0] - p06;
+    m[4] = sd + p12; m[5] = sd + p34; m[6] = sd + p56;
+    m[7] = lo_xy + hi_xy; m[8] = lo_x - hi_x; m[9] = lo_y - hi_y;
+    fwrite(m, sizeof(LBStoreReal), 10, fp);
+  }
+  fclose(fp);
+  collide(lb);
+}
+
+void lbload(LBSys lb, char *loadfile) {
+  long n;
+  int q;
+  FILE *fp;
+  LBReal b = 72.0, dbybc2 = 1.0 / 24.0, dd2bybc4 = 1.0 / 8.0;
+  LBReal fdd2bybc4 = 4.0 * dd2bybc4, edbybc2 = 8.0 * dbybc2;
+  if (lb->changed_objects) syncobjs(lb);
+  if ((fp = fopen(loadfile, "r")) == NULL) { printf("lbload: %s could not be opened\n", loadfile); exit(EXIT_FAILURE); }
+  for (n = 0; n < lb->nnodes; n++) {
+    LBStoreReal s[10], drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz;
+    LBReal rhobyb, erhobyb, trsby3, ru, st, v[15];
+    if (fread(s, sizeof(LBStoreReal), 10, fp) != 10) memset(s, 0, sizeof s);
+    drho = s[0];
+    rux = (lb->rescale) * s[1]; ruy = (lb->rescale) * s[2]; ruz = (lb->rescale) * s[3];
+    sxx = s[4]; syy = s[5]; szz = s[6]; sxy = s[7]; sxz = s[8]; syz = s[9];
+    rhobyb = drho / b; erhobyb = 8.0 * rhobyb;
+    trsby3 = (sxx + syy + szz) / 3.0;
+    v[0] = 2.0 * erhobyb - 2.0 * fdd2bybc4 * trsby3;
+    ru = edbybc2 * rux; st = fdd2bybc4 * (sxx - trsby3);
+    v[1] = erhobyb + ru + st; v[2] = erhobyb - ru + st;
+    ru = edbybc2 * ruy; st = fdd2bybc4 * (syy - trsby3);
+    v[3] = erhobyb + ru + st; v[4] = erhobyb - ru + st;
+    ru = edbybc2 * ruz; st = fdd2bybc4 * (szz - trsby3);
+    v[5] = erhobyb + ru + st; v[6] = erhobyb - ru + st;
+    ru = dbybc2 * (rux + ruy + ruz); st = dd2bybc4 * (trsby3 + sxy + sxz + syz);
+    v[7] = rhobyb + ru + st; v[14] = rhobyb - ru + st;
+    ru = dbybc2 * (rux - ruy - ruz); st = dd2bybc4 * (trsby3 - sxy - sxz + syz);
+    v[8] = rhobyb - ru + st; v[13] = rhobyb + ru + st;
+    ru = dbybc2 * (rux - ruy + ruz); st = dd2bybc4 * (trsby3 - sxy + sxz - syz);
+    v[9] = rhobyb + ru + st; v[12] = rhobyb - ru + st;
+    ru = dbybc2 * (rux + ruy - ruz); st = dd2bybc4 * (trsby3 + sxy - sxz - syz);
+    v[10] = rhobyb - ru + st; v[11] = rhobyb + ru + st;
+    for (q = 0; q < 15; q++) {
+      if (lb->load_average) lb->a[q + 15 * n] += 0.5 * v[q];
+      else lb->a[q + 15 * n] = v[q];
+    }
+  }
+  fclose(fp);
+  if (lb->skip_solid)
+    for (n = 0; n < lb->nnodes; n++)
+      if (lb->obj[n] != NULL) for (q = 0; q < 15; q++) lb->a[q + 15 * n] = 0.0;
+  lb->status = POST_PROPAGATE;
+  collide(lb);
+  lb->rescale = 1.0;
+}
+
 /* ------------------------------------------------------------------------
  * appended helpers so drivers written for the GPU library run unchanged
  * ---------------------------------------------------------------------- */

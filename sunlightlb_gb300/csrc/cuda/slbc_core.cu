@@ -306,8 +306,8 @@ int ensure_graph(Lattice &L) {
 namespace slbc {
 void count_launch(int n) { g_launches += n; }
 int reduction_blocks(const Lattice &L) {
-  long long rows = (long long)L.esi * L.esj;
-  return (int)std::max<long long>(1, std::min<long long>(rows, 152 * 4));
+  // 8 blocks of 256 threads per SM, fewer for small lattices
+  return (int)std::max<long long>(1, std::min<long long>((L.nnodes + 255) / 256, 152 * 8));
 }
 }  // namespace slbc
 

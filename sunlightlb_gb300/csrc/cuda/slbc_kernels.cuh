@@ -279,36 +279,40 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
 }
 
 // Velocity sums of accvmean (reference src/lbmeasure.c:78-97) per block:
-// rows (i,j) are dealt to blocks round-robin, threads stride along k.
+// block b reduces the contiguous node range [b*chunk, (b+1)*chunk), its
+// threads striding through it; the fixed partition makes the sums
+// deterministic.
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads)
 k_vsum(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double b0, double b1,
        double b2, const T *bf, const double *psi, double *partials) {
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  const long long rows = (long long)p.esi * p.esj;
+  const long long n = (long long)p.esi * p.esj * p.esk;
+  const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = lo + chunk < n ? lo + chunk : n;
   const T *P = p.pop;
   const long long S = p.npad;
-  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
-    const int i = (int)(r / p.esj), j = (int)(r % p.esj);
-    for (int k = threadIdx.x; k < p.esk; k += blockDim.x) {
-      const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
-      const int x = nb.at(0, 0, 0);
-      const uint16_t fl = p.flags[x];
-      if (fl & FLAG_SOLID) continue;
-      double t[15];
+  for (long long e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    const int x = (int)e;
+    const uint16_t fl = p.flags[x];
+    if (fl & FLAG_SOLID) continue;
+    int i, j, k;
+    decode(x, p.esj, p.esk, i, j, k);
+    const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+    double t[15];
 #pragma unroll
-      for (int q = 0; q < 15; q++) t[q] = (double)post_value<T>(P, S, layout, q, x, fl, nb);
-      double bx = b0, by = b1, bz = b2;
-      if (!bf_uniform) { bx = (double)bf[x]; by = (double)bf[S + x]; bz = (double)bf[2 * S + x]; }
-      const double rho = rho0 + t[0] + t[1] + t[2] + t[3] + t[4] + t[5] + t[6] + t[7] + t[8] +
-                         t[9] + t[10] + t[11] + t[12] + t[13] + t[14];
-      const double ux = (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14] + fac * bx) / rho;
-      const double uy = (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14] + fac * by) / rho;
-      const double uz = (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14] + fac * bz) / rho;
-      double w = 1.0;
-      if (psi) { w = psi[x]; w = w * w; }
-      v[0] += w * ux; v[1] += w * uy; v[2] += w * uz; v[3] += w; v[4] += 1.0;
-    }
+    for (int q = 0; q < 15; q++) t[q] = (double)post_value<T>(P, S, layout, q, x, fl, nb);
+    double bx = b0, by = b1, bz = b2;
+    if (!bf_uniform) { bx = (double)bf[x]; by = (double)bf[S + x]; bz = (double)bf[2 * S + x]; }
+    const double rho = rho0 + t[0] + t[1] + t[2] + t[3] + t[4] + t[5] + t[6] + t[7] + t[8] +
+                       t[9] + t[10] + t[11] + t[12] + t[13] + t[14];
+    const double ux = (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14] + fac * bx) / rho;
+    const double uy = (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14] + fac * by) / rho;
+    const double uz = (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14] + fac * bz) / rho;
+    double w = 1.0;
+    if (psi) { w = psi[x]; w = w * w; }
+    v[0] += w * ux; v[1] += w * uy; v[2] += w * uz; v[3] += w; v[4] += 1.0;
   }
   block_sum<5>(v);
   if (threadIdx.x == 0)

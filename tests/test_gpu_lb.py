@@ -141,10 +141,14 @@ def test_fp32_close_to_fp64(gpu, orc):
 
 
 def test_precision_switch_keeps_state(gpu):
-    lb = two_spheres(gpu, steps=20, measure=False)
-    before = lb.pops()
-    lb.precision = 1
-    gpu.lbstep(lb)
-    lb.precision = 0
-    after = lb.pops()
-    assert np.abs(after - before).max() < 1e-3 * np.abs(before).max()
+    """Changing lb->precision between steps carries the state over: 20 FP64
+    steps, one FP32 step, back to FP64 equals 21 FP64 steps to FP32
+    rounding."""
+    a = two_spheres(gpu, steps=20, measure=False)
+    a.precision = 1
+    gpu.lbstep(a)
+    a.precision = 0
+    b = two_spheres(gpu, steps=21, measure=False)
+    pa, pb = a.pops(), b.pops()
+    assert a.step == b.step == 21
+    assert np.abs(pa - pb).max() < 1e-6 * np.abs(pb).max()

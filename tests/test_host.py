@@ -1,0 +1,186 @@
+"""Host side of the GB300 library, on the CPU: the shared library loads and
+exports every function the headers declare, set-up routines (objects,
+geometry, mask, wall velocity, body force, adsorption marks) give exactly
+the oracle's host arrays, and device calls fail loudly when there is no GPU.
+None of these tests launches a kernel."""
+
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions(header):
+    with open(os.path.join(ROOT, "include", header)) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set()
+    for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", text, re.M):
+        names.add(m.group(1))
+    return names
+
+
+@pytest.mark.parametrize("header", ["sunlightlb.h", "slb_device.h"])
+def test_library_exports_every_declared_function(gpu, header):
+    names = declared_functions(header)
+    assert len(names) > 10
+    missing = [n for n in sorted(names) if not hasattr(gpu.dll, n)]
+    assert not missing, f"{header}: not exported: {missing}"
+
+
+def obj_ids(lb):
+    """Object id per node (-1 fluid), independent of pointer values."""
+    ids = {o.address: o.id for o in lb.objects()}
+    raw = lb.array("obj")
+    return np.array([ids.get(int(p), -2) if p else -1 for p in raw])
+
+
+def same_host_state(a, b):
+    assert np.array_equal(obj_ids(a), obj_ids(b))
+    assert np.array_equal(a.array("mask"), b.array("mask"))
+    assert a.next_id == b.next_id and a.changed_objects == b.changed_objects
+    pa = [(o.id, o.posx, o.posy, o.posz) for o in a.objects()]
+    pb = [(o.id, o.posx, o.posy, o.posz) for o in b.objects()]
+    assert pa == pb
+    for f in ("ux", "uy", "uz", "bx", "by", "bz"):
+        assert np.array_equal(a.array(f), b.array(f)), f
+
+
+def build_geometry(L, rng_seed):
+    rng = np.random.default_rng(rng_seed)
+    lb = L.newlb(11, 12, 13, "null")
+    rets = []
+    for _ in range(12):
+        r = float(rng.uniform(-1.0, 6.0))
+        c = [float(v) for v in rng.uniform(-4.0, 16.0, 3)]
+        o = L.insertsph(lb, r, *c)
+        rets.append(o is None)
+    rets.append(L.insertcyl(lb, "y", 2.2, 3.0, 4.5) is None)
+    rets.append(L.insertcyl(lb, "zh", 4.5, 5.0, 5.0) is None)
+    rets.append(L.insertwall(lb, "x", 10) is None)
+    rets.append(L.insertwall(lb, "k", 40) is None)       # out of range: empty object stays
+    rets.append(L.insertslab(lb, 1.5, 4.5, -1.0, 3.2, 7.0, 12.5) is None)
+    rets.append(L.insertslab(lb, 3.0, 3.5, 0, 1, 0, 1) is None)  # no node
+    L.syncobjs(lb)
+    return lb, rets
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_geometry_set_up_matches_oracle(gpu, orc, seed):
+    a, ra = build_geometry(gpu, seed)
+    b, rb = build_geometry(orc, seed)
+    assert ra == rb
+    same_host_state(a, b)
+    assert gpu.countfluid(a) == orc.countfluid(b)
+    for kind in ("links", "faces"):
+        assert gpu.countmask(a, kind) == orc.countmask(b, kind)
+
+
+def test_flatten_invert_remove_match_oracle(gpu, orc):
+    out = []
+    for L in (gpu, orc):
+        lb, _ = build_geometry(L, 7)
+        L.flattenobj(lb)
+        s1 = (obj_ids(lb).copy(), [(o.id, o.posx, o.posy, o.posz) for o in lb.objects()])
+        L.invertobj(lb)
+        L.syncobjs(lb)
+        s2 = (obj_ids(lb).copy(), lb.array("mask").copy(), [(o.id, o.posx) for o in lb.objects()])
+        L.removeobjs(lb)
+        s3 = (obj_ids(lb).copy(), lb.next_id)
+        out.append((s1, s2, s3))
+    (a1, a2, a3), (b1, b2, b3) = out
+    assert np.array_equal(a1[0], b1[0]) and a1[1] == b1[1]
+    assert np.array_equal(a2[0], b2[0]) and np.array_equal(a2[1], b2[1]) and a2[2] == b2[2]
+    assert np.array_equal(a3[0], b3[0]) and a3[1] == b3[1]
+
+
+def test_wall_velocity_and_body_force_match_oracle(gpu, orc):
+    states = []
+    for L in (gpu, orc):
+        lb, _ = build_geometry(L, 4)
+        for o in lb.objects():
+            o.velx, o.vely, o.velz = 1e-3 * o.id, -2e-3, 5e-4
+            o.angx, o.angy, o.angz = 1e-4, 2e-4 * o.id, -3e-4
+        L.vspread(lb)
+        L.vset(lb, 0, 0, 0, 0.1, 0.2, 0.3)
+        L.vset(lb, 50, 0, 0, 0.1, 0.2, 0.3)
+        L.addbf(lb, 1e-5, -2e-6, 3e-7)
+        L.addbf(lb, 1e-5, 0.0, 0.0)
+        states.append(lb)
+    same_host_state(*states)
+    gpu.zerobf(states[0]); orc.zerobf(states[1])
+    same_host_state(*states)
+
+
+def test_adsorption_marks_match_oracle(gpu, orc):
+    masks = []
+    for L in (gpu, orc):
+        lb, _ = build_geometry(L, 5)
+        mp = L.newmp(lb, "null")
+        L.adsph(mp, 4.0, 5.0, 5.0, 5.0)
+        L.adslab(mp, -1, 5, -1, 20, 3, 9)
+        L.adcyl(mp, "x", 3.0, 6.0, 6.0)
+        m1 = lb.array("mask").copy()
+        L.adall(mp)
+        m2 = lb.array("mask").copy()
+        L.adnone(mp)
+        masks.append((m1, m2, lb.array("mask").copy()))
+    for x, y in zip(*masks):
+        assert np.array_equal(x, y)
+
+
+def test_insertsph_bounding_box_equals_full_scan(gpu, orc):
+    """The library scans only a sphere's bounding box; the node set must be
+    the reference's full-lattice scan for awkward radii and centres."""
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        dims = [int(v) for v in rng.integers(1, 9, 3)]
+        r = float(rng.choice([0.0, 0.5, 1.0, np.sqrt(2.0), 2.5, 7.9, 30.0, -3.0]))
+        c = [float(v) for v in rng.uniform(-10, 18, 3)]
+        res = []
+        for L in (gpu, orc):
+            lb = L.newlb(*dims, "null")
+            o = L.insertsph(lb, r, *c)
+            res.append((o is None, obj_ids(lb), lb.next_id))
+        assert res[0][0] == res[1][0] and np.array_equal(res[0][1], res[1][1]) and res[0][2] == res[1][2]
+
+
+def test_struct_layout_shared_with_reference():
+    """The fields a SWIG driver sees sit at the reference's offsets; the
+    appended fields come after next_id."""
+    from sunlightlb_gb300.binding import LBSysBase, LBSysExt, MPSysBase, MPSysExt
+    for f, _ in LBSysBase._fields_:
+        assert getattr(LBSysBase, f).offset == getattr(LBSysExt, f).offset
+    assert LBSysExt.precision.offset >= LBSysBase.next_id.offset + 4
+    for f, _ in MPSysBase._fields_:
+        assert getattr(MPSysBase, f).offset == getattr(MPSysExt, f).offset
+
+
+def test_device_call_without_gpu_fails_loudly(gpu):
+    """No CPU path: without a CUDA device the first device call exits with
+    the reference's fatal-error convention and a clear message."""
+    if gpu.dll.slbc_device_count() > 0:
+        pytest.skip("a GPU is present")
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from sunlightlb_gb300.SunlightLB import *\n"
+            "lb = newlb(8, 8, 8, 'null')\n"
+            "insertsph(lb, 2.0, 3.5, 3.5, 3.5)\n"
+            "lbstep(lb)\n"
+            "print('still running')\n") % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "still running" not in r.stdout
+    assert "no CUDA device" in r.stderr
+
+
+def test_host_mirror_without_device(gpu):
+    lb = gpu.newlb(4, 5, 6, "null")
+    gpu.lbpull(lb)              # allocates the mirror, no device needed
+    a = lb.array("a")
+    assert a.shape == (120, 15) and not a.any()

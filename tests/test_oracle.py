@@ -1,0 +1,123 @@
+"""The CPU oracle pinned against builds of the reference (CPU only).
+
+The golden fixtures of tests/golden/ were produced by tests/golden/make_golden.py
+from two builds of the reference's own sources: a strict IEEE build (the
+bit-exact target) and the as-shipped -O3 -ffast-math build.  The oracle must
+reproduce the strict build's populations bit for bit and the shipped
+build's results to 1e-12 relative; the known-answer runs of the reference's
+examples must give the published numbers.
+"""
+
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from scenarios import objects_ft, two_spheres
+from golden.make_golden import (LB_CASES, MP_CASES, mp_case, rcp_perm, sccp_sphere,
+                                sphere_converge)
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def digest(arr):
+    a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64)) + 0.0
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def rel_close(a, b, tol):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.abs(a - b).max() <= tol * max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", sorted(LB_CASES))
+def test_lb_case_matches_reference(orc, name):
+    g = load("lb_cases.json")["cases"]
+    lb = two_spheres(orc, **LB_CASES[name])
+    a = lb.array("a")
+    assert digest(a) == g["strict"][name]["pops_sha256"]
+    assert lb.step == g["strict"][name]["step"]
+    assert [lb.vmeanx, lb.vmeany, lb.vmeanz] == g["strict"][name]["vmean"]
+    assert objects_ft(lb).tolist() == g["strict"][name]["objects_ft"]
+    shipped = g["shipped"][name]
+    assert rel_close([lb.vmeanx, lb.vmeany, lb.vmeanz], shipped["vmean"], 1e-12)
+    assert rel_close(objects_ft(lb)[:, :3], np.array(shipped["objects_ft"])[:, :3], 1e-12)
+    assert rel_close(a.ravel()[:: max(1, a.size // 16)][:16], shipped["pops_sample"], 1e-12)
+
+
+@pytest.mark.parametrize("name", sorted(MP_CASES))
+def test_mp_case_matches_reference(orc, name):
+    g = load("mp_cases.json")["cases"]
+    r = mp_case(orc, **MP_CASES[name])
+    assert r["p_sha256"] == g["strict"][name]["p_sha256"]
+    for key in ("mpmean", "mpspread_x", "adtotal"):
+        assert r[key] == g["strict"][name][key]
+        assert abs(r[key] - g["shipped"][name][key]) <= 1e-12 * max(abs(g["shipped"][name][key]), 1e-300)
+
+
+def test_sccp_sphere_known_answer(orc):
+    kat = load("kat.json")["kat"]["sccp_sphere"]
+    r = sccp_sphere(orc)
+    assert r["u_mean"] == kat["strict"]["u_mean"]
+    assert round(r["u_mean"], 6) == kat["published"]["u_mean"]
+
+
+def test_rcp_permeability_known_answer(orc):
+    kat = load("kat.json")["kat"]["rcp_perm"]
+    spheres = load("rcp144.json")["spheres"]
+    r = rcp_perm(orc, spheres)
+    assert r["k"] == kat["strict"]["k"]
+    assert round(r["k"], 6) == kat["published"]["k"]
+    assert round(r["vmeanx"], 6) == kat["published"]["vmeanx"]
+    assert round(r["pore_fraction"], 2) == kat["published"]["pore_fraction"]
+
+
+def test_plain_method_first_2000_steps(orc):
+    kat = load("kat.json")["kat"]["sphere_converge"]
+    r = sphere_converge(orc, stop_at=2000)
+    assert r["vmeanx"] == kat["strict"]["vmeanx_at_2000"]
+
+
+def test_oracle_equals_reference_build_live(orc, ref_strict):
+    """Where the reference is built here: more geometries, compared live."""
+    for cfg in (dict(dims=(9, 10, 11), steps=13, moving=1, stokes=0, tau=0.55),
+                dict(dims=(4, 20, 6), steps=9, skip=1)):
+        a = two_spheres(orc, **cfg)
+        b = two_spheres(ref_strict, **cfg)
+        assert np.array_equal(a.array("a"), b.array("a"))
+        assert a.vmeanx == b.vmeanx
+
+
+def test_partial_adsorption_conserves_mass(orc):
+    """Extension (no reference counterpart): adsorption probability P.  With
+    the flow frozen, fluid + adsorbed tracer is conserved to round-off for
+    any P, and P = 1 is the reference's all-or-nothing adsorption."""
+    L = orc
+    lb = L.newlb(12, 13, 15, "null")
+    lb.tau = 0.7
+    L.insertsph(lb, 3.5, 5.5, 6.0, 7.2)
+    L.addbf(lb, 1e-3, 2e-4, 0)
+    for _ in range(20):
+        L.lbstep(lb)
+    for P in (0.0, 0.01, 0.37, 1.0):
+        mp = L.newmp(lb, "null")
+        mp.alpha = 0.3
+        mp.adprob = P
+        L.mpinit(mp)
+        L.adall(mp)
+        L.mpall(mp, 1.0)
+        m0 = L.mptotal(mp, "all")
+        for _ in range(60):
+            L.mpstep(mp)
+        m1 = L.mptotal(mp, "fluid") + L.mptotal(mp, "adsorbed")
+        assert abs(m1 - m0) <= 1e-12 * m0, (P, m0, m1)
+        if P == 0.0:
+            assert L.mptotal(mp, "adsorbed") == 0.0
+        L.adnone(mp)
