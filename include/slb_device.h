@@ -159,6 +159,36 @@ int slbc_mp_zero_ads(slbc_tracer *t);
 /* dst p += src p on fluid nodes (reference src/mpmisc.c:233-246). */
 int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src);
 
+/* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
+ * device memory.  For callers that cannot call cudaMalloc where they need
+ * the result: an application that hands out all device memory from its own
+ * pool, or a time-stepping loop that must not allocate (cudaMalloc can
+ * synchronise the whole device and can fail under memory pressure in the
+ * middle of a run).  No counterpart in the reference.
+ *   pop, npad, precision, layout: populations as described at the top of
+ *     this header (device memory);
+ *   flags: per-node flag words (device, 16 bit: bit 15 = solid node, bit q =
+ *     the link between x and x - c_q joins a fluid and a solid node);
+ *   bx, by, bz: uniform body force, used when bf is NULL; otherwise bf holds
+ *     3*npad per-node values of the population type (device);
+ *   psi: per-node weights (device) or NULL; out: 5 doubles (device), written
+ *     as out[0..4] of slbc_vsum.
+ * Its only intermediate data, one partial sum per reduction block, lives in
+ * a static device array of SLBC_VSUM_NOALLOC_MAX_BLOCKS * 5 doubles that
+ * every GPU loading the library keeps until the process exits; nblocks (the
+ * number of reduction blocks) must lie in 1..SLBC_VSUM_NOALLOC_MAX_BLOCKS
+ * and larger values are rejected with an error.  The first call on each
+ * device looks up the array's device address; make that first call before
+ * any stream capture.  Every call shares the array, so calls that overlap on
+ * the GPU (on different streams) race.  Work is queued on `stream` and not
+ * synchronised. */
+#define SLBC_VSUM_NOALLOC_MAX_BLOCKS 1216
+int slbc_vsum_noalloc(const void *pop, long long npad, int precision, int layout,
+                      const unsigned short *flags, int esi, int esj, int esk,
+                      double rho0, double fac, double bx, double by, double bz,
+                      const void *bf, const double *psi, int nblocks, double *out,
+                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif

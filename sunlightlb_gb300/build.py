@@ -24,7 +24,7 @@ LIB = os.path.join(LIB_DIR, "libsunlightlb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CUDA_DIR]
 # FP64 kernels: no FMA contraction, so FP64 results equal the reference's
-PER_FILE = {"slbc_f64.cu": ["-fmad=false"]}
+PER_FILE = {"slbc_f64.cu": ["-fmad=false"], "slbc_noalloc.cu": ["-fmad=false"]}
 # host C: strict IEEE double (no contraction, which gcc applies on aarch64)
 CC_FLAGS = ["-O2", "-fPIC", "-std=gnu99", "-Wall", "-Wno-unused-result",
             "-fno-fast-math", "-ffp-contract=off", "-I" + INC, "-I" + HOST_DIR]

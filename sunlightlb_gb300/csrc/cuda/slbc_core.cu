@@ -305,6 +305,7 @@ int ensure_graph(Lattice &L) {
 
 namespace slbc {
 void count_launch(int n) { g_launches += n; }
+void set_error(const std::string &msg) { g_err = msg; }
 int reduction_blocks(const Lattice &L) {
   // 8 blocks of 256 threads per SM, fewer for small lattices
   return (int)std::max<long long>(1, std::min<long long>((L.nnodes + 255) / 256, 152 * 8));

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "slb_device.h"
@@ -147,8 +148,9 @@ struct ForceArgs {
 SLBC_DECLARE_LAUNCHERS(f64)
 SLBC_DECLARE_LAUNCHERS(f32)
 
-// Launch bookkeeping (defined in slbc_core.cu)
+// Launch bookkeeping and error text (defined in slbc_core.cu)
 void count_launch(int n = 1);
+void set_error(const std::string &msg);
 int reduction_blocks(const Lattice &L);
 constexpr int kReduceThreads = 256;
 
