@@ -47,7 +47,9 @@ RMIN, RMAX = 4.0, 8.0
 FORCE = 1e-6
 TAU = 1.0
 SEED = 1
-BYTES_PER_UPDATE = {0: 240, 1: 120}  # 2 * 15 populations * bytes per population
+# bytes per node update: 2 * 15 populations * bytes per population; BF16
+# deviation storage also reads and writes one float4 of moments
+BYTES_PER_UPDATE = {0: 240, 1: 120, 2: 92}
 CHECK = 100                           # check interval of the e2e run (98 steps + measure)
 
 
@@ -131,14 +133,19 @@ def measured_peak():
 
 
 def profile_traffic(prec_name):
-    """DRAM bytes per launch of the fused step from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "lb_step_traffic.json")
+    """DRAM bytes per launch of the fused step (mean of the odd and even
+    step) from the committed ncu summary profiles/lb_step_128.md, line
+    'traffic_per_launch_<precision>: <bytes>'."""
+    p = os.path.join(ROOT, "profiles", "lb_step_128.md")
     try:
         with open(p) as f:
-            d = json.load(f)
-        return d.get(prec_name)
+            for line in f:
+                key = f"traffic_per_launch_{prec_name}:"
+                if line.strip().startswith(key):
+                    return int(float(line.split(":", 1)[1].split()[0]))
     except Exception:
-        return None
+        pass
+    return None
 
 
 def build_lattice(L, precision, spheres, solid):
@@ -148,7 +155,100 @@ def build_lattice(L, precision, spheres, solid):
     return lb
 
 
+class Flusher:
+    """L2 flush between timed steps: write a 256 MiB buffer (larger than the
+    129 MB L2), then read it back so the lines left in L2 are clean and no
+    write-back of flush data lands inside the next timed step."""
+
+    def __init__(self, torch):
+        self.buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.buf.zero_()
+        self.buf.sum()
+
+
+def time_steps(torch, L, lb, steps, warmup, flusher=None):
+    """Per-step device times (ms) of `steps` lbstep calls, CUDA events on
+    the lattice's own stream, optional L2 flush before each timed step."""
+    stream = torch.cuda.ExternalStream(L.lbgetstream(lb))
+    for _ in range(warmup):
+        L.lbstep(lb)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for s in range(steps):
+            if flusher is not None:
+                flusher()
+            starts[s].record(stream)
+            L.lbstep(lb)
+            ends[s].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(starts, ends)]
+
+
+def tuning(L, lb):
+    import ctypes
+    cfg = (ctypes.c_int * 4)()
+    state = L.lbtuning(lb, ctypes.addressof(cfg))
+    return {"state": {1: "tuned", -1: "default", 0: "none"}.get(state, state),
+            "even": {"rows_per_thread": cfg[0], "threads_k": cfg[1]},
+            "odd": {"rows_per_thread": cfg[2], "threads_k": cfg[3]}}
+
+
+def variant_line(torch, L, name, n, solid, precision, steps, flush):
+    from sunlightlb_gb300 import workloads as W
+    lb = L.newlb(n, n, n, "null")
+    lb.precision = precision
+    lb.tau = TAU
+    lb.stokes_flow = 1
+    W.insert_solid(L, lb, solid)
+    L.flattenobj(lb)
+    L.syncobjs(lb)
+    L.addbf(lb, FORCE, 0.0, 0.0)
+    L.lbsteps(lb, 2)
+    ms = time_steps(torch, L, lb, steps, 3, Flusher(torch) if flush else None)
+    mean = sum(ms) / len(ms)
+    nodes = lb.nnodes
+    peak, kind = measured_peak()
+    gbs = BYTES_PER_UPDATE[precision] * nodes / (mean * 1e-3) / 1e9
+    out = {"lattice": n, "populations": {0: "fp64", 1: "fp32", 2: "bf16 deviation + fp32 moments"}[precision],
+           "MLUPS": round(nodes / (mean * 1e-3) / 1e6, 1), "bytes_per_update": BYTES_PER_UPDATE[precision],
+           "ms_per_step": round(mean, 5), "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
+           "l2": "flushed" if flush else "lattice larger than L2", "tuning": tuning(L, lb)}
+    L.freelb(lb)
+    return name, out
+
+
+def permeability_run(torch, L, solid, precision, tol, maxsteps):
+    """Packed bed to convergence (checks every 100 steps until the relative
+    change of the mean flow is below tol): update steps, wall time and the
+    Darcy constant k = vmeanx * eta / b."""
+    from sunlightlb_gb300 import workloads as W
+    lb = L.newlb(N_SIDE, N_SIDE, N_SIDE, "null")
+    lb.precision = precision
+    lb.tau = TAU
+    lb.stokes_flow = 1
+    W.insert_solid(L, lb, solid)
+    L.flattenobj(lb)
+    L.syncobjs(lb)
+    L.addbf(lb, FORCE, 0.0, 0.0)
+    L.lbsteps(lb, 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps = L.lbconverge(lb, CHECK, tol, maxsteps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    k = W.permeability(lb, FORCE)
+    objs = lb.objects()
+    drag = objs[0].frcx if objs else None
+    L.freelb(lb)
+    return {"steps": steps + 2, "wall_s": round(dt, 3), "k": k, "drag_x": drag, "converged": steps < maxsteps}
+
+
 def run_mine(args):
+    import numpy as np
     import torch
     import sunlightlb_gb300
     from sunlightlb_gb300 import workloads as W
@@ -159,37 +259,27 @@ def run_mine(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     L = sunlightlb_gb300.library()
-    precision = 1 if args.precision == "fp32" else 0
-    prec_name = "fp32" if precision == 1 else "fp64"
+    precision = {"fp64": 0, "fp32": 1, "bf16dev": 2}[args.precision]
+    prec_name = args.precision
     spheres, solid = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
     lb = build_lattice(L, precision, spheres, solid)
     nodes = lb.nnodes
 
     # -------- device-resident throughput: one step per timed iteration --------
-    L.lbsteps(lb, 2)  # first device call uploads the lattice
-    stream = torch.cuda.ExternalStream(L.lbgetstream(lb))
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    L.lbsteps(lb, 2)  # first device call: upload, autotune
+    flusher = Flusher(torch)
     for _ in range(args.warmup):
         L.lbstep(lb)
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     k0 = L.lbkernelcount()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         t0 = time.perf_counter()
-        for s in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                starts[s].record(stream)
-            L.lbstep(lb)
-            ends[s].record(stream)
-        torch.cuda.synchronize()
+        step_ms = time_steps(torch, L, lb, args.steps, 0, flusher)
         wall = time.perf_counter() - t0
     launches = L.lbkernelcount() - k0
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
     value, ms_per_step = aggregate(total_ms, nodes, args.steps, world,
                                    torch.distributed if world > 1 else None, "cuda")
@@ -197,14 +287,34 @@ def run_mine(args):
         torch.distributed.barrier()
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE[precision] * nodes / (ms_per_step * 1e-3) / 1e9
+    tune = tuning(L, lb)
 
     # -------- end-to-end through the public API with host buffers -------------
     e2e = run_e2e(L, precision, spheres, solid, args)
 
+    # -------- other precisions and sizes of the same packing ------------------
+    variants = {}
+    if not args.no_variants and rank == 0:
+        big = np.tile(solid, (2, 2, 2))  # 256^3, the 128^3 packing repeated periodically
+        for name, n, sol, prec, flush in (("fp32_256", 256, big, 1, False),
+                                          ("bf16dev_128", N_SIDE, solid, 2, True),
+                                          ("bf16dev_256", 256, big, 2, False),
+                                          ("fp64_128", N_SIDE, solid, 0, True)):
+            k, v = variant_line(torch, L, name, n, sol, prec, min(args.steps, 30), flush)
+            variants[k] = v
+
+    perm = {}
+    if not args.no_convergence and rank == 0:
+        for name, prec in (("fp64", 0), ("fp32", 1), ("bf16dev", 2)):
+            perm[name] = permeability_run(torch, L, solid, prec, 1e-8, args.max_converge_steps)
+        if "fp64" in perm and perm["fp64"]["k"]:
+            for name in perm:
+                perm[name]["k_rel_error_vs_fp64"] = abs(perm[name]["k"] - perm["fp64"]["k"]) / abs(perm["fp64"]["k"])
+
     if rank != 0:
         return
     line = {
-        "metric": "MLUPS (million lattice updates per second, all nodes), fused FP32 step",
+        "metric": "MLUPS (million lattice updates per second, all nodes), packed-bed lattice Boltzmann step",
         "value": round(value, 1),
         "unit": "MLUPS",
         "n_gpus": world,
@@ -214,9 +324,9 @@ def run_mine(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": {0: "f64", 1: "f32", 2: "f32 arithmetic, bf16 deviation storage"}[precision],
         "data": "synthetic seeded RSA sphere packing (the reference publishes no benchmark data set)",
-        "config": config(prec_name, "flushed between timed steps (256 MiB write)"),
+        "config": dict(config(prec_name, "flushed between timed steps (256 MiB write, then read)"), autotune=tune),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": profile_traffic(prec_name),
@@ -225,6 +335,8 @@ def run_mine(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed": round(wall, 4),
+        "variants": variants,
+        "permeability": dict(perm, criterion="|d vmeanx| / vmeanx < 1e-8 between 100-step checks"),
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spheres, solid, budget_s=args.cpu_seconds)
@@ -319,7 +431,7 @@ def run_reference(args):
     cb = cpu_baseline(spheres, solid, budget_s=budget, threads=threads)
     line = {
         "impl": "reference",
-        "metric": "MLUPS (million lattice updates per second, all nodes), fused FP32 step",
+        "metric": "MLUPS (million lattice updates per second, all nodes), packed-bed lattice Boltzmann step",
         "value": cb["value"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic seeded RSA sphere packing",
@@ -336,8 +448,11 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--e2e-intervals", type=int, default=10)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16dev"])
+    ap.add_argument("--e2e-intervals", type=int, default=20)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-convergence", action="store_true")
+    ap.add_argument("--max-converge-steps", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

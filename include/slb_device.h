@@ -87,6 +87,14 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
 int slbc_put_pops(slbc_lattice *h, const double *a);
 int slbc_get_pops(slbc_lattice *h, double *a);
 int slbc_layout(slbc_lattice *h);
+/* Launch shape of the fused step per parity, cfg = {even rows per thread,
+ * even threads along k, odd rows per thread, odd threads along k}.  The
+ * first slbc_step of a lattice of 2^20 nodes or more times the candidate
+ * shapes on a copy of the populations and keeps the fastest (environment
+ * SLB_AUTOTUNE=0 turns this off); get returns 1 tuned, -1 defaults, 0 not
+ * yet decided; set pins a shape. */
+int slbc_get_tuning(slbc_lattice *h, int cfg[4]);
+int slbc_set_tuning(slbc_lattice *h, const int cfg[4]);
 
 /* Fused update steps from a post-collision state (replaces lbstep,
  * reference src/lbkernel.c:49-51): n in-place AA steps.  use_graph replays

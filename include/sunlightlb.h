@@ -299,6 +299,10 @@ void *lbgetstream(LBSys);
 void lbsetstream(LBSys, void *);
 /* Number of GPU kernel launches made by the library so far (all lattices). */
 long lbkernelcount(void);
+/* Launch shape the autotuner chose for the fused step of lb, cfg[4] = {even
+ * rows per thread, even threads along k, odd rows per thread, odd threads
+ * along k}; returns 1 tuned, -1 defaults, 0 not decided yet. */
+int lbtuning(LBSys, int *);
 /* Release every host and device resource of mp. */
 void freemp(MPSys);
 /* Host mirror mp->p: mppull copies the device tracer into it, mppush marks

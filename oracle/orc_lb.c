@@ -811,6 +811,7 @@ void lbpull(LBSys lb) { (void)lb; }
 void lbpush(LBSys lb) { (void)lb; }
 void lbsteps(LBSys lb, int n) { int s; for (s = 0; s < n; s++) lbstep(lb); }
 long lbkernelcount(void) { return 0; }
+int lbtuning(LBSys lb, int *cfg) { (void)lb; cfg[0] = cfg[1] = cfg[2] = cfg[3] = 0; return 0; }
 
 int lbconverge(LBSys lb, int interval, LBReal tol, int maxsteps) {
   int steps = 0, have = 0;

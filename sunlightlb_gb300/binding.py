@@ -131,7 +131,7 @@ PROTOS = {
     # appended API
     "lbpull": ("v", "L"), "lbpush": ("v", "L"), "lbsteps": ("v", "Li"),
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
-    "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "freemp": ("v", "M"),
+    "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "freemp": ("v", "M"),
     "lbsetvel": ("v", "LDDDD"), "mptotal": ("d", "Ms"), "mppull": ("v", "M"), "mppush": ("v", "M"),
 }
 

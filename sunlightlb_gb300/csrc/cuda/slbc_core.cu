@@ -47,7 +47,10 @@ int fail_msg(const std::string &m) {
     if (e_ != cudaSuccess) return fail(#call, e_); \
   } while (0)
 
+// bytes of one stored population, and of the side arrays (body force, wall
+// velocity) that the kernels read in their arithmetic type
 size_t elem_size(int precision) { return precision == 0 ? 8 : precision == 1 ? 4 : 2; }
+size_t side_size(int precision) { return precision == 0 ? 8 : 4; }
 
 // kernels that do not depend on the population type -------------------------
 
@@ -70,15 +73,6 @@ __global__ void k_flags(const int *objidx, uint16_t *flags, int esi, int esj, in
     if ((objidx[y] >= 0) != solid) f |= (uint16_t)(1u << q);
   }
   flags[x] = f;
-}
-
-__global__ void k_final_sum(const double *partials, int n, int nv, double *out) {
-  // one thread per component, fixed order: deterministic
-  const int c = threadIdx.x;
-  if (c >= nv) return;
-  double s = 0.0;
-  for (int b = 0; b < n; b++) s += partials[nv * b + c];
-  out[c] = s;
 }
 
 __global__ void k_scale(double *v, long long n, double fac) {
@@ -220,6 +214,15 @@ int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 // per-precision dispatch ------------------------------------------------------
 #define DISPATCH(L, name, ...)                                               \
   ((L).precision == 0 ? name##_f64(__VA_ARGS__) : name##_f32(__VA_ARGS__))
+// operations that also exist for BF16 deviation storage
+#define DISPATCH3(L, name, ...)                                              \
+  ((L).precision == 2 ? name##_bf16(__VA_ARGS__) : DISPATCH(L, name, __VA_ARGS__))
+
+int no_bf16(const Lattice &L, const char *what) {
+  if (L.precision != 2) return 0;
+  g_err = std::string(what) + ": not available for BF16 deviation storage (use FP32 or FP64 populations)";
+  return 1;
+}
 
 int ensure_staging(Lattice &L, long long nodes, int per_node) {
   const long long want = std::min<long long>(nodes, 1 << 20);
@@ -249,7 +252,7 @@ int ensure_partials(Lattice &L, int n) {
 // put the state into a post-collision AA layout (C0 or C1)
 int to_aa(Lattice &L) {
   if (L.layout == SLBC_LAYOUT_N) {
-    CK(DISPATCH(L, launch_swap, L));
+    CK(DISPATCH3(L, launch_swap, L));
     L.layout = SLBC_LAYOUT_C0;
   }
   return 0;
@@ -257,6 +260,7 @@ int to_aa(Lattice &L) {
 
 // put the state into layout N
 int to_natural(Lattice &L) {
+  if (L.layout != SLBC_LAYOUT_N && no_bf16(L, "conversion to the reference layout")) return 1;
   if (L.layout == SLBC_LAYOUT_C0) {
     CK(DISPATCH(L, launch_swap, L));
   } else if (L.layout == SLBC_LAYOUT_C1) {
@@ -271,15 +275,67 @@ int to_natural(Lattice &L) {
 
 int one_step(Lattice &L) {
   const int odd = L.layout == SLBC_LAYOUT_C0;
-  CK(DISPATCH(L, launch_step, L, odd));
+  CK(DISPATCH3(L, launch_step, L, odd));
   L.layout = odd ? SLBC_LAYOUT_C1 : SLBC_LAYOUT_C0;
+  return 0;
+}
+
+// Autotuner of the fused step: for each parity, time every candidate launch
+// shape (rows per thread, threads along k) on a copy of the populations --
+// the lattice's own state is not touched -- and keep the fastest.  Lattices
+// below 2^20 nodes use the default shape; SLB_AUTOTUNE=0 disables tuning.
+int autotune(Lattice &L) {
+  static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
+  const int ncand = (int)(sizeof cand / sizeof cand[0]);
+  const char *env = getenv("SLB_AUTOTUNE");
+  for (int p = 0; p < 2; p++) { L.tuned[p].npt = 1; L.tuned[p].block_k = 128; }
+  if ((env && env[0] == '0') || L.nnodes < (1LL << 20) || L.esk < 64) {
+    L.tune_state = -1;
+    return 0;
+  }
+  if (ensure_scratch(L)) return 1;
+  const size_t bytes = 15 * (size_t)L.npad * elem_size(L.precision);
+  CK(cudaMemcpyAsync(L.scratch, L.pop, bytes, cudaMemcpyDeviceToDevice, L.stream));
+  std::swap(L.pop, L.scratch);  // kernels below run on the copy
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int rc = 0;
+  for (int parity = 0; parity < 2 && !rc; parity++) {
+    float best = 1e30f;
+    int besti = 1;
+    for (int c = 0; c < ncand && !rc; c++) {
+      L.tuned[parity].npt = cand[c][0];
+      L.tuned[parity].block_k = cand[c][1];
+      float tmin = 1e30f;
+      for (int rep = 0; rep < 4 && !rc; rep++) {
+        cudaEventRecord(e0, L.stream);
+        if (DISPATCH3(L, launch_step, L, parity) != cudaSuccess) rc = 1;
+        cudaEventRecord(e1, L.stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = 1;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < tmin) tmin = ms;
+      }
+      if (tmin < best) { best = tmin; besti = c; }
+    }
+    L.tuned[parity].npt = cand[besti][0];
+    L.tuned[parity].block_k = cand[besti][1];
+  }
+  g_launches -= 2 * ncand * 4;  // tuning launches are not part of the simulation
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::swap(L.pop, L.scratch);
+  if (rc) return fail_msg("autotune: a candidate launch failed");
+  L.tune_state = 1;
+  L.generation++;
   return 0;
 }
 
 constexpr int kGraphPairs = 25;  // one graph = 50 steps, starting from C0
 
 int ensure_graph(Lattice &L) {
-  if (L.graph && L.graph_generation == L.generation) return 0;
+  if (L.graph && L.graph_generation == L.generation && L.graph_mom == L.mom_cur) return 0;
   if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal));
@@ -298,6 +354,7 @@ int ensure_graph(Lattice &L) {
   if (e != cudaSuccess) return fail("cudaGraphInstantiate", e);
   L.graph_steps = 2 * kGraphPairs;
   L.graph_generation = L.generation;
+  L.graph_mom = L.mom_cur;
   return 0;
 }
 
@@ -329,8 +386,8 @@ int slbc_create(slbc_lattice **out, int esi, int esj, int esk, int precision) {
   if (esi < 1 || esj < 1 || esk < 1) return fail_msg("slbc_create: lattice sides must be >= 1");
   const long long n = (long long)esi * esj * esk;
   if (n >= (1LL << 31)) return fail_msg("slbc_create: lattice has 2^31 nodes or more");
-  if (precision < 0 || precision > 1)
-    return fail_msg("slbc_create: precision must be 0 (FP64) or 1 (FP32)");
+  if (precision < 0 || precision > 2)
+    return fail_msg("slbc_create: precision must be 0 (FP64), 1 (FP32) or 2 (BF16 deviations)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail_msg("slbc_create: no CUDA device is available (the GB300 library has no CPU path)");
@@ -349,6 +406,10 @@ int slbc_create(slbc_lattice **out, int esi, int esj, int esk, int precision) {
   if (e == cudaSuccess) e = cudaMemset(L.objidx, 0xff, (size_t)n * sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&L.host_out, 64 * sizeof(double));
+  for (int b = 0; b < 2 && e == cudaSuccess && precision == 2; b++) {
+    e = cudaMalloc(&L.mom[b], (size_t)L.npad * 4 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(L.mom[b], 0, (size_t)L.npad * 4 * sizeof(float));
+  }
   if (e != cudaSuccess) {
     slbc_destroy(h);
     return fail("slbc_create", e);
@@ -365,7 +426,7 @@ void slbc_destroy(slbc_lattice *h) {
   if (L.stream) cudaStreamSynchronize(L.stream);
   void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
                   L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
-                  L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.ref_mom};
+                  L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1]};
   for (void *b : bufs) if (b) cudaFree(b);
   if (L.host_out) cudaFreeHost(L.host_out);
   if (L.graph) cudaGraphExecDestroy(L.graph);
@@ -391,6 +452,27 @@ int slbc_synchronize(slbc_lattice *h) {
 }
 
 int slbc_layout(slbc_lattice *h) { return h->L.layout; }
+
+int slbc_get_tuning(slbc_lattice *h, int cfg[4]) {
+  const Lattice &L = h->L;
+  cfg[0] = L.tuned[0].npt; cfg[1] = L.tuned[0].block_k;
+  cfg[2] = L.tuned[1].npt; cfg[3] = L.tuned[1].block_k;
+  return L.tune_state;
+}
+
+int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
+  Lattice &L = h->L;
+  for (int p = 0; p < 2; p++) {
+    const int npt = cfg[2 * p], bx = cfg[2 * p + 1];
+    if ((npt != 1 && npt != 2) || (bx != 32 && bx != 64 && bx != 128 && bx != 256))
+      return fail_msg("slbc_set_tuning: rows per thread must be 1 or 2 and threads along k 32, 64, 128 or 256");
+    L.tuned[p].npt = npt;
+    L.tuned[p].block_k = bx;
+  }
+  L.tune_state = 1;
+  L.generation++;
+  return 0;
+}
 
 int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *bnd_node,
                       const int *bnd_obj, long nbnd) {
@@ -492,7 +574,7 @@ int slbc_set_bodyforce(slbc_lattice *h, const double *bx, const double *by, cons
   L.bf_uniform = uniform ? 1 : 0;
   L.bf_const[0] = c[0]; L.bf_const[1] = c[1]; L.bf_const[2] = c[2];
   if (!uniform) {
-    const size_t es = elem_size(L.precision);
+    const size_t es = side_size(L.precision);
     CK(cudaMalloc(&L.bf, 3 * (size_t)L.npad * es));
     std::vector<char> buf((size_t)n * es);
     const double *src[3] = {bx, by, bz};
@@ -514,7 +596,7 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
   if (L.uw) { cudaStreamSynchronize(L.stream); cudaFree(L.uw); L.uw = nullptr; }
   if (ux && uy && uz) {
     const long long n = L.nnodes;
-    const size_t es = elem_size(L.precision);
+    const size_t es = side_size(L.precision);
     CK(cudaMalloc(&L.uw, 3 * (size_t)L.npad * es));
     std::vector<char> buf((size_t)n * es);
     const double *src[3] = {ux, uy, uz};
@@ -539,7 +621,7 @@ int slbc_put_pops(slbc_lattice *h, const double *a) {
     const long long n = std::min(chunk, L.nnodes - x0);
     CK(cudaMemcpyAsync(L.staging, a + 15 * x0, (size_t)(15 * n) * sizeof(double),
                        cudaMemcpyHostToDevice, L.stream));
-    CK(DISPATCH(L, launch_put, L, L.staging, x0, n));
+    CK(DISPATCH3(L, launch_put, L, L.staging, x0, n));
   }
   CK(cudaStreamSynchronize(L.stream));
   L.layout = SLBC_LAYOUT_N;
@@ -552,7 +634,7 @@ int slbc_get_pops(slbc_lattice *h, double *a) {
   const long long chunk = L.staging_nodes / 15;
   for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
     const long long n = std::min(chunk, L.nnodes - x0);
-    CK(DISPATCH(L, launch_get, L, L.staging, x0, n));
+    CK(DISPATCH3(L, launch_get, L, L.staging, x0, n));
     CK(cudaMemcpyAsync(a + 15 * x0, L.staging, (size_t)(15 * n) * sizeof(double),
                        cudaMemcpyDeviceToHost, L.stream));
     CK(cudaStreamSynchronize(L.stream));
@@ -563,6 +645,7 @@ int slbc_get_pops(slbc_lattice *h, double *a) {
 int slbc_step(slbc_lattice *h, int n, int use_graph) {
   Lattice &L = h->L;
   if (to_aa(L)) return 1;
+  if (L.tune_state == 0 && autotune(L)) return 1;
   int done = 0;
   if (use_graph && n >= 2 * 2 * kGraphPairs) {
     if (L.layout == SLBC_LAYOUT_C1) { if (one_step(L)) return 1; done++; }
@@ -582,12 +665,13 @@ int slbc_step(slbc_lattice *h, int n, int use_graph) {
 int slbc_force_step(slbc_lattice *h) {
   Lattice &L = h->L;
   if (to_aa(L)) return 1;
-  CK(DISPATCH(L, launch_force, L));
+  CK(DISPATCH3(L, launch_force, L));
   return one_step(L);
 }
 
 int slbc_bbl(slbc_lattice *h, int with_force) {
   Lattice &L = h->L;
+  if (no_bf16(L, "slbc_bbl")) return 1;
   if (to_natural(L)) return 1;
   CK(DISPATCH(L, launch_bbl, L, with_force));
   return 0;
@@ -595,6 +679,7 @@ int slbc_bbl(slbc_lattice *h, int with_force) {
 
 int slbc_propagate(slbc_lattice *h) {
   Lattice &L = h->L;
+  if (no_bf16(L, "slbc_propagate")) return 1;
   if (to_natural(L)) return 1;
   if (ensure_scratch(L)) return 1;
   CK(DISPATCH(L, launch_propagate, L));
@@ -606,7 +691,7 @@ int slbc_propagate(slbc_lattice *h) {
 int slbc_collide(slbc_lattice *h) {
   Lattice &L = h->L;
   if (to_natural(L)) return 1;
-  CK(DISPATCH(L, launch_collide, L));
+  CK(DISPATCH3(L, launch_collide, L));
   return 0;
 }
 
@@ -649,8 +734,8 @@ int slbc_vsum(slbc_lattice *h, double fac, const double *psi, double out[5]) {
     CK(cudaMallocAsync(&dpsi, (size_t)L.nnodes * sizeof(double), L.stream));
     CK(cudaMemcpyAsync(dpsi, psi, (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice, L.stream));
   }
-  CK(DISPATCH(L, launch_vsum, L, fac, dpsi, L.partials, nb));
-  k_final_sum<<<1, 32, 0, L.stream>>>(L.partials, nb, 5, L.partials + 5 * nb);
+  CK(DISPATCH3(L, launch_vsum, L, fac, dpsi, L.partials, nb));
+  k_final_sum_tree<5><<<1, 256, 0, L.stream>>>(L.partials, nb, L.partials + 5 * nb);
   count_launch();
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(L.host_out, L.partials + 5 * nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
@@ -694,7 +779,7 @@ int slbc_set_velocity(slbc_lattice *h, const double *rho, const double *ux, cons
       buf[4 * e + 1] = ux[x0 + e]; buf[4 * e + 2] = uy[x0 + e]; buf[4 * e + 3] = uz[x0 + e];
     }
     CK(cudaMemcpyAsync(L.staging, buf.data(), (size_t)(4 * n) * sizeof(double), cudaMemcpyHostToDevice, L.stream));
-    CK(DISPATCH(L, launch_setvel, L, L.staging, x0, n, rho != nullptr, skip_solid));
+    CK(DISPATCH3(L, launch_setvel, L, L.staging, x0, n, rho != nullptr, skip_solid));
     CK(cudaStreamSynchronize(L.stream));
   }
   L.layout = SLBC_LAYOUT_N;
@@ -750,7 +835,7 @@ void slbc_mp_destroy(slbc_tracer *t) {
 int slbc_mp_rhoinit(slbc_lattice *h) {
   Lattice &L = h->L;
   if (!L.mp_rho64) CK(cudaMalloc(&L.mp_rho64, (size_t)L.nnodes * sizeof(double)));
-  CK(DISPATCH(L, launch_mp_rhoinit, L));
+  CK(DISPATCH3(L, launch_mp_rhoinit, L));
   return 0;
 }
 
@@ -792,6 +877,7 @@ int slbc_mp_get(slbc_tracer *t, double *p) {
 int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
                  const double *objstate, int nobj) {
   Lattice &L = t->h->L;
+  if (no_bf16(L, "slbc_mp_step")) return 1;
   if (!L.mp_rho64) return fail_msg("slbc_mp_step: density snapshot missing");
   if (!t->f64 && !L.mp_rho32) return fail_msg("slbc_mp_step: FP32 density snapshot missing");
   if (moving) {
@@ -820,7 +906,7 @@ static int mp_reduce(slbc_tracer *t, int axis, double out[5]) {
     k_mp_sums<float><<<nb, kReduceThreads, 0, L.stream>>>((const float *)t->p, L.flags, L.ads, L.nnodes, L.esj, L.esk, axis, L.partials);
   count_launch();
   CK(cudaGetLastError());
-  k_final_sum<<<1, 32, 0, L.stream>>>(L.partials, nb, 5, L.partials + 5 * nb);
+  k_final_sum_tree<5><<<1, 256, 0, L.stream>>>(L.partials, nb, L.partials + 5 * nb);
   count_launch();
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(L.host_out, L.partials + 5 * nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, L.stream));

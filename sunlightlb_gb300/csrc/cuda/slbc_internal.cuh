@@ -44,6 +44,12 @@ __host__ __device__ constexpr int OPP(int q) {
 constexpr uint16_t FLAG_SOLID = 0x8000u;
 constexpr uint16_t FLAG_LINKS = 0x7FFEu;
 
+// Launch shape of the fused step (chosen by the autotuner per parity).
+struct StepConfig {
+  int npt = 0;      // rows along j per thread (1 or 2); 0 = not tuned
+  int block_k = 0;  // threads along k
+};
+
 // Device state of one lattice.
 struct Lattice {
   int esi = 0, esj = 0, esk = 0;
@@ -83,8 +89,11 @@ struct Lattice {
   // moment propagation: density snapshot (FP64, and FP32 for FP32 tracers)
   double *mp_rho64 = nullptr;
   float *mp_rho32 = nullptr;
-  // BF16 variant: reference moments (drho, ru) per node in FP32
-  float *ref_mom = nullptr;
+  // BF16 deviation storage: post-collision moments (drho, ru), two float4
+  // buffers swapped every step, and the deviation scale
+  void *mom[2] = {nullptr, nullptr};
+  int mom_cur = 0;
+  int graph_mom = 0;
   double bf16_scale = 1.0;
   // execution
   cudaStream_t stream = nullptr;
@@ -93,7 +102,8 @@ struct Lattice {
   int graph_steps = 0;
   unsigned long long generation = 1;  // bumped when anything the step reads changes
   unsigned long long graph_generation = 0;
-  int block_k = 128;          // threads along k (autotuned)
+  StepConfig tuned[2];        // [0] even step, [1] odd step
+  int tune_state = 0;         // 0 not tuned, 1 tuned, -1 tuning disabled
 };
 
 // Arguments shared by the population kernels.
@@ -147,6 +157,18 @@ struct ForceArgs {
 
 SLBC_DECLARE_LAUNCHERS(f64)
 SLBC_DECLARE_LAUNCHERS(f32)
+
+// BF16 deviation storage (slbc_bf16.cu): the operations it supports
+cudaError_t launch_step_bf16(Lattice &L, int odd);
+cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n);
+cudaError_t launch_get_bf16(Lattice &L, double *stage, long long x0, long long n);
+cudaError_t launch_swap_bf16(Lattice &L);
+cudaError_t launch_vsum_bf16(Lattice &L, double fac, const double *psi, double *partials, int nblocks);
+cudaError_t launch_force_bf16(Lattice &L);
+cudaError_t launch_setvel_bf16(Lattice &L, const double *stage, long long x0, long long n, int has_rho,
+                               int skip_solid);
+cudaError_t launch_collide_bf16(Lattice &L);
+cudaError_t launch_mp_rhoinit_bf16(Lattice &L);
 
 // Launch bookkeeping and error text (defined in slbc_core.cu)
 void count_launch(int n = 1);

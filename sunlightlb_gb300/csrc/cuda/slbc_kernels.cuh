@@ -163,53 +163,89 @@ __device__ __forceinline__ void apply_wall(T (&t)[15], uint16_t fl, bool solid, 
 
 // One fused update step (bounce-back + streaming + collision) of every node.
 // ODD = false: C1 -> C0 (local), ODD = true: C0 -> C1 (pull and push).
-// Grid: (ceil(esk/blockDim.x), esj, esi).
-template <typename T, bool ODD, bool EXACT>
+// MOVING compiles the wall terms in, BFU selects a uniform body force (a
+// kernel constant) over per-node arrays, NPT is the number of rows along j
+// one thread updates (more memory requests in flight per thread).
+// Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT>
 __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, i = blockIdx.z;
+  const int i = blockIdx.z;
   const int esk = a.p.esk;
   if (k >= esk) return;
-  const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, esk);
-  const int x = nb.at(0, 0, 0);
-  const uint16_t fl = __ldg(a.p.flags + x);
-  const bool solid = (fl & FLAG_SOLID) != 0;
   T *__restrict__ P = a.p.pop;
   const long long S = a.p.npad;
-  T t[15];
-  if (!ODD) {
 #pragma unroll
-    for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
-  } else {
-    t[0] = P[x];
+  for (int r = 0; r < NPT; r++) {
+    const int j = blockIdx.y * NPT + r;
+    if (NPT > 1 && j >= a.p.esj) break;
+    const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, esk);
+    const int x = nb.at(0, 0, 0);
+    const uint16_t fl = __ldg(a.p.flags + x);
+    const bool solid = (fl & FLAG_SOLID) != 0;
+    T t[15];
+    if (!ODD) {
 #pragma unroll
-    for (int q = 1; q < 15; q++) {
-      const bool bnd = (fl >> q) & 1;
-      const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
-      const int slot = bnd ? q : OPP(q);
-      t[q] = P[slot * S + src];
+      for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
+    } else {
+      t[0] = P[x];
+#pragma unroll
+      for (int q = 1; q < 15; q++) {
+        const bool bnd = (fl >> q) & 1;
+        const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+        const int slot = bnd ? q : OPP(q);
+        t[q] = P[slot * S + src];
+      }
     }
-  }
-  if (a.moving && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
-  if (!(a.skip_solid && solid)) {
-    T bx = a.bfx, by = a.bfy, bz = a.bfz;
-    if (!a.bf_uniform) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
-    collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
-  }
-  if (!ODD) {
+    if (MOVING && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
+    if (!(a.skip_solid && solid)) {
+      T bx = a.bfx, by = a.bfy, bz = a.bfz;
+      if (!BFU) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
+      collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
+    }
+    if (!ODD) {
 #pragma unroll
-    for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
-  } else {
-    P[x] = t[0];
+      for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
+    } else {
+      P[x] = t[0];
 #pragma unroll
-    for (int q = 1; q < 15; q++) {
-      const bool bnd = (fl >> OPP(q)) & 1;
-      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
-      const int slot = bnd ? OPP(q) : q;
-      P[slot * S + dst] = t[q];
+      for (int q = 1; q < 15; q++) {
+        const bool bnd = (fl >> OPP(q)) & 1;
+        const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+        const int slot = bnd ? OPP(q) : q;
+        P[slot * S + dst] = t[q];
+      }
     }
   }
 }
+
+// Explicitly rounded add / multiply: never contracted into FMA, so the
+// reduction kernels give the same bits whatever -fmad a translation unit uses.
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+
+// Compensated accumulator: FP64 for FP64 data; for FP32 data a float-float
+// pair (Knuth's TwoSum keeps the rounding error of every addition), about 48
+// significant bits computed on the FP32 pipe, turned into FP64 once.
+template <typename T> struct Acc;
+template <> struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s = radd(s, x); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct Acc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float sum = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(sum, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bp)), __fsub_rn(x, bp));
+    hi = sum;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 // Post-collision population q of node x in a given layout (see slb_device.h).
 template <typename T>
@@ -236,22 +272,46 @@ __global__ void k_force(PopArgs<T> p, int layout, int moving, const T *uw, Force
   const uint16_t fl = p.flags[s];
   const T *P = p.pop;
   const long long S = p.npad;
-  double fx = f.f[e], fy = f.f[f.nbnd + e], fz = f.f[2 * f.nbnd + e];
-  double ux = 0.0, uy = 0.0, uz = 0.0;
-  if (moving) { ux = (double)uw[s]; uy = (double)uw[S + s]; uz = (double)uw[2 * S + s]; }
+  if (sizeof(T) == 8) {
+    // FP64 populations: the reference's arithmetic, in link order
+    double fx = f.f[e], fy = f.f[f.nbnd + e], fz = f.f[2 * f.nbnd + e];
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    if (moving) { ux = (double)uw[s]; uy = (double)uw[S + s]; uz = (double)uw[2 * S + s]; }
 #pragma unroll
-  for (int q = 1; q < 15; q++) {
-    if (!((fl >> OPP(q)) & 1)) continue;
-    const int n = nb.at(CX(q), CY(q), CZ(q));
-    double av, bv;
-    if (layout == SLBC_LAYOUT_N) { av = (double)P[q * S + s]; bv = (double)P[OPP(q) * S + n]; }
-    else { av = (double)P[OPP(q) * S + s]; bv = (double)P[q * S + n]; }
-    const double dp = moving ? 2.0 * (av - bv - link_term<double>(q, ux, uy, uz)) : 2.0 * (av - bv);
-    if (CX(q) > 0) fx += dp; else if (CX(q) < 0) fx -= dp;
-    if (CY(q) > 0) fy += dp; else if (CY(q) < 0) fy -= dp;
-    if (CZ(q) > 0) fz += dp; else if (CZ(q) < 0) fz -= dp;
+    for (int q = 1; q < 15; q++) {
+      if (!((fl >> OPP(q)) & 1)) continue;
+      const int n = nb.at(CX(q), CY(q), CZ(q));
+      double av, bv;
+      if (layout == SLBC_LAYOUT_N) { av = (double)P[q * S + s]; bv = (double)P[OPP(q) * S + n]; }
+      else { av = (double)P[OPP(q) * S + s]; bv = (double)P[q * S + n]; }
+      const double dp = moving ? 2.0 * (av - bv - link_term<double>(q, ux, uy, uz)) : 2.0 * (av - bv);
+      if (CX(q) > 0) fx += dp; else if (CX(q) < 0) fx -= dp;
+      if (CY(q) > 0) fy += dp; else if (CY(q) < 0) fy -= dp;
+      if (CZ(q) > 0) fz += dp; else if (CZ(q) < 0) fz -= dp;
+    }
+    f.f[e] = fx; f.f[f.nbnd + e] = fy; f.f[2 * f.nbnd + e] = fz;
+  } else {
+    // FP32 populations: link terms in FP32 (a - b and the wall term are
+    // exact-ish at these magnitudes), sums compensated, stored in FP64
+    Acc<float> ax, ay, az;
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    if (moving) { ux = (float)uw[s]; uy = (float)uw[S + s]; uz = (float)uw[2 * S + s]; }
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      if (!((fl >> OPP(q)) & 1)) continue;
+      const int n = nb.at(CX(q), CY(q), CZ(q));
+      float av, bv;
+      if (layout == SLBC_LAYOUT_N) { av = (float)P[q * S + s]; bv = (float)P[OPP(q) * S + n]; }
+      else { av = (float)P[OPP(q) * S + s]; bv = (float)P[q * S + n]; }
+      float dp = __fsub_rn(av, bv);
+      if (moving) dp = __fsub_rn(dp, link_term<float>(q, ux, uy, uz));
+      dp = __fmul_rn(2.f, dp);
+      if (CX(q) != 0) ax.add(CX(q) > 0 ? dp : -dp);
+      if (CY(q) != 0) ay.add(CY(q) > 0 ? dp : -dp);
+      if (CZ(q) != 0) az.add(CZ(q) > 0 ? dp : -dp);
+    }
+    f.f[e] += ax.value(); f.f[f.nbnd + e] += ay.value(); f.f[2 * f.nbnd + e] += az.value();
   }
-  f.f[e] = fx; f.f[f.nbnd + e] = fy; f.f[2 * f.nbnd + e] = fz;
 }
 
 // Deterministic block reduction of NV doubles; thread 0 gets the totals.
@@ -281,18 +341,23 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
 // Velocity sums of accvmean (reference src/lbmeasure.c:78-97) per block:
 // block b reduces the contiguous node range [b*chunk, (b+1)*chunk), its
 // threads striding through it; the fixed partition makes the sums
-// deterministic.
+// deterministic.  The per-node velocity is formed in the population type
+// (FP64: one reciprocal of rho instead of three divisions) and accumulated
+// in FP64.
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads)
 k_vsum(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double b0, double b1,
        double b2, const T *bf, const double *psi, double *partials) {
-  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  Acc<T> ax, ay, az;
+  double wsum = 0.0;
+  int count = 0;
   const long long n = (long long)p.esi * p.esj * p.esk;
   const long long chunk = (n + gridDim.x - 1) / gridDim.x;
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = lo + chunk < n ? lo + chunk : n;
   const T *P = p.pop;
   const long long S = p.npad;
+  const T r0 = (T)rho0, tf = (T)fac;
   for (long long e = lo + threadIdx.x; e < hi; e += blockDim.x) {
     const int x = (int)e;
     const uint16_t fl = p.flags[x];
@@ -300,24 +365,49 @@ k_vsum(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double
     int i, j, k;
     decode(x, p.esj, p.esk, i, j, k);
     const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
-    double t[15];
+    T t[15];
 #pragma unroll
-    for (int q = 0; q < 15; q++) t[q] = (double)post_value<T>(P, S, layout, q, x, fl, nb);
-    double bx = b0, by = b1, bz = b2;
-    if (!bf_uniform) { bx = (double)bf[x]; by = (double)bf[S + x]; bz = (double)bf[2 * S + x]; }
-    const double rho = rho0 + t[0] + t[1] + t[2] + t[3] + t[4] + t[5] + t[6] + t[7] + t[8] +
-                       t[9] + t[10] + t[11] + t[12] + t[13] + t[14];
-    const double ux = (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14] + fac * bx) / rho;
-    const double uy = (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14] + fac * by) / rho;
-    const double uz = (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14] + fac * bz) / rho;
-    double w = 1.0;
-    if (psi) { w = psi[x]; w = w * w; }
-    v[0] += w * ux; v[1] += w * uy; v[2] += w * uz; v[3] += w; v[4] += 1.0;
+    for (int q = 0; q < 15; q++) t[q] = post_value<T>(P, S, layout, q, x, fl, nb);
+    T bx = (T)b0, by = (T)b1, bz = (T)b2;
+    if (!bf_uniform) { bx = bf[x]; by = bf[S + x]; bz = bf[2 * S + x]; }
+    T rho = r0, nx, ny, nz;
+#pragma unroll
+    for (int q = 0; q < 15; q++) rho = radd(rho, t[q]);
+    nx = radd(radd(radd(radd(radd(radd(radd(radd(radd(radd(t[1], -t[2]), t[7]), -t[8]), t[9]), -t[10]), t[11]), -t[12]), t[13]), -t[14]), rmul(tf, bx));
+    ny = radd(radd(radd(radd(radd(radd(radd(radd(radd(radd(t[3], -t[4]), t[7]), t[8]), -t[9]), -t[10]), t[11]), t[12]), -t[13]), -t[14]), rmul(tf, by));
+    nz = radd(radd(radd(radd(radd(radd(radd(radd(radd(radd(t[5], -t[6]), t[7]), t[8]), t[9]), t[10]), -t[11]), -t[12]), -t[13]), -t[14]), rmul(tf, bz));
+    const T rinv = T(1) / rho;
+    T ux = rmul(nx, rinv), uy = rmul(ny, rinv), uz = rmul(nz, rinv);
+    if (psi) {
+      const double w = rmul(psi[x], psi[x]);
+      ax.add((T)rmul(w, (double)ux)); ay.add((T)rmul(w, (double)uy)); az.add((T)rmul(w, (double)uz));
+      wsum = radd(wsum, w);
+    } else {
+      ax.add(ux); ay.add(uy); az.add(uz);
+    }
+    count++;
   }
+  double v[5] = {ax.value(), ay.value(), az.value(), psi ? wsum : (double)count, (double)count};
   block_sum<5>(v);
   if (threadIdx.x == 0)
 #pragma unroll
     for (int c = 0; c < 5; c++) partials[5 * blockIdx.x + c] = v[c];
+}
+
+// Final sum of nb partial records of NV doubles in one block: each thread
+// adds a fixed strided subset in order, then a fixed-shape tree.
+template <int NV>
+__global__ void __launch_bounds__(256) k_final_sum_tree(const double *partials, int nb, double *out) {
+  double v[NV];
+#pragma unroll
+  for (int c = 0; c < NV; c++) v[c] = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < NV; c++) v[c] += partials[NV * b + c];
+  block_sum<NV>(v);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int c = 0; c < NV; c++) out[c] = v[c];
 }
 
 // Host AoS staging (FP64, a[15*x + q]) -> layout N.

@@ -46,11 +46,36 @@ static dim3 row_grid(const Lattice &L, int bx) {
 
 static int flat_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+template <bool ODD, bool MOVING, bool BFU>
+static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
+  const dim3 grid((unsigned)((L.esk + bx - 1) / bx), (unsigned)((L.esj + npt - 1) / npt), (unsigned)L.esi);
+  if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2><<<grid, bx, 0, L.stream>>>(a);
+  else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1><<<grid, bx, 0, L.stream>>>(a);
+}
+
+template <bool ODD>
+static void step_dispatch(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
+  if (a.moving) {
+    if (a.bf_uniform) step_variant<ODD, true, true>(L, a, npt, bx);
+    else step_variant<ODD, true, false>(L, a, npt, bx);
+  } else {
+    if (a.bf_uniform) step_variant<ODD, false, true>(L, a, npt, bx);
+    else step_variant<ODD, false, false>(L, a, npt, bx);
+  }
+}
+
+// One fused step with the tuned (rows per thread, threads along k) of this
+// parity; small lattices use one row per thread and the block width that
+// fits esk.
 cudaError_t SLBC_FN(launch_step)(Lattice &L, int odd) {
-  const int bx = L.esk >= L.block_k ? L.block_k : (L.esk >= 64 ? 64 : 32);
+  const StepConfig &c = L.tuned[odd ? 1 : 0];
+  int bx = c.block_k, npt = c.npt;
+  if (bx <= 0) { bx = 128; npt = 1; }
+  while (bx > 32 && bx / 2 >= L.esk) bx /= 2;
+  if (L.esj < 2) npt = 1;
   StepArgs<T_> a = step_args(L);
-  if (odd) k_step<T_, true, SLBC_EXACT><<<row_grid(L, bx), bx, 0, L.stream>>>(a);
-  else k_step<T_, false, SLBC_EXACT><<<row_grid(L, bx), bx, 0, L.stream>>>(a);
+  if (odd) step_dispatch<true>(L, a, npt, bx);
+  else step_dispatch<false>(L, a, npt, bx);
   count_launch();
   return cudaGetLastError();
 }

@@ -32,14 +32,6 @@ static __device__ __align__(256) double g_vsum_scratch[5 * kMaxBlocks];
 void *g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_lock;
 
-__global__ void k_vsum_final(const double *partials, int n, double *out) {
-  const int c = threadIdx.x;
-  if (c >= 5) return;
-  double s = 0.0;
-  for (int b = 0; b < n; b++) s += partials[5 * b + c];
-  out[c] = s;
-}
-
 int scratch_for_current_device(double **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -80,7 +72,7 @@ cudaError_t launch(const void *pop, long long npad, int layout, const unsigned s
   slbc::count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_vsum_final<<<1, 32, 0, st>>>(scratch, nblocks, out);
+  slbc::k_final_sum_tree<5><<<1, 256, 0, st>>>(scratch, nblocks, out);
   slbc::count_launch();
   return cudaGetLastError();
 }

@@ -284,8 +284,8 @@ slbc_lattice *slb_device(LBSys lb) {
     st->a_gen++;
   }
   if (st->dev == NULL) {
-    if (lb->precision != SLB_FP64 && lb->precision != SLB_FP32)
-      error("lb->precision must be SLB_FP64 or SLB_FP32");
+    if (lb->precision != SLB_FP64 && lb->precision != SLB_FP32 && lb->precision != SLB_BF16)
+      error("lb->precision must be SLB_FP64, SLB_FP32 or SLB_BF16");
     slb_check(slbc_create(&st->dev, lb->esi, lb->esj, lb->esk, lb->precision), "device set-up");
     st->dev_precision = lb->precision;
     st->geom_sent = st->ads_sent = st->bf_sent = st->uw_sent = 0;
@@ -333,6 +333,14 @@ void lbpull(LBSys lb) {
   slb_pull_rho(lb);
 }
 
+/* Deviation storage keeps post-collision states only: a separate bounce-back
+ * or propagation phase, or a tracer step, moves the lattice to FP32 first. */
+void slb_need_populations(LBSys lb, const char *what) {
+  if (lb->precision != SLB_BF16) return;
+  printf("%s needs stored populations: lb->precision changed from SLB_BF16 to SLB_FP32\n", what);
+  lb->precision = SLB_FP32;
+}
+
 void slb_pull_rho(LBSys lb) {
   slb_priv *st = slb_state(lb);
   if (st->dev == NULL || lb->rho == NULL || st->host_rho_valid) return;
@@ -366,6 +374,11 @@ void lbsetstream(LBSys lb, void *stream) {
   slb_check(slbc_set_stream(slb_device(lb), stream), "stream change");
 }
 long lbkernelcount(void) { return slbc_launch_count(); }
+int lbtuning(LBSys lb, int *cfg) {
+  slb_priv *st = slb_state(lb);
+  if (st->dev == NULL) { cfg[0] = cfg[1] = cfg[2] = cfg[3] = 0; return 0; }
+  return slbc_get_tuning(st->dev, cfg);
+}
 
 /* ---- printing and bookkeeping (reference src/lbmisc.c:156-412) ---------- */
 
@@ -392,12 +405,13 @@ void wrpars(LBSys lb) {
   for (x = 0; x < lb->nnodes; x++)
     if (lb->obj[x] == NULL) { fxs += lb->bx[x]; fys += lb->by[x]; fzs += lb->bz[x]; nfluid++; }
   nu = (lb->tau - 0.5) / 3.0; eta = lb->rho0 * nu;
-  msize = (15.0 * (lb->precision == SLB_FP32 ? 4 : 8) + 2.0) * lb->nnodes;
+  msize = (lb->precision == SLB_BF16 ? 15.0 * 2 + 32.0 : 15.0 * (lb->precision == SLB_FP32 ? 4 : 8)) * lb->nnodes + 2.0 * lb->nnodes;
   printf("---------------------------------------------------\n");
   printf(" Operating parameters\n");
   printf("---------------------------------------------------\n");
   printf(" LB size = %i * %i * %i = %i\n", lb->esi, lb->esj, lb->esk, lb->nnodes);
-  printf(" Using %s precision populations on the GPU\n", lb->precision == SLB_FP32 ? "single" : "double");
+  printf(" Using %s populations on the GPU\n", lb->precision == SLB_FP32 ? "single precision" :
+         lb->precision == SLB_BF16 ? "BF16 deviation (FP32 moments)" : "double precision");
   printf(" Device memory requirement approx %0.2f MByte\n", msize / (1024.0 * 1024.0));
   printf(" rho0 = %0.4f\n", lb->rho0);
   printf(" tau, nu, eta = %0.4f %0.4f %0.4f\n", lb->tau, nu, eta);

@@ -119,6 +119,7 @@ void mpstep(MPSys mp) {
   slbc_tracer *t;
   double *state = NULL;
   int nobj = 0;
+  slb_need_populations(mp->lb, "Moment propagation");
   if (mp->to_be_initialised) mpinit(mp);
   t = tracer(mp);
   if (mp->lb->status != POST_COLLIDE) {

@@ -53,5 +53,6 @@ void slb_forces_changed(LBSys lb);
 long slb_node(LBSys lb, int i, int j, int k);
 void slb_trace(LBSys lb, const char *what);
 void slb_pull_rho(LBSys lb);
+void slb_need_populations(LBSys lb, const char *what);
 
 #endif

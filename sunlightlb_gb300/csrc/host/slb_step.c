@@ -24,6 +24,7 @@ static void after_collide(LBSys lb) {
 /* reference src/lbkernel.c:35-45: bounce-back as a separate phase */
 static void bounce(LBSys lb, int with_force) {
   slbc_lattice *d;
+  slb_need_populations(lb, "A separate bounce-back phase");
   if (lb->changed_objects) syncobjs(lb);
   d = slb_device(lb);
   if (lb->status != POST_COLLIDE) out_of_position(lb, "Bounceback");
@@ -45,7 +46,9 @@ void bblforce(LBSys lb) {
 
 /* reference src/lbkernel.c:623-762 */
 void propagate(LBSys lb) {
-  slbc_lattice *d = slb_device(lb);
+  slbc_lattice *d;
+  slb_need_populations(lb, "A separate propagation phase");
+  d = slb_device(lb);
   if (lb->status != POST_BBL) out_of_position(lb, "Propagation");
   slb_check(slbc_propagate(d), "propagation");
   slb_device_changed(lb);
