@@ -88,7 +88,9 @@ int slbc_put_pops(slbc_lattice *h, const double *a);
 int slbc_get_pops(slbc_lattice *h, double *a);
 int slbc_layout(slbc_lattice *h);
 /* Launch shape of the fused step per parity, cfg = {even rows per thread,
- * even threads along k, odd rows per thread, odd threads along k}.  The
+ * even threads along k, odd rows per thread, odd threads along k}; for BF16
+ * lattices the "rows per thread" entries are planes per block (1..64) and
+ * threads along k is 32.  The
  * first slbc_step of a lattice of 2^20 nodes or more times the candidate
  * shapes on a copy of the populations and keeps the fastest (environment
  * SLB_AUTOTUNE=0 turns this off); get returns 1 tuned, -1 defaults, 0 not

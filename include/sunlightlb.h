@@ -301,7 +301,8 @@ void lbsetstream(LBSys, void *);
 long lbkernelcount(void);
 /* Launch shape the autotuner chose for the fused step of lb, cfg[4] = {even
  * rows per thread, even threads along k, odd rows per thread, odd threads
- * along k}; returns 1 tuned, -1 defaults, 0 not decided yet. */
+ * along k} (BF16 lattices: planes per block in place of rows per thread);
+ * returns 1 tuned, -1 defaults, 0 not decided yet. */
 int lbtuning(LBSys, int *);
 /* Release every host and device resource of mp. */
 void freemp(MPSys);

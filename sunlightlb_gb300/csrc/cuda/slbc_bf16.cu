@@ -72,61 +72,131 @@ __device__ __forceinline__ float bf_post(const Bf16Args &a, int layout, int q, i
 
 // The fused step of k_step for deviation storage (same pull rule, same AA
 // layouts); also writes the new moments.
+//
+// Every population is reconstructed with the moments of the node that
+// produced it, so a node reads the moments of its 14 neighbours.  A block of
+// 32 (k) x 8 (j) threads marches along i over `planes` planes and keeps the
+// moments of three consecutive planes, with a one-node halo, in shared
+// memory; the plane after next is fetched into registers while the current
+// one is updated.  Moments then cross L2 about 1.7 times per node instead of
+// 15 times.
+constexpr int kTileK = 32, kTileJ = 8;
+constexpr int kHaloK = kTileK + 2, kHaloJ = kTileJ + 2;
+constexpr int kPlane = kHaloK * kHaloJ;                 // float4 per plane
+constexpr int kTileThreads = kTileK * kTileJ;
+constexpr int kPlaneLoads = (kPlane + kTileThreads - 1) / kTileThreads;
+
+__device__ __forceinline__ int wrap_index(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
 template <bool ODD, bool MOVING, bool BFU>
-__global__ void __launch_bounds__(256) k_step_bf16(Bf16Args a, StepArgs<float> s) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y, i = blockIdx.z;
-  if (k >= a.esk) return;
-  const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
-  const int x = nb.at(0, 0, 0);
-  const uint16_t fl = __ldg(a.flags + x);
-  const bool solid = (fl & FLAG_SOLID) != 0;
-  const float4 mx = __ldg(a.Min + x);
-  float t[15];
-  t[0] = eq_pop(0, mx) + dev_load(a, 0, x);
+__global__ void __launch_bounds__(kTileThreads, 4) k_step_bf16(Bf16Args a, StepArgs<float> s, int planes) {
+  __shared__ float4 ring[3][kPlane];
+  const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
+  const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
+  const int np = min(planes, a.esi - i0);
+  const int plane_nodes = a.esj * a.esk;
+  // offsets within a plane of this thread's share of the halo tile (wrapped)
+  int off[kPlaneLoads];
 #pragma unroll
-  for (int q = 1; q < 15; q++) {
-    const bool bnd = (fl >> q) & 1;
-    if (bnd) {
-      // own post-collision opp(q): slot q of x in both C0 and C1
-      t[q] = eq_pop(OPP(q), mx) + dev_load(a, q, x);
-    } else {
-      const int y = nb.at(-CX(q), -CY(q), -CZ(q));
-      const float4 my = __ldg(a.Min + y);
-      t[q] = eq_pop(q, my) + (ODD ? dev_load(a, OPP(q), y) : dev_load(a, q, x));
-    }
+  for (int e = 0; e < kPlaneLoads; e++) {
+    const int c = tid + kTileThreads * e;
+    off[e] = c < kPlane ? wrap_index(j0 - 1 + c / kHaloK, a.esj) * a.esk + wrap_index(k0 - 1 + c % kHaloK, a.esk)
+                        : -1;
   }
-  if (MOVING && (fl & FLAG_LINKS)) apply_wall<float>(t, fl, solid, nb, x, s.uw, s.p.npad);
-  float4 mo;
-  if (!(s.skip_solid && solid)) {
-    float bx = s.bfx, by = s.bfy, bz = s.bfz;
-    if (!BFU) { bx = s.bf[x]; by = s.bf[s.p.npad + x]; bz = s.bf[2 * s.p.npad + x]; }
-    collide<float, false>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
+  // plane p sits in ring slot (p - i0 + 1) % 3
+  float4 pre[kPlaneLoads];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int base = wrap_index(i0 - 1 + h, a.esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = __ldg(a.Min + base + off[e]);
   }
-  // moments of the post-collision populations (the collision conserves drho
-  // and sets ru; summing keeps skipped solid nodes exact too)
   {
-    const float p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
-    const float lo = t[7] + t[8] + t[9] + t[10], hi = t[11] + t[12] + t[13] + t[14];
-    mo.x = t[0] + p12 + p34 + p56 + lo + hi;
-    mo.y = t[1] - t[2] + (t[7] - t[8] + t[9] - t[10]) + (t[11] - t[12] + t[13] - t[14]);
-    mo.z = t[3] - t[4] + (t[7] + t[8] - t[9] - t[10]) + (t[11] + t[12] - t[13] - t[14]);
-    mo.w = t[5] - t[6] + lo - hi;
-  }
-  a.Mout[x] = mo;
-  const long long S = a.npad;
-  if (!ODD) {
+    const int base = wrap_index(i0 + 1, a.esi) * plane_nodes;
 #pragma unroll
-    for (int q = 0; q < 15; q++)
-      a.D[OPP(q) * S + x] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
-  } else {
-    a.D[x] = __float2bfloat16_rn((t[0] - eq_pop(0, mo)) * a.scale);
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) pre[e] = __ldg(a.Min + base + off[e]);
+  }
+  const long long S = a.npad;
+  for (int ii = 0; ii < np; ii++) {
+    const int i = i0 + ii;
+    const int sm = ii % 3, s0 = (ii + 1) % 3, sp = (ii + 2) % 3;  // planes i-1, i, i+1
+    __syncthreads();  // slot sp held plane i-2, last read in the previous iteration
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[sp][tid + kTileThreads * e] = pre[e];
+    __syncthreads();
+    if (ii + 1 < np) {
+      const int base = wrap_index(i + 2, a.esi) * plane_nodes;
+#pragma unroll
+      for (int e = 0; e < kPlaneLoads; e++)
+        if (off[e] >= 0) pre[e] = __ldg(a.Min + base + off[e]);
+    }
+    const int j = j0 + tj, k = k0 + tk;
+    if (j >= a.esj || k >= a.esk) continue;
+    const float4 *P[3] = {ring[sm], ring[s0], ring[sp]};
+    const int c0 = (tj + 1) * kHaloK + tk + 1;
+    const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
+    const int x = nb.at(0, 0, 0);
+    const uint16_t fl = __ldg(a.flags + x);
+    const bool solid = (fl & FLAG_SOLID) != 0;
+    const float4 mx = P[1][c0];
+    // Branch-free selection of each population's cell and producer moments,
+    // so that all 15 loads are in flight together.  A bounce-back link
+    // (bit q) returns the node's own post-collision opp(q), held in slot q
+    // of x in both C0 and C1; its equilibrium eq_opp(q)(m) is eq_q of m with
+    // the momentum negated (exact: only signs change).  Otherwise the
+    // population was produced by y = x - c_q.
+    const float4 mneg = make_float4(mx.x, -mx.y, -mx.z, -mx.w);
+    float t[15];
+    t[0] = eq_pop(0, mx) + dev_load(a, 0, x);
 #pragma unroll
     for (int q = 1; q < 15; q++) {
-      const bool bnd = (fl >> OPP(q)) & 1;
-      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
-      const int slot = bnd ? OPP(q) : q;
-      a.D[slot * S + dst] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
+      const bool bnd = (fl >> q) & 1;
+      const float4 my = P[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
+      const float4 m = bnd ? mneg : my;
+      int src = x, slot = q;
+      if (ODD) {
+        src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+        slot = bnd ? q : OPP(q);
+      }
+      t[q] = eq_pop(q, m) + dev_load(a, slot, src);
+    }
+    if (MOVING && (fl & FLAG_LINKS)) apply_wall<float>(t, fl, solid, nb, x, s.uw, s.p.npad);
+    if (!(s.skip_solid && solid)) {
+      float bx = s.bfx, by = s.bfy, bz = s.bfz;
+      if (!BFU) { bx = s.bf[x]; by = s.bf[s.p.npad + x]; bz = s.bf[2 * s.p.npad + x]; }
+      collide<float, false>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
+    }
+    // moments of the post-collision populations (the collision conserves
+    // drho and sets ru; summing keeps skipped solid nodes exact too)
+    float4 mo;
+    {
+      const float p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
+      const float lo = t[7] + t[8] + t[9] + t[10], hi = t[11] + t[12] + t[13] + t[14];
+      mo.x = t[0] + p12 + p34 + p56 + lo + hi;
+      mo.y = t[1] - t[2] + (t[7] - t[8] + t[9] - t[10]) + (t[11] - t[12] + t[13] - t[14]);
+      mo.z = t[3] - t[4] + (t[7] + t[8] - t[9] - t[10]) + (t[11] + t[12] - t[13] - t[14]);
+      mo.w = t[5] - t[6] + lo - hi;
+    }
+    a.Mout[x] = mo;
+    if (!ODD) {
+#pragma unroll
+      for (int q = 0; q < 15; q++)
+        a.D[OPP(q) * S + x] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
+    } else {
+      a.D[x] = __float2bfloat16_rn((t[0] - eq_pop(0, mo)) * a.scale);
+#pragma unroll
+      for (int q = 1; q < 15; q++) {
+        const bool bnd = (fl >> OPP(q)) & 1;
+        const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+        const int slot = bnd ? OPP(q) : q;
+        a.D[slot * S + dst] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
+      }
     }
   }
 }
@@ -344,25 +414,35 @@ static StepArgs<float> step_args_f(Lattice &L) {
 static int fblocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 template <bool ODD>
-static void bf_step(Lattice &L, const Bf16Args &a, const StepArgs<float> &s, dim3 g, int bx) {
+static void bf_step(Lattice &L, const Bf16Args &a, const StepArgs<float> &s, dim3 g, int planes) {
+  const dim3 b(kTileK, kTileJ);
   if (s.moving) {
-    if (s.bf_uniform) k_step_bf16<ODD, true, true><<<g, bx, 0, L.stream>>>(a, s);
-    else k_step_bf16<ODD, true, false><<<g, bx, 0, L.stream>>>(a, s);
+    if (s.bf_uniform) k_step_bf16<ODD, true, true><<<g, b, 0, L.stream>>>(a, s, planes);
+    else k_step_bf16<ODD, true, false><<<g, b, 0, L.stream>>>(a, s, planes);
   } else {
-    if (s.bf_uniform) k_step_bf16<ODD, false, true><<<g, bx, 0, L.stream>>>(a, s);
-    else k_step_bf16<ODD, false, false><<<g, bx, 0, L.stream>>>(a, s);
+    if (s.bf_uniform) k_step_bf16<ODD, false, true><<<g, b, 0, L.stream>>>(a, s, planes);
+    else k_step_bf16<ODD, false, false><<<g, b, 0, L.stream>>>(a, s, planes);
   }
 }
 
+// planes per block: the tuned value (npt field of the parity's StepConfig),
+// else the largest of 1..8 that still gives about four blocks per SM
+int bf16_default_planes(const Lattice &L) {
+  const long long tiles = (long long)((L.esk + kTileK - 1) / kTileK) * ((L.esj + kTileJ - 1) / kTileJ);
+  int p = 8;
+  while (p > 1 && tiles * ((L.esi + p - 1) / p) < 152 * 4) p /= 2;
+  return p;
+}
+
 cudaError_t launch_step_bf16(Lattice &L, int odd) {
-  int bx = L.tuned[odd ? 1 : 0].block_k;
-  if (bx <= 0) bx = 128;
-  while (bx > 32 && bx / 2 >= L.esk) bx /= 2;
-  const dim3 g((unsigned)((L.esk + bx - 1) / bx), (unsigned)L.esj, (unsigned)L.esi);
+  int planes = L.tuned[odd ? 1 : 0].npt;
+  if (planes <= 0) planes = bf16_default_planes(L);
+  const dim3 g((unsigned)((L.esk + kTileK - 1) / kTileK), (unsigned)((L.esj + kTileJ - 1) / kTileJ),
+               (unsigned)((L.esi + planes - 1) / planes));
   const Bf16Args a = bf_args(L);
   const StepArgs<float> s = step_args_f(L);
-  if (odd) bf_step<true>(L, a, s, g, bx);
-  else bf_step<false>(L, a, s, g, bx);
+  if (odd) bf_step<true>(L, a, s, g, planes);
+  else bf_step<false>(L, a, s, g, planes);
   count_launch();
   L.mom_cur = 1 - L.mom_cur;
   return cudaGetLastError();

@@ -285,10 +285,17 @@ int one_step(Lattice &L) {
 // the lattice's own state is not touched -- and keep the fastest.  Lattices
 // below 2^20 nodes use the default shape; SLB_AUTOTUNE=0 disables tuning.
 int autotune(Lattice &L) {
-  static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
-  const int ncand = (int)(sizeof cand / sizeof cand[0]);
+  // FP64/FP32: {rows per thread, threads along k}; BF16: {planes per block, 32}
+  static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
+  static const int cand_bf[][2] = {{1, 32}, {2, 32}, {4, 32}, {8, 32}, {16, 32}};
+  const bool bf = L.precision == 2;
+  const int (*cand)[2] = bf ? cand_bf : cand_fp;
+  const int ncand = bf ? 5 : 6;
   const char *env = getenv("SLB_AUTOTUNE");
-  for (int p = 0; p < 2; p++) { L.tuned[p].npt = 1; L.tuned[p].block_k = 128; }
+  for (int p = 0; p < 2; p++) {
+    L.tuned[p].npt = bf ? bf16_default_planes(L) : 1;
+    L.tuned[p].block_k = bf ? 32 : 128;
+  }
   if ((env && env[0] == '0') || L.nnodes < (1LL << 20) || L.esk < 64) {
     L.tune_state = -1;
     return 0;
@@ -297,6 +304,18 @@ int autotune(Lattice &L) {
   const size_t bytes = 15 * (size_t)L.npad * elem_size(L.precision);
   CK(cudaMemcpyAsync(L.scratch, L.pop, bytes, cudaMemcpyDeviceToDevice, L.stream));
   std::swap(L.pop, L.scratch);  // kernels below run on the copy
+  // BF16 steps also write moments: run them on a copy of those too
+  void *mom_saved[2] = {L.mom[0], L.mom[1]};
+  const int mom_cur_saved = L.mom_cur;
+  void *mom_tmp = nullptr;
+  if (bf) {
+    CK(cudaMalloc(&mom_tmp, 2 * sizeof(float4) * (size_t)L.npad));
+    CK(cudaMemcpyAsync(mom_tmp, L.mom[L.mom_cur], sizeof(float4) * (size_t)L.npad, cudaMemcpyDeviceToDevice,
+                       L.stream));
+    L.mom[0] = mom_tmp;
+    L.mom[1] = (char *)mom_tmp + sizeof(float4) * (size_t)L.npad;
+    L.mom_cur = 0;
+  }
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -326,6 +345,13 @@ int autotune(Lattice &L) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   std::swap(L.pop, L.scratch);
+  if (bf) {
+    cudaStreamSynchronize(L.stream);
+    cudaFree(mom_tmp);
+    L.mom[0] = mom_saved[0];
+    L.mom[1] = mom_saved[1];
+    L.mom_cur = mom_cur_saved;
+  }
   if (rc) return fail_msg("autotune: a candidate launch failed");
   L.tune_state = 1;
   L.generation++;
@@ -464,8 +490,12 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
   Lattice &L = h->L;
   for (int p = 0; p < 2; p++) {
     const int npt = cfg[2 * p], bx = cfg[2 * p + 1];
-    if ((npt != 1 && npt != 2) || (bx != 32 && bx != 64 && bx != 128 && bx != 256))
+    if (L.precision == 2) {
+      if (npt < 1 || npt > 64 || bx != 32)
+        return fail_msg("slbc_set_tuning: BF16 lattices take 1 to 64 planes per block and 32 threads along k");
+    } else if ((npt != 1 && npt != 2) || (bx != 32 && bx != 64 && bx != 128 && bx != 256)) {
       return fail_msg("slbc_set_tuning: rows per thread must be 1 or 2 and threads along k 32, 64, 128 or 256");
+    }
     L.tuned[p].npt = npt;
     L.tuned[p].block_k = bx;
   }

@@ -160,6 +160,7 @@ SLBC_DECLARE_LAUNCHERS(f32)
 
 // BF16 deviation storage (slbc_bf16.cu): the operations it supports
 cudaError_t launch_step_bf16(Lattice &L, int odd);
+int bf16_default_planes(const Lattice &L);
 cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n);
 cudaError_t launch_get_bf16(Lattice &L, double *stage, long long x0, long long n);
 cudaError_t launch_swap_bf16(Lattice &L);
