@@ -442,6 +442,135 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---- flow + passive scalar in a large packed bed ----------------------------
+
+TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED = 0.35, 6.0, 12.0, 4
+TRACER_ALPHA, TRACER_ADPROB = 0.5, 0.01
+# bytes per tracer update: 15 FP32 populations + p in, rho, p out
+TRACER_BYTES = {1: 60 + 3 * 4, 0: 60 + 3 * 8}
+
+
+def time_tracer(torch, L, lb, mp, steps):
+    """Device time (ms) of `steps` mpstep calls, CUDA events on the
+    lattice's stream."""
+    stream = torch.cuda.ExternalStream(L.lbgetstream(lb))
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        for _ in range(steps):
+            L.mpstep(mp)
+        b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b)
+
+
+def cpu_tracer_baseline(budget_s):
+    """The oracle's FP64 tracer update (restatement of the reference's
+    mpstep) on one host core, on a 64^3 crop of the same kind of packing."""
+    from sunlightlb_gb300 import workloads as W
+    L = oracle_lib()
+    lb, _ = W.large_bed(L, 64, TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED, precision=0)
+    L.addbf(lb, 1e-5, 0.0, 0.0)
+    for _ in range(20):
+        L.lbstep(lb)
+    mp = L.newmp(lb, "null")
+    mp.alpha = TRACER_ALPHA
+    mp.adprob = TRACER_ADPROB
+    L.mpinit(mp)
+    L.adall(mp)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        L.mpwall(mp, "x", 0, 1.0)
+        L.mpstep(mp)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(lb.nnodes * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+            "sample": f"{steps} FP64 tracer updates (with the source plane) of a 64^3 packing of the same kind"}
+
+
+def run_tracer(args):
+    """Large packed bed, flow at pore Reynolds number about 1, then a passive
+    scalar with partial adsorption carried through the frozen flow."""
+    import torch
+    import sunlightlb_gb300
+    from sunlightlb_gb300 import workloads as W
+
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    L = sunlightlb_gb300.library()
+    n = args.side
+    t0 = time.perf_counter()
+    lb, spheres = W.large_bed(L, n, TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED, precision=1)
+    t_build = time.perf_counter() - t0
+    diameter = 2.0 * statistics.mean(r for r, _, _, _ in spheres)
+    nodes = lb.nnodes
+    L.lbsteps(lb, 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    flow = W.calibrated_flow(L, lb, diameter, re_target=1.0, maxsteps=args.max_converge_steps)
+    torch.cuda.synchronize()
+    flow["wall_s"] = round(time.perf_counter() - t0, 2)
+    flow["fluid_fraction"] = L.countfluid(lb) / nodes
+    peak, peak_kind = measured_peak()
+    with Clocks(local) as clk:
+        ms = time_steps(torch, L, lb, 60, 3)
+    step_ms = statistics.mean(ms)
+    flow_kernel = {"MLUPS": round(nodes / (step_ms * 1e-3) / 1e6, 1), "ms_per_step": round(step_ms, 4),
+                   "hbm_gbs": round(BYTES_PER_UPDATE[1] * nodes / (step_ms * 1e-3) / 1e9, 1),
+                   "frac_of_measured_hbm": round(BYTES_PER_UPDATE[1] * nodes / (step_ms * 1e-3) / 1e9 / peak, 4),
+                   "bytes_per_update": BYTES_PER_UPDATE[1], "clocks": clk.summary()}
+    tracers = {}
+    for name, prec, nsteps in (("fp32", 1, args.tracer_steps), ("fp64", 0, args.fp64_tracer_steps)):
+        if nsteps <= 0:
+            continue
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mp, curve, bal = W.tracer_breakthrough(L, lb, nsteps, precision=prec, alpha=TRACER_ALPHA,
+                                               adprob=TRACER_ADPROB, sample_every=args.sample_every)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        kms = time_tracer(torch, L, lb, mp, 50) / 50
+        gbs = TRACER_BYTES[prec] * nodes / (kms * 1e-3) / 1e9
+        tracers[name] = {
+            "steps": nsteps, "wall_s": round(wall, 2),
+            "MLUPS_with_source_and_samples": round(nodes * nsteps / wall / 1e6, 1),
+            "kernel": {"MLUPS": round(nodes / (kms * 1e-3) / 1e6, 1), "ms_per_step": round(kms, 4),
+                       "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
+                       "bytes_per_update": TRACER_BYTES[prec]},
+            "balance": bal,
+            "balance_rel_error": (bal["all"] - bal["injected"]) / bal["injected"] if bal["injected"] else None,
+            "breakthrough": curve,
+        }
+        L.freemp(mp)
+    if "fp32" in tracers and "fp64" in tracers:
+        c32 = dict(tracers["fp32"]["breakthrough"])
+        c64 = dict(tracers["fp64"]["breakthrough"])
+        common = sorted(set(c32) & set(c64))
+        tracers["fp32_vs_fp64"] = {
+            "breakthrough_max_abs_diff": max(abs(c32[s] - c64[s]) for s in common) if common else None,
+            "adsorbed_rel_diff": abs(tracers["fp32"]["balance"]["adsorbed"] - tracers["fp64"]["balance"]["adsorbed"])
+            / max(abs(tracers["fp64"]["balance"]["adsorbed"]), 1e-300)
+            if tracers["fp32"]["steps"] == tracers["fp64"]["steps"] else None}
+    line = {
+        "workload": f"flow and passive scalar, periodic {n}^3 packed bed",
+        "metric": "MLUPS of the flow and tracer kernels; breakthrough and tracer mass balance",
+        "config": {"lattice": [n, n, n], "solid_fraction_target": TRACER_PHI,
+                   "radii": [TRACER_RMIN, TRACER_RMAX], "seed": TRACER_SEED, "spheres": len(spheres),
+                   "mean_diameter": diameter, "tau": 1.0, "flow": "Navier-Stokes (stokes_flow = 0), FP32 populations",
+                   "tracer_alpha": TRACER_ALPHA, "adsorption_probability": TRACER_ADPROB,
+                   "source": "mpwall x = 0, p = 1, re-set before every update"},
+        "build_s": round(t_build, 1), "flow": flow, "flow_kernel": flow_kernel, "tracer": tracers,
+        "measured_peak_gbs": peak, "peak_kind": peak_kind,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_tracer_baseline(args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    L.freelb(lb)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -455,11 +584,19 @@ def main():
     ap.add_argument("--max-converge-steps", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="packed", choices=["packed", "tracer"],
+                    help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive scalar")
+    ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")
+    ap.add_argument("--tracer-steps", type=int, default=50000)
+    ap.add_argument("--fp64-tracer-steps", type=int, default=50000)
+    ap.add_argument("--sample-every", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "tracer":
+        run_tracer(args)
     else:
         run_mine(args)
 

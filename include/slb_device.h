@@ -162,6 +162,15 @@ int slbc_mp_minmax(slbc_tracer *t, double out[2]);
  * kind 0 all; 1 slab, geo = x1,x2,y1,y2,z1,z2; 2 wall, geo = axis, pos;
  * 3 sphere, geo = rad, ox, oy, oz; 4 cylinder, geo = axis, hole, rad, a, b. */
 int slbc_mp_fill(slbc_tracer *t, int kind, const double *geo, double value);
+/* Tracer added by slbc_mp_fill, sum of (value - old p) over the nodes set
+ * since the tracer was created or last reset (no counterpart in the
+ * reference: the mass balance of a constant-concentration source).  reset
+ * = 1 zeroes the count after reading it. */
+int slbc_mp_injected(slbc_tracer *t, int reset, double *out);
+/* out[0] = sum of p, out[1] = number of fluid nodes on the plane axis = pos
+ * (axis 0, 1, 2 for i, j, k; no counterpart in the reference: the
+ * breakthrough curve of a tracer front). */
+int slbc_mp_plane(slbc_tracer *t, int axis, int pos, double out[2]);
 /* p *= fac on fluid nodes (reference src/mpmisc.c:214-225). */
 int slbc_mp_scale(slbc_tracer *t, double fac);
 /* p = 0 on adsorbing nodes (reference src/mpads.c:177-186). */

@@ -315,8 +315,14 @@ void mppush(MPSys);
  * src/lbstore.c:340-401) followed by a collision. */
 void lbsetvel(LBSys, LBReal *, LBReal *, LBReal *, LBReal *);
 /* Tracer totals over "fluid", "solid", "adsorbed" or "all" nodes (the sums
- * that mpcheck and adtotal print, reference src/mpmisc.c:121-136). */
+ * that mpcheck and adtotal print, reference src/mpmisc.c:121-136), or
+ * "injected": the tracer that mpall, mpslab, mpwall, mpsph and mpcyl have
+ * added (sum of pval - old p over the nodes they set) since mpinit, for the
+ * mass balance of a constant-concentration source. */
 LBReal mptotal(MPSys, char *);
+/* Mean tracer over the fluid nodes of the plane "x"/"y"/"z" = pos (0 when
+ * the plane has no fluid node): the breakthrough curve of a front. */
+LBReal mpplane(MPSys, char *, int);
 
 #ifdef __cplusplus
 }

@@ -57,8 +57,15 @@ MPSys newmp(LBSys lb, char *name) {
   mp->name = myscmp("null", name) ? NULL : mycopy(name);
   mp->adprob = 1.0;
   mp->precision = lb->precision;
-  mp->priv = NULL;
+  mp->priv = zalloc(sizeof(double));  /* tracer added by the fills (extension) */
   return mp;
+}
+
+/* p = pval on a fluid node, counting what the fill adds (extension: the
+ * GB300 library's injected-tracer count, not in the reference) */
+static void set_p(MPSys mp, long n, LBReal pval) {
+  *(double *)mp->priv += pval - mp->p[n];
+  mp->p[n] = pval;
 }
 
 /* reference src/mpmisc.c:64-79 */
@@ -76,6 +83,7 @@ void mprhoinit(MPSys mp) {
 void mpinit(MPSys mp) {
   mprhoinit(mp);
   memset(mp->p, 0, mp->lb->nnodes * sizeof(LBReal));
+  *(double *)mp->priv = 0.0;
   mp->step = 0; mp->to_be_initialised = 0;
 }
 
@@ -180,6 +188,7 @@ void mpcheck(MPSys mp) {
 LBReal mptotal(MPSys mp, char *which) {
   LBReal pfl, psl, pad = 0.0;
   long n;
+  if (which[0] == 'i') return *(double *)mp->priv;
   mp_totals(mp, &pfl, &psl);
   if (which[0] == 'f') return pfl;
   if (which[0] == 's') return psl;
@@ -188,6 +197,29 @@ LBReal mptotal(MPSys mp, char *which) {
     return pad;
   }
   return pfl + psl;
+}
+
+/* extension: mean tracer over the fluid nodes of one plane */
+LBReal mpplane(MPSys mp, char *type, int pos) {
+  LBSys lb = mp->lb;
+  int i, j, k, axis, lim[3];
+  double sum = 0.0, cnt = 0.0;
+  lim[0] = lb->esi; lim[1] = lb->esj; lim[2] = lb->esk;
+  switch (type[0]) {
+    case 'x': case 'i': axis = 0; break;
+    case 'y': case 'j': axis = 1; break;
+    case 'z': case 'k': axis = 2; break;
+    default: printf("Unrecognised direction for a plane\n"); return 0.0;
+  }
+  if (pos < 0 || pos > lim[axis] - 1) { printf("plane position out of range\n"); return 0.0; }
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    int c = (axis == 0) ? i : (axis == 1) ? j : k;
+    long n = node(lb, i, j, k);
+    if (c != pos || lb->obj[n] != NULL) continue;
+    sum += mp->p[n];
+    cnt += 1.0;
+  }
+  return cnt > 0.0 ? sum / cnt : 0.0;
 }
 
 /* reference src/mpmisc.c:142-158 */
@@ -251,7 +283,7 @@ LBReal mpspread(MPSys mp, char *dirn) {
 
 void mpall(MPSys mp, LBReal pval) {
   long n;
-  for (n = 0; n < mp->lb->nnodes; n++) if (mp->lb->obj[n] == NULL) mp->p[n] = pval;
+  for (n = 0; n < mp->lb->nnodes; n++) if (mp->lb->obj[n] == NULL) set_p(mp, n, pval);
 }
 
 void mpslab(MPSys mp, LBReal x1, LBReal x2, LBReal y1, LBReal y2, LBReal z1, LBReal z2, LBReal pval) {
@@ -260,7 +292,7 @@ void mpslab(MPSys mp, LBReal x1, LBReal x2, LBReal y1, LBReal y2, LBReal z1, LBR
   for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++)
     if (i > x1 && i < x2 && j > y1 && j < y2 && k > z1 && k < z2) {
       long n = node(lb, i, j, k);
-      if (lb->obj[n] == NULL) mp->p[n] = pval;
+      if (lb->obj[n] == NULL) set_p(mp, n, pval);
     }
 }
 
@@ -280,7 +312,7 @@ void mpwall(MPSys mp, char *type, int wallpos, LBReal pval) {
     long n;
     if (c != wallpos) continue;
     n = node(lb, i, j, k);
-    if (lb->obj[n] == NULL) mp->p[n] = pval;
+    if (lb->obj[n] == NULL) set_p(mp, n, pval);
   }
 }
 
@@ -291,7 +323,7 @@ void mpsph(MPSys mp, LBReal rad, LBReal ox, LBReal oy, LBReal oz, LBReal pval) {
   for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
     LBReal rsq = (i - ox) * (i - ox) + (j - oy) * (j - oy) + (k - oz) * (k - oz);
     long n = node(lb, i, j, k);
-    if (rsq < radsq && lb->obj[n] == NULL) mp->p[n] = pval;
+    if (rsq < radsq && lb->obj[n] == NULL) set_p(mp, n, pval);
   }
 }
 
@@ -309,7 +341,7 @@ void mpcyl(MPSys mp, char *type, LBReal rad, LBReal a, LBReal b, LBReal pval) {
     }
     within = (rsq < radsq);
     if (type[1] != '\0') within = !within;
-    if (within && lb->obj[n] == NULL) mp->p[n] = pval;
+    if (within && lb->obj[n] == NULL) set_p(mp, n, pval);
   }
 }
 
@@ -393,5 +425,5 @@ void mppush(MPSys mp) { (void)mp; }
 
 void freemp(MPSys mp) {
   if (mp == NULL) return;
-  free(mp->p); free(mp->newp); free(mp->name); free(mp);
+  free(mp->priv); free(mp->p); free(mp->newp); free(mp->name); free(mp);
 }

@@ -23,6 +23,7 @@ struct slbc_tracer {
   slbc_lattice *h = nullptr;
   int f64 = 1;
   void *p = nullptr, *p2 = nullptr;
+  double *acc = nullptr;  // tracer added by fills since creation or the last reset
   double *objstate = nullptr;
   int objstate_cap = 0;
 };
@@ -163,33 +164,79 @@ __global__ void k_mp_minmax(const TP *p, const uint16_t *flags, long long n, dou
   }
 }
 
-// tracer injection on fluid nodes of a region (reference src/mpobjs.c)
+// Node of entry e of a plane (axis 0: i = pos, 1: j = pos, 2: k = pos).
+__device__ __forceinline__ long long plane_node(long long e, int axis, int pos, int esi, int esj, int esk) {
+  int i, j, k;
+  if (axis == 0) { i = pos; j = (int)(e / esk); k = (int)(e % esk); }
+  else if (axis == 1) { j = pos; i = (int)(e / esk); k = (int)(e % esk); }
+  else { k = pos; i = (int)(e / esj); j = (int)(e % esj); }
+  return ((long long)i * esj + j) * esk + k;
+}
+
+// Tracer injection on the fluid nodes of a region (reference src/mpobjs.c).
+// Kind 2 (a wall) visits only the nodes of its plane.  Each block also
+// writes the sum of (value - old p) over the nodes it set, so the host
+// layer can keep count of the tracer the fills have added.
 template <typename TP>
-__global__ void k_mp_fill(TP *p, const uint16_t *flags, int esi, int esj, int esk, int kind,
-                          double g0, double g1, double g2, double g3, double g4, double g5,
-                          double value) {
-  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= (long long)esi * esj * esk) return;
-  if (flags[x] & FLAG_SOLID) return;
-  const int k = (int)(x % esk), r = (int)(x / esk), j = r % esj, i = r / esj;
-  bool in = false;
-  switch (kind) {
-    case 0: in = true; break;
-    case 1: in = i > g0 && i < g1 && j > g2 && j < g3 && k > g4 && k < g5; break;
-    case 2: { const int c = (int)g0 == 0 ? i : (int)g0 == 1 ? j : k; in = c == (int)g1; } break;
-    case 3: {
-      const double rsq = (i - g1) * (i - g1) + (j - g2) * (j - g2) + (k - g3) * (k - g3);
-      in = rsq < g0 * g0;
-    } break;
-    case 4: {
-      const int ax = (int)g0;
-      const double u = ax == 0 ? j : i, v = ax == 2 ? j : k;
-      const double rsq = (u - g3) * (u - g3) + (v - g4) * (v - g4);
-      in = rsq < g2 * g2;
-      if (g1 != 0.0) in = !in;
-    } break;
+__global__ void __launch_bounds__(kReduceThreads)
+k_mp_fill(TP *p, const uint16_t *flags, int esi, int esj, int esk, int kind, double g0, double g1,
+          double g2, double g3, double g4, double g5, double value, long long count, double *partials) {
+  double v[1] = {0.0};
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long x = kind == 2 ? plane_node(e, (int)g0, (int)g1, esi, esj, esk) : e;
+    if (flags[x] & FLAG_SOLID) continue;
+    const int k = (int)(x % esk), r = (int)(x / esk), j = r % esj, i = r / esj;
+    bool in = false;
+    switch (kind) {
+      case 0: in = true; break;
+      case 1: in = i > g0 && i < g1 && j > g2 && j < g3 && k > g4 && k < g5; break;
+      case 2: in = true; break;
+      case 3: {
+        const double rsq = (i - g1) * (i - g1) + (j - g2) * (j - g2) + (k - g3) * (k - g3);
+        in = rsq < g0 * g0;
+      } break;
+      case 4: {
+        const int ax = (int)g0;
+        const double u = ax == 0 ? j : i, w = ax == 2 ? j : k;
+        const double rsq = (u - g3) * (u - g3) + (w - g4) * (w - g4);
+        in = rsq < g2 * g2;
+        if (g1 != 0.0) in = !in;
+      } break;
+    }
+    if (in) {
+      const TP nv = (TP)value;
+      v[0] += (double)nv - (double)p[x];
+      p[x] = nv;
+    }
   }
-  if (in) p[x] = (TP)value;
+  block_sum<1>(v);
+  if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+// acc[0] += sum of nb partials, in a fixed order
+__global__ void __launch_bounds__(256) k_sum_into(const double *partials, int nb, double *acc) {
+  double v[1] = {0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v[0] += partials[b];
+  block_sum<1>(v);
+  if (threadIdx.x == 0) acc[0] += v[0];
+}
+
+// sum of p and number of fluid nodes on one plane
+template <typename TP>
+__global__ void __launch_bounds__(kReduceThreads)
+k_mp_plane(const TP *p, const uint16_t *flags, int esi, int esj, int esk, int axis, int pos,
+           long long count, double *partials) {
+  double v[2] = {0.0, 0.0};
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long x = plane_node(e, axis, pos, esi, esj, esk);
+    if (flags[x] & FLAG_SOLID) continue;
+    v[0] += (double)p[x];
+    v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  if (threadIdx.x == 0) { partials[2 * blockIdx.x] = v[0]; partials[2 * blockIdx.x + 1] = v[1]; }
 }
 
 template <typename TP>
@@ -828,6 +875,8 @@ int slbc_mp_create(slbc_lattice *h, slbc_tracer **out, int use_f64) {
   if (e == cudaSuccess) e = cudaMalloc(&t->p2, (size_t)L.nnodes * es);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->p, 0, (size_t)L.nnodes * es, L.stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->p2, 0, (size_t)L.nnodes * es, L.stream);
+  if (e == cudaSuccess) e = cudaMalloc(&t->acc, sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->acc, 0, sizeof(double), L.stream);
   if (e == cudaSuccess && !L.mp_rho64) {
     e = cudaMalloc(&L.mp_rho64, (size_t)L.nnodes * sizeof(double));
     if (e == cudaSuccess) {
@@ -858,6 +907,7 @@ void slbc_mp_destroy(slbc_tracer *t) {
   if (t->h) cudaStreamSynchronize(t->h->L.stream);
   if (t->p) cudaFree(t->p);
   if (t->p2) cudaFree(t->p2);
+  if (t->acc) cudaFree(t->acc);
   if (t->objstate) cudaFree(t->objstate);
   delete t;
 }
@@ -964,17 +1014,66 @@ int slbc_mp_minmax(slbc_tracer *t, double out[2]) {
   return 0;
 }
 
+static long long plane_size(const Lattice &L, int axis) {
+  return axis == 0 ? (long long)L.esj * L.esk : axis == 1 ? (long long)L.esi * L.esk : (long long)L.esi * L.esj;
+}
+
 int slbc_mp_fill(slbc_tracer *t, int kind, const double *geo, double value) {
   Lattice &L = t->h->L;
   double g[6] = {0, 0, 0, 0, 0, 0};
   const int ng = kind == 1 ? 6 : kind == 2 ? 2 : kind == 3 ? 4 : kind == 4 ? 5 : 0;
   for (int c = 0; c < ng; c++) g[c] = geo[c];
+  long long count = L.nnodes;
+  if (kind == 2) {
+    const int axis = (int)g[0], pos = (int)g[1];
+    const int lim = axis == 0 ? L.esi : axis == 1 ? L.esj : L.esk;
+    if (axis < 0 || axis > 2 || pos < 0 || pos >= lim) return fail_msg("slbc_mp_fill: wall outside the lattice");
+    count = plane_size(L, axis);
+  }
+  const int nb = (int)std::max<long long>(1, std::min<long long>(blocks_for(count, kReduceThreads), 152 * 4));
+  if (ensure_partials(L, nb + 8)) return 1;
   if (t->f64)
-    k_mp_fill<double><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((double *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value);
+    k_mp_fill<double><<<nb, kReduceThreads, 0, L.stream>>>((double *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
   else
-    k_mp_fill<float><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((float *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value);
+    k_mp_fill<float><<<nb, kReduceThreads, 0, L.stream>>>((float *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
   count_launch();
   CK(cudaGetLastError());
+  k_sum_into<<<1, 256, 0, L.stream>>>(L.partials, nb, t->acc);
+  count_launch();
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int slbc_mp_injected(slbc_tracer *t, int reset, double *out) {
+  Lattice &L = t->h->L;
+  double v = 0.0;
+  CK(cudaMemcpyAsync(&v, t->acc, sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  if (out) *out = v;
+  if (reset) CK(cudaMemsetAsync(t->acc, 0, sizeof(double), L.stream));
+  return 0;
+}
+
+int slbc_mp_plane(slbc_tracer *t, int axis, int pos, double out[2]) {
+  Lattice &L = t->h->L;
+  const int lim = axis == 0 ? L.esi : axis == 1 ? L.esj : L.esk;
+  if (axis < 0 || axis > 2 || pos < 0 || pos >= lim) return fail_msg("slbc_mp_plane: plane outside the lattice");
+  const long long count = plane_size(L, axis);
+  const int nb = (int)std::max<long long>(1, std::min<long long>(blocks_for(count, kReduceThreads), 152 * 2));
+  if (ensure_partials(L, 2 * nb + 8)) return 1;
+  if (t->f64)
+    k_mp_plane<double><<<nb, kReduceThreads, 0, L.stream>>>((const double *)t->p, L.flags, L.esi, L.esj, L.esk, axis, pos, count, L.partials);
+  else
+    k_mp_plane<float><<<nb, kReduceThreads, 0, L.stream>>>((const float *)t->p, L.flags, L.esi, L.esj, L.esk, axis, pos, count, L.partials);
+  count_launch();
+  CK(cudaGetLastError());
+  k_final_sum_tree<2><<<1, 256, 0, L.stream>>>(L.partials, nb, L.partials + 2 * nb);
+  count_launch();
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(L.host_out, L.partials + 2 * nb, 2 * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
+  CK(cudaStreamSynchronize(L.stream));
+  out[0] = L.host_out[0];
+  out[1] = L.host_out[1];
   return 0;
 }
 

@@ -97,7 +97,7 @@ void mpinit(MPSys mp) {
   memset(mp->p, 0, (size_t)mp->lb->nnodes * sizeof(LBReal));
   st->p_gen++;
   st->host_p_valid = 1;
-  tracer(mp);
+  slb_check(slbc_mp_injected(tracer(mp), 1, NULL), "injected tracer");
   mp->step = 0;
   mp->to_be_initialised = 0;
   printf("MP '%s' initialised and ready to go.\n", mp->name);
@@ -162,14 +162,35 @@ void mpcheck(MPSys mp) {
   mptrace(mp, "mpcheck");
 }
 
-/* appended: tracer totals, which = "fluid", "solid", "adsorbed" or "all" */
+/* appended: tracer totals, which = "fluid", "solid", "adsorbed", "all" or
+ * "injected" (added by the device fills since mpinit) */
 LBReal mptotal(MPSys mp, char *which) {
   double s[5];
+  if (which[0] == 'i') {
+    double v = 0.0;
+    slb_check(slbc_mp_injected(tracer(mp), 0, &v), "injected tracer");
+    return v;
+  }
   sums(mp, -1, s);
   if (which[0] == 'f') return s[0];
   if (which[0] == 's') return s[1];
   if (which[0] == 'a' && which[1] == 'd') return s[2];
   return s[0] + s[1];
+}
+
+/* appended: mean tracer over the fluid nodes of the plane type = pos */
+LBReal mpplane(MPSys mp, char *type, int pos) {
+  double s[2];
+  int axis, lim;
+  switch (type[0]) {
+    case 'x': case 'i': axis = 0; lim = mp->lb->esi; break;
+    case 'y': case 'j': axis = 1; lim = mp->lb->esj; break;
+    case 'z': case 'k': axis = 2; lim = mp->lb->esk; break;
+    default: printf("Unrecognised direction for a plane\n"); return 0.0;
+  }
+  if (pos < 0 || pos > lim - 1) { printf("plane position out of range\n"); return 0.0; }
+  slb_check(slbc_mp_plane(tracer(mp), axis, pos, s), "tracer plane");
+  return s[1] > 0.0 ? s[0] / s[1] : 0.0;
 }
 
 /* reference src/mpmisc.c:142-158 */

@@ -85,37 +85,105 @@ def _stamp(solid, rad, centre):
     return added
 
 
-def rsa_packing(n, phi, rmin, rmax, seed=1, overlap=False, max_tries=2_000_000):
+def _splitmix_block(state, count):
+    """The next `count` outputs of a splitmix64 generator in `state` (the
+    generator is a counter hash, so a block is computed at once); returns
+    (new state, uint64 array)."""
+    k = np.arange(1, count + 1, dtype=np.uint64)
+    z = np.uint64(state) + k * np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    z = z ^ (z >> np.uint64(31))
+    return (state + count * 0x9E3779B97F4A7C15) & MASK64, z
+
+
+def _min_image_hits(cand, rc, cen, rad, n):
+    """For each candidate row of cand (m x 3) with radius rc (m), whether any
+    sphere of cen/rad (m x K x 3 / m x K, NaN radius = empty) overlaps it
+    under the periodic minimum-image convention."""
+    d = cen - cand[:, None, :]
+    d -= n * np.round(d / n)
+    dist = np.sqrt((d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2])
+    return np.any(dist < rad + rc[:, None], axis=1)
+
+
+def rsa_packing(n, phi, rmin, rmax, seed=1, overlap=False, max_tries=50_000_000, block=4096):
     """Random sequential addition of spheres in a periodic n^3 box.
 
-    Centres uniform in [0, n)^3, radii uniform in [rmin, rmax]; a sphere is
-    accepted when its periodic minimum-image distance to every accepted one
-    is at least the sum of the radii (any distance when overlap=True).
-    Stops once the lattice solid fraction (nodes inside a sphere or an
-    image) reaches phi.  Returns (spheres [(r, x, y, z)], solid mask)."""
-    rng = SplitMix64(seed)
+    Centres uniform in [0, n)^3, radii uniform in [rmin, rmax] (four
+    splitmix64 draws per try: x, y, z, r); a sphere is accepted when its
+    periodic minimum-image distance to every accepted one is at least the sum
+    of the radii (any distance when overlap=True).  Stops once the lattice
+    solid fraction (nodes inside a sphere or an image) reaches phi.  Returns
+    (spheres [(r, x, y, z)], solid mask).
+
+    Tries are drawn a block at a time and tested together against the
+    spheres accepted before the block (binned in cubic cells of side
+    >= 2 rmax, so only the 27 cells around a candidate matter); the few
+    survivors are then taken in order and tested against the spheres
+    accepted earlier in the same block, which gives exactly the sequential
+    decisions."""
+    state = seed & MASK64
     solid = np.zeros((n, n, n), dtype=bool)
     spheres = []
-    centres = np.zeros((0, 3))
-    radii = np.zeros(0)
+    ncell = max(1, int(n // (2.0 * rmax)))
+    cw = n / ncell
+    cap = 8
+    grid = np.full((ncell, ncell, ncell, cap), -1, dtype=np.int64)
+    fill = np.zeros((ncell, ncell, ncell), dtype=np.int64)
+    cen = np.zeros((1024, 3))
+    rad = np.zeros(1024)
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
     tries = 0
     nset = 0
     target = phi * solid.size
     while nset < target:
-        tries += 1
-        if tries > max_tries:
-            raise RuntimeError(f"RSA stalled at solid fraction {nset / solid.size:.4f} < {phi}")
-        c = np.array([rng.uniform(0.0, n) for _ in range(3)])
-        r = rng.uniform(rmin, rmax)
-        if not overlap and len(spheres):
-            d = centres - c
-            d -= n * np.round(d / n)
-            if np.any(np.sqrt((d * d).sum(axis=1)) < radii + r):
-                continue
-        spheres.append((r, float(c[0]), float(c[1]), float(c[2])))
-        centres = np.vstack([centres, c])
-        radii = np.append(radii, r)
-        nset += _stamp(solid, r, c)
+        state, z = _splitmix_block(state, 4 * block)
+        u = ((z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))).reshape(block, 4)
+        C = 0.0 + (n - 0.0) * u[:, :3]
+        R = rmin + (rmax - rmin) * u[:, 3]
+        alive = np.ones(block, dtype=bool)
+        ns = len(spheres)
+        if not overlap and ns:
+            if ncell < 3:
+                hit = _min_image_hits(C, R, np.broadcast_to(cen[:ns], (block, ns, 3)),
+                                      np.broadcast_to(rad[:ns], (block, ns)), n)
+            else:
+                ci = np.minimum(ncell - 1, (C // cw).astype(np.int64))
+                nb = (ci[:, None, :] + offs[None, :, :]) % ncell
+                idx = grid[nb[..., 0], nb[..., 1], nb[..., 2]].reshape(block, -1)
+                valid = idx >= 0
+                safe = np.where(valid, idx, 0)
+                r_nb = np.where(valid, rad[safe], np.nan)
+                hit = _min_image_hits(C, R, cen[safe], r_nb, n)
+            alive &= ~hit
+        first_new = ns
+        for t in np.nonzero(alive)[0] if not overlap else range(block):
+            if tries + t + 1 > max_tries:
+                raise RuntimeError(f"RSA stalled at solid fraction {nset / solid.size:.4f} < {phi}")
+            c = C[t]
+            r = float(R[t])
+            if not overlap and len(spheres) > first_new:
+                m = len(spheres)
+                if _min_image_hits(c[None, :], np.array([r]), cen[None, first_new:m], rad[None, first_new:m], n)[0]:
+                    continue
+            m = len(spheres)
+            if m == len(rad):
+                cen = np.vstack([cen, np.zeros_like(cen)])
+                rad = np.concatenate([rad, np.zeros_like(rad)])
+            cen[m] = c
+            rad[m] = r
+            cell = tuple(min(ncell - 1, int(c[a] // cw)) for a in range(3))
+            if fill[cell] == cap:
+                grid = np.concatenate([grid, np.full(grid.shape, -1, dtype=np.int64)], axis=3)
+                cap *= 2
+            grid[cell + (fill[cell],)] = m
+            fill[cell] += 1
+            spheres.append((r, float(c[0]), float(c[1]), float(c[2])))
+            nset += _stamp(solid, r, c)
+            if nset >= target:
+                break
+        tries += block
     return spheres, solid
 
 
@@ -193,3 +261,72 @@ def packed_bed(L, n=128, phi=0.30, rmin=4.0, rmax=8.0, seed=1, force=1e-6, tau=1
     L.syncobjs(lb)
     L.addbf(lb, force, 0.0, 0.0)
     return lb, spheres, solid
+
+
+def large_bed(L, n=512, phi=0.35, rmin=6.0, rmax=12.0, seed=4, precision=1, tau=1.0):
+    """Periodic packed bed for flow with a passive scalar: seeded RSA
+    spheres (each sphere plus its periodic images inserted with insertsph,
+    then flattenobj, as examples/rcp_perm.pl:105-116 does), fixed objects.
+    Returns (lb, spheres)."""
+    spheres, _ = rsa_packing(n, phi, rmin, rmax, seed)
+    lb = L.newlb(n, n, n, "null")
+    if L.extended:
+        lb.precision = precision
+    lb.tau = tau
+    lb.stokes_flow = 1
+    insert_spheres(L, lb, spheres)
+    L.syncobjs(lb)
+    return lb, spheres
+
+
+def pore_reynolds(lb, diameter):
+    """Re = vmeanx * d / nu with nu = (tau - 1/2) / 3 (lattice units)."""
+    return lb.vmeanx * diameter / ((lb.tau - 0.5) / 3.0)
+
+
+def calibrated_flow(L, lb, diameter, re_target=1.0, b0=1e-6, stokes_tol=1e-5, tol=1e-7, check=100,
+                    maxsteps=40000):
+    """Body force along x that gives a pore Reynolds number re_target: a
+    Stokes run at b0 to convergence fixes the linear response, b = b0 *
+    re_target / Re(b0); the flow is then run with the inertial term
+    (stokes_flow = 0) at b to convergence.  Returns a dict of the steps,
+    forces and Reynolds numbers."""
+    lb.stokes_flow = 1
+    L.zerobf(lb)
+    L.addbf(lb, b0, 0.0, 0.0)
+    s0 = L.lbconverge(lb, check, stokes_tol, maxsteps)
+    re0 = pore_reynolds(lb, diameter)
+    b = b0 * re_target / re0
+    lb.stokes_flow = 0
+    L.zerobf(lb)
+    L.addbf(lb, b, 0.0, 0.0)
+    s1 = L.lbconverge(lb, check, tol, maxsteps)
+    return {"stokes_steps": s0, "b_stokes": b0, "re_stokes": re0, "b": b, "steps": s1,
+            "re": pore_reynolds(lb, diameter), "vmeanx": lb.vmeanx, "converged": s1 < maxsteps}
+
+
+def tracer_breakthrough(L, lb, steps, precision=1, alpha=0.5, adprob=0.01, sample_every=500, source=1.0):
+    """Passive scalar in the frozen flow of lb: newmp + mpinit, every
+    boundary node adsorbing (adall) with probability adprob per encounter,
+    a constant-concentration plane at x = 0 re-set before every update
+    (mpwall), and the mean tracer over the fluid nodes of the last plane
+    x = esi - 1 every sample_every updates.  Returns (mp, curve, balance)
+    where balance holds the tracer in the fluid, on adsorbing nodes, in
+    total, and the tracer the source added."""
+    mp = L.newmp(lb, "null")
+    if L.extended:
+        mp.precision = precision
+        mp.adprob = adprob
+    mp.alpha = alpha
+    L.mpinit(mp)
+    L.adall(mp)
+    last = lb.esi - 1
+    curve = []
+    for s in range(1, steps + 1):
+        L.mpwall(mp, "x", 0, source)
+        L.mpstep(mp)
+        if s % sample_every == 0 or s == steps:
+            curve.append((s, L.mpplane(mp, "x", last)))
+    balance = {"fluid": L.mptotal(mp, "fluid"), "adsorbed": L.mptotal(mp, "adsorbed"),
+               "all": L.mptotal(mp, "all"), "injected": L.mptotal(mp, "injected")}
+    return mp, curve, balance

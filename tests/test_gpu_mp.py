@@ -118,3 +118,33 @@ def test_tracer_utilities_match_oracle(gpu, orc):
     assert np.array_equal(out[0][1], out[1][1])
     for a, b in zip(out[0][2], out[1][2]):
         assert abs(a - b) <= TOL * max(abs(b), 1e-300)
+
+
+@pytest.mark.parametrize("mp_precision", [0, 1])
+def test_source_plane_breakthrough_and_balance(gpu, orc, mp_precision):
+    """Constant-concentration source plane re-set every step (mpwall), partial
+    adsorption, frozen flow: the breakthrough samples (mpplane) and the
+    injected tracer (mptotal "injected") match the oracle, and fluid +
+    adsorbed tracer = injected to round-off."""
+    out = []
+    for L in (gpu, orc):
+        lb, mp = tracer_run(L, ads=1, adprob=0.01, steps=0, interleave=False, precision=1 if L is gpu else 0,
+                            mp_precision=mp_precision if L is gpu else None)
+        L.mpinit(mp)
+        L.adall(mp)
+        curve = []
+        for s in range(120):
+            L.mpwall(mp, "x", 0, 1.0)
+            L.mpstep(mp)
+            if s % 10 == 9:
+                curve.append(L.mpplane(mp, "x", lb.esi - 1))
+        inj = L.mptotal(mp, "injected")
+        held = L.mptotal(mp, "fluid") + L.mptotal(mp, "adsorbed")
+        out.append((np.array(curve), inj, held))
+    (cg, ig, hg), (co, io, ho) = out
+    # the GPU flow is FP32 here: tolerances of an FP32 flow / FP32 tracer
+    tol = 1e-4 if mp_precision else 2e-5
+    assert np.abs(cg - co).max() <= tol * max(np.abs(co).max(), 1e-30)
+    assert abs(ig - io) <= tol * io
+    assert abs(ho - io) <= 1e-12 * io          # oracle: exact balance
+    assert abs(hg - ig) <= (1e-5 if mp_precision else 1e-12) * ig
