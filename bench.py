@@ -528,32 +528,37 @@ def run_tracer(args):
             continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        mp, curve, bal = W.tracer_breakthrough(L, lb, nsteps, precision=prec, alpha=TRACER_ALPHA,
-                                               adprob=TRACER_ADPROB, sample_every=args.sample_every)
+        mp, curve, bals = W.tracer_breakthrough(L, lb, nsteps, precision=prec, alpha=TRACER_ALPHA,
+                                                adprob=TRACER_ADPROB, sample_every=args.sample_every)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         kms = time_tracer(torch, L, lb, mp, 50) / 50
         gbs = TRACER_BYTES[prec] * nodes / (kms * 1e-3) / 1e9
+        _, fl, ad, al, inj = bals[-1]
         tracers[name] = {
             "steps": nsteps, "wall_s": round(wall, 2),
-            "MLUPS_with_source_and_samples": round(nodes * nsteps / wall / 1e6, 1),
+            "MLUPS_with_planes_and_samples": round(nodes * nsteps / wall / 1e6, 1),
             "kernel": {"MLUPS": round(nodes / (kms * 1e-3) / 1e6, 1), "ms_per_step": round(kms, 4),
                        "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
                        "bytes_per_update": TRACER_BYTES[prec]},
-            "balance": bal,
-            "balance_rel_error": (bal["all"] - bal["injected"]) / bal["injected"] if bal["injected"] else None,
+            "balance": {"fluid": fl, "adsorbed": ad, "all": al, "injected": inj,
+                        "rel_error": (al - inj) / inj if inj else None},
             "breakthrough": curve,
+            "balances": bals,
         }
         L.freemp(mp)
     if "fp32" in tracers and "fp64" in tracers:
         c32 = dict(tracers["fp32"]["breakthrough"])
         c64 = dict(tracers["fp64"]["breakthrough"])
+        b32 = {b[0]: b for b in tracers["fp32"]["balances"]}
+        b64 = {b[0]: b for b in tracers["fp64"]["balances"]}
         common = sorted(set(c32) & set(c64))
+        last = common[-1] if common else None
         tracers["fp32_vs_fp64"] = {
+            "compared_at_steps": [common[0], last] if common else None,
             "breakthrough_max_abs_diff": max(abs(c32[s] - c64[s]) for s in common) if common else None,
-            "adsorbed_rel_diff": abs(tracers["fp32"]["balance"]["adsorbed"] - tracers["fp64"]["balance"]["adsorbed"])
-            / max(abs(tracers["fp64"]["balance"]["adsorbed"]), 1e-300)
-            if tracers["fp32"]["steps"] == tracers["fp64"]["steps"] else None}
+            "adsorbed_rel_diff": abs(b32[last][2] - b64[last][2]) / max(abs(b64[last][2]), 1e-300) if last else None,
+            "held_rel_diff": abs(b32[last][3] - b64[last][3]) / max(abs(b64[last][3]), 1e-300) if last else None}
     line = {
         "workload": f"flow and passive scalar, periodic {n}^3 packed bed",
         "metric": "MLUPS of the flow and tracer kernels; breakthrough and tracer mass balance",
@@ -561,7 +566,8 @@ def run_tracer(args):
                    "radii": [TRACER_RMIN, TRACER_RMAX], "seed": TRACER_SEED, "spheres": len(spheres),
                    "mean_diameter": diameter, "tau": 1.0, "flow": "Navier-Stokes (stokes_flow = 0), FP32 populations",
                    "tracer_alpha": TRACER_ALPHA, "adsorption_probability": TRACER_ADPROB,
-                   "source": "mpwall x = 0, p = 1, re-set before every update"},
+                   "source": "mpwall x = 0, p = 1, and absorbing mpwall x = side - 1, p = 0, re-set before every update",
+                   "breakthrough_plane": "x = side - 2 (mean over its fluid nodes)"},
         "build_s": round(t_build, 1), "flow": flow, "flow_kernel": flow_kernel, "tracer": tracers,
         "measured_peak_gbs": peak, "peak_kind": peak_kind,
     }
@@ -588,7 +594,7 @@ def main():
                     help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive scalar")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")
     ap.add_argument("--tracer-steps", type=int, default=50000)
-    ap.add_argument("--fp64-tracer-steps", type=int, default=50000)
+    ap.add_argument("--fp64-tracer-steps", type=int, default=10000)
     ap.add_argument("--sample-every", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:

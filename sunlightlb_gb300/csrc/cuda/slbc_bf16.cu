@@ -80,17 +80,6 @@ __device__ __forceinline__ float bf_post(const Bf16Args &a, int layout, int q, i
 // memory; the plane after next is fetched into registers while the current
 // one is updated.  Moments then cross L2 about 1.7 times per node instead of
 // 15 times.
-constexpr int kTileK = 32, kTileJ = 8;
-constexpr int kHaloK = kTileK + 2, kHaloJ = kTileJ + 2;
-constexpr int kPlane = kHaloK * kHaloJ;                 // float4 per plane
-constexpr int kTileThreads = kTileK * kTileJ;
-constexpr int kPlaneLoads = (kPlane + kTileThreads - 1) / kTileThreads;
-
-__device__ __forceinline__ int wrap_index(int v, int n) {
-  v %= n;
-  return v < 0 ? v + n : v;
-}
-
 template <bool ODD, bool MOVING, bool BFU>
 __global__ void __launch_bounds__(kTileThreads, 4) k_step_bf16(Bf16Args a, StepArgs<float> s, int planes) {
   __shared__ float4 ring[3][kPlane];

@@ -115,6 +115,25 @@ __global__ void k_distrib_obj(const int *obj_first_piece, const int *obj_npiece,
   for (int c = 0; c < 6; c++) ft[6 * o + c] = v[c];
 }
 
+// Per fluid node, the boundary links whose solid end adsorbs (bit q: the
+// solid node x - c_q has its adsorption byte set).
+__global__ void k_ads_links(const uint16_t *flags, const unsigned char *ads, uint16_t *links, int esi,
+                            int esj, int esk) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= (long long)esi * esj * esk) return;
+  const uint16_t fl = flags[x];
+  uint16_t mask = 0;
+  if (!(fl & FLAG_SOLID) && (fl & FLAG_LINKS)) {
+    int i, j, k;
+    decode((int)x, esj, esk, i, j, k);
+    const Nbr nb = make_nbr(i, j, k, esi, esj, esk);
+#pragma unroll
+    for (int q = 1; q < 15; q++)
+      if (((fl >> q) & 1) && ads[nb.at(-CX(q), -CY(q), -CZ(q))]) mask |= (uint16_t)(1u << q);
+  }
+  links[x] = mask;
+}
+
 // tracer sums: fluid, solid, adsorbing, first and second moment along axis
 template <typename TP>
 __global__ void __launch_bounds__(kReduceThreads)
@@ -499,7 +518,8 @@ void slbc_destroy(slbc_lattice *h) {
   if (L.stream) cudaStreamSynchronize(L.stream);
   void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
                   L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
-                  L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1]};
+                  L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1],
+                  L.ads_links};
   for (void *b : bufs) if (b) cudaFree(b);
   if (L.host_out) cudaFreeHost(L.host_out);
   if (L.graph) cudaGraphExecDestroy(L.graph);
@@ -554,6 +574,7 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
 int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *bnd_node,
                       const int *bnd_obj, long nbnd) {
   Lattice &L = h->L;
+  L.ads_version++;  // the boundary links change
   const long long n = L.nnodes;
   for (long long x = 0; x < n; x++) h->solid_host[x] = objidx[x] >= 0;
   CK(cudaMemcpyAsync(L.objidx, objidx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, L.stream));
@@ -623,6 +644,7 @@ int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads) {
   if (!L.ads) CK(cudaMalloc(&L.ads, (size_t)L.nnodes));
   CK(cudaMemcpyAsync(L.ads, ads, (size_t)L.nnodes, cudaMemcpyHostToDevice, L.stream));
   CK(cudaStreamSynchronize(L.stream));
+  L.ads_version++;
   return 0;
 }
 
@@ -958,6 +980,13 @@ int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
                  const double *objstate, int nobj) {
   Lattice &L = t->h->L;
   if (no_bf16(L, "slbc_mp_step")) return 1;
+  if (L.ads && L.ads_links_version != L.ads_version) {
+    if (!L.ads_links) CK(cudaMalloc(&L.ads_links, (size_t)L.nnodes * sizeof(uint16_t)));
+    k_ads_links<<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>(L.flags, L.ads, L.ads_links, L.esi, L.esj, L.esk);
+    count_launch();
+    CK(cudaGetLastError());
+    L.ads_links_version = L.ads_version;
+  }
   if (!L.mp_rho64) return fail_msg("slbc_mp_step: density snapshot missing");
   if (!t->f64 && !L.mp_rho32) return fail_msg("slbc_mp_step: FP32 density snapshot missing");
   if (moving) {

@@ -72,6 +72,10 @@ struct Lattice {
   double *obj_pos = nullptr;    // 3 * nobj
   double *obj_ft = nullptr;     // 6 * nobj
   unsigned char *ads = nullptr; // adsorption byte per node
+  // per fluid node, bit q: the link from x - c_q is a boundary link from an
+  // adsorbing solid node (rebuilt when ads_version moved on)
+  uint16_t *ads_links = nullptr;
+  long ads_version = 0, ads_links_version = -1;
   int *objidx = nullptr;        // object index per node (-1 fluid)
   // parameters
   slbc_params par{};

@@ -45,6 +45,20 @@ __device__ __forceinline__ Nbr make_nbr(int i, int j, int k, int esi, int esj, i
   return n;
 }
 
+// Plane-marching tiles: a block of kTileK (k) x kTileJ (j) threads walks
+// along i and keeps per-node values of three consecutive planes, with a
+// one-node halo, in shared memory (kPlane entries per plane).
+constexpr int kTileK = 32, kTileJ = 8;
+constexpr int kHaloK = kTileK + 2, kHaloJ = kTileJ + 2;
+constexpr int kPlane = kHaloK * kHaloJ;
+constexpr int kTileThreads = kTileK * kTileJ;
+constexpr int kPlaneLoads = (kPlane + kTileThreads - 1) / kTileThreads;
+
+__device__ __forceinline__ int wrap_index(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
 __device__ __forceinline__ void decode(int x, int esj, int esk, int &i, int &j, int &k) {
   k = x % esk;
   const int r = x / esk;

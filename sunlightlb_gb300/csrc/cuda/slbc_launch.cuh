@@ -166,14 +166,40 @@ cudaError_t SLBC_FN(launch_mp_rhoinit)(Lattice &L) {
 cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, int tp_f64,
                                     double alpha, double adprob, int moving,
                                     const double *objstate) {
-  const int bx = L.esk >= 128 ? 128 : (L.esk >= 64 ? 64 : 32);
+  // planes per block: the largest of 1..8 that still gives about four
+  // blocks per SM
+  const long long tiles = (long long)((L.esk + kTileK - 1) / kTileK) * ((L.esj + kTileJ - 1) / kTileJ);
+  int planes = 8;
+  while (planes > 1 && tiles * ((L.esi + planes - 1) / planes) < 152 * 4) planes /= 2;
+  const dim3 grid((unsigned)((L.esk + kTileK - 1) / kTileK), (unsigned)((L.esj + kTileJ - 1) / kTileJ),
+                  (unsigned)((L.esi + planes - 1) / planes));
+  const dim3 block(kTileK, kTileJ);
   MpArgs m;
   m.p_in = p_in; m.p_out = p_out;
   m.rho = tp_f64 ? (const void *)L.mp_rho64 : (const void *)L.mp_rho32;
-  m.ads = L.ads; m.objidx = L.objidx; m.objstate = objstate; m.moving = moving;
+  m.ads = L.ads; m.ads_links = L.ads_links; m.objidx = L.objidx; m.objstate = objstate; m.moving = moving;
   m.alpha = alpha; m.adprob = adprob; m.rho0 = L.par.rho0;
-  if (tp_f64) k_mp_step<T_, double><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), L.layout, m);
-  else k_mp_step<T_, float><<<row_grid(L, bx), bx, 0, L.stream>>>(pop_args(L), L.layout, m);
+  m.alpha_f = (float)alpha; m.adprob_f = (float)adprob; m.rho0_f = (float)L.par.rho0;
+  m.partial = adprob != 1.0;
+  // the wrap-node buckets need more than the default 48 KB of dynamic
+  // shared memory for FP64 tracers
+  static unsigned long long attr_set[2] = {0, 0};  // per device, bit = device index
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ULL << (dev & 63);
+  if (!(attr_set[tp_f64 ? 1 : 0] & bit)) {
+    cudaError_t e = tp_f64
+        ? cudaFuncSetAttribute(k_mp_step<T_, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               mp_bucket_bytes<double>())
+        : cudaFuncSetAttribute(k_mp_step<T_, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               mp_bucket_bytes<float>());
+    if (e != cudaSuccess) return e;
+    attr_set[tp_f64 ? 1 : 0] |= bit;
+  }
+  if (tp_f64)
+    k_mp_step<T_, double><<<grid, block, mp_bucket_bytes<double>(), L.stream>>>(pop_args(L), L.layout, m, planes);
+  else
+    k_mp_step<T_, float><<<grid, block, mp_bucket_bytes<float>(), L.stream>>>(pop_args(L), L.layout, m, planes);
   count_launch();
   return cudaGetLastError();
 }

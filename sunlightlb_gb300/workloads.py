@@ -306,13 +306,17 @@ def calibrated_flow(L, lb, diameter, re_target=1.0, b0=1e-6, stokes_tol=1e-5, to
 
 
 def tracer_breakthrough(L, lb, steps, precision=1, alpha=0.5, adprob=0.01, sample_every=500, source=1.0):
-    """Passive scalar in the frozen flow of lb: newmp + mpinit, every
-    boundary node adsorbing (adall) with probability adprob per encounter,
-    a constant-concentration plane at x = 0 re-set before every update
-    (mpwall), and the mean tracer over the fluid nodes of the last plane
-    x = esi - 1 every sample_every updates.  Returns (mp, curve, balance)
-    where balance holds the tracer in the fluid, on adsorbing nodes, in
-    total, and the tracer the source added."""
+    """Passive scalar in the frozen flow of lb, carried along x through a
+    column: newmp + mpinit, every boundary node adsorbing (adall) with
+    probability adprob per encounter, a constant-concentration source plane
+    x = 0 (p = source) and an absorbing plane x = esi - 1 (p = 0), both re-set
+    before every update with mpwall.  The absorbing plane keeps the source
+    from reaching the far end through the periodic wrap; the breakthrough
+    curve is the mean tracer over the fluid nodes of the plane before it,
+    x = esi - 2, every sample_every updates.  Returns (mp, curve, balances):
+    curve = [(step, mean)], balances = [(step, fluid, adsorbed, all,
+    injected)] with the tracer the two planes added (the absorbing plane
+    counts negative)."""
     mp = L.newmp(lb, "null")
     if L.extended:
         mp.precision = precision
@@ -320,13 +324,15 @@ def tracer_breakthrough(L, lb, steps, precision=1, alpha=0.5, adprob=0.01, sampl
     mp.alpha = alpha
     L.mpinit(mp)
     L.adall(mp)
-    last = lb.esi - 1
-    curve = []
+    sink = lb.esi - 1
+    probe = max(0, lb.esi - 2)
+    curve, balances = [], []
     for s in range(1, steps + 1):
         L.mpwall(mp, "x", 0, source)
+        L.mpwall(mp, "x", sink, 0.0)
         L.mpstep(mp)
         if s % sample_every == 0 or s == steps:
-            curve.append((s, L.mpplane(mp, "x", last)))
-    balance = {"fluid": L.mptotal(mp, "fluid"), "adsorbed": L.mptotal(mp, "adsorbed"),
-               "all": L.mptotal(mp, "all"), "injected": L.mptotal(mp, "injected")}
-    return mp, curve, balance
+            curve.append((s, L.mpplane(mp, "x", probe)))
+            balances.append((s, L.mptotal(mp, "fluid"), L.mptotal(mp, "adsorbed"), L.mptotal(mp, "all"),
+                             L.mptotal(mp, "injected")))
+    return mp, curve, balances
