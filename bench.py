@@ -577,6 +577,149 @@ def run_tracer(args):
     L.freelb(lb)
 
 
+# ---- batched ensemble of small moving-sphere domains ------------------------
+
+BATCH_SIDES = (24, 32, 40, 48, 56, 64)
+BATCH_RMIN, BATCH_RMAX, BATCH_SPEED, BATCH_SEED = 3.0, 6.0, 1e-3, 2
+
+
+def batch_domains(ndom, seed=BATCH_SEED):
+    """Seeded domains: (side, radius, centre, velocity)."""
+    from sunlightlb_gb300 import workloads as W
+    rng = W.SplitMix64(seed)
+    out = []
+    for _ in range(ndom):
+        side = BATCH_SIDES[min(len(BATCH_SIDES) - 1, int(rng.uniform(0.0, len(BATCH_SIDES))))]
+        rad = rng.uniform(BATCH_RMIN, BATCH_RMAX)
+        centre = [rng.uniform(0.0, side) for _ in range(3)]
+        vel = [BATCH_SPEED * c for c in rng.unit_vector()]
+        out.append((side, rad, centre, vel))
+    return out
+
+
+def build_domain(L, side, rad, centre, vel, precision=1):
+    """Periodic cube with one sphere (and its periodic images, merged into
+    one object) translating at vel: fixed node map, wall velocity spread to
+    the solid nodes (vspread), Stokes flow, tau = 1."""
+    from sunlightlb_gb300 import workloads as W
+    lb = L.newlb(side, side, side, "null")
+    if L.extended:
+        lb.precision = precision
+    lb.tau = 1.0
+    lb.stokes_flow = 1
+    lb.objects_moving = 1
+    for c in W.images((side, side, side), rad, centre):
+        L.insertsph(lb, rad, c[0], c[1], c[2])
+    obj = L.flattenobj(lb)
+    obj.velx, obj.vely, obj.velz = vel
+    L.syncobjs(lb)
+    L.vspread(lb)
+    return lb
+
+
+def drag(lb):
+    o = lb.objects()[0]
+    return [o.frcx, o.frcy, o.frcz]
+
+
+def _oracle_domain(spec, steps, out, slot):
+    L = oracle_lib()
+    lb = build_domain(L, *spec, precision=0)
+    for _ in range(steps):
+        L.lbstep(lb)
+    L.measure(lb)
+    out[slot] = drag(lb)
+
+
+def run_batch(args):
+    """Many independent moving-sphere domains: one persistent launch for
+    all of them (batchsteps) against the same domains one at a time
+    (lbsteps per domain), per-domain drag compared; a seeded subset against
+    the CPU oracle (FP64)."""
+    import torch
+    import sunlightlb_gb300
+
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    L = sunlightlb_gb300.library()
+    specs = batch_domains(args.domains)
+    nodes = sum(s[0] ** 3 for s in specs)
+    steps = args.batch_steps
+    t0 = time.perf_counter()
+    batch = [build_domain(L, *sp) for sp in specs]
+    alone = [build_domain(L, *sp) for sp in specs]
+    t_build = time.perf_counter() - t0
+    for lb in batch + alone:  # upload, first device use
+        L.lbsteps(lb, 2)
+    torch.cuda.synchronize()
+    b = L.newbatch()
+    for lb in batch:
+        L.batchadd(b, lb)
+    L.batchsteps(b, 2)  # set-up, warm-up
+    torch.cuda.synchronize()
+    k0 = L.lbkernelcount()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        L.batchsteps(b, steps)
+        torch.cuda.synchronize()
+        t_batch = time.perf_counter() - t0
+    launches = L.lbkernelcount() - k0
+    t0 = time.perf_counter()
+    for lb in alone:
+        L.lbsteps(lb, steps)
+        torch.cuda.synchronize()  # one domain at a time
+    t_alone = time.perf_counter() - t0
+    worst = 0.0
+    drags = []
+    for lb1, lb2 in zip(batch, alone):
+        L.measure(lb1)
+        L.measure(lb2)
+        d1, d2 = drag(lb1), drag(lb2)
+        drags.append(d1)
+        scale = max(abs(c) for c in d2) or 1.0
+        worst = max(worst, max(abs(x - y) for x, y in zip(d1, d2)) / scale)
+    peak, peak_kind = measured_peak()
+    gbs = BYTES_PER_UPDATE[1] * nodes * steps / t_batch / 1e9
+    line = {
+        "workload": f"batched ensemble: {args.domains} periodic moving-sphere domains, sides {list(BATCH_SIDES)}",
+        "metric": "MLUPS of all domains together, batched (one persistent launch) vs one domain at a time",
+        "config": {"domains": args.domains, "cells": nodes, "steps": steps, "radii": [BATCH_RMIN, BATCH_RMAX],
+                   "speed": BATCH_SPEED, "seed": BATCH_SEED, "tau": 1.0, "flow": "Stokes",
+                   "populations": "fp32", "boundary": "moving-wall link bounce-back on the fixed node map (vspread)"},
+        "build_s": round(t_build, 1),
+        "batched": {"wall_s": round(t_batch, 3), "MLUPS": round(nodes * steps / t_batch / 1e6, 1),
+                    "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
+                    "gpu_launches": launches, "clocks": clk.summary()},
+        "one_at_a_time": {"wall_s": round(t_alone, 3), "MLUPS": round(nodes * steps / t_alone / 1e6, 1)},
+        "speedup": round(t_alone / t_batch, 2),
+        "drag_max_rel_diff_batched_vs_one_at_a_time": worst,
+        "measured_peak_gbs": peak, "peak_kind": peak_kind,
+    }
+    if args.cpu_subset > 0:
+        # the smallest domains, FP64 on the CPU oracle, one thread each
+        sub = sorted(range(len(specs)), key=lambda d: (specs[d][0], d))[:args.cpu_subset]
+        out = [None] * len(sub)
+        t0 = time.perf_counter()
+        ts = [threading.Thread(target=_oracle_domain, args=(specs[d], steps + 4, out, n)) for n, d in enumerate(sub)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        t_cpu = time.perf_counter() - t0
+        rel = []
+        for n, d in enumerate(sub):
+            ref = out[n]
+            scale = max(abs(c) for c in ref) or 1.0
+            rel.append(max(abs(x - y) for x, y in zip(drags[d], ref)) / scale)
+        line["cpu_subset"] = {"domains": sub, "steps": steps + 4, "wall_s": round(t_cpu, 2), "cores": len(sub),
+                              "MLUPS": round(sum(specs[d][0] ** 3 for d in sub) * (steps + 4) / t_cpu / 1e6, 2),
+                              "kind": "port", "drag_max_rel_diff_gpu_fp32_vs_cpu_fp64": max(rel)}
+    print(json.dumps(line), flush=True)
+    L.freebatch(b)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -590,8 +733,12 @@ def main():
     ap.add_argument("--max-converge-steps", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="packed", choices=["packed", "tracer"],
-                    help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive scalar")
+    ap.add_argument("--workload", default="packed", choices=["packed", "tracer", "batch"],
+                    help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive "
+                         "scalar; batch: many small moving-sphere domains in one launch")
+    ap.add_argument("--domains", type=int, default=512, help="batch workload: number of domains")
+    ap.add_argument("--batch-steps", type=int, default=20000)
+    ap.add_argument("--cpu-subset", type=int, default=8, help="batch workload: domains checked on the CPU oracle")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")
     ap.add_argument("--tracer-steps", type=int, default=50000)
     ap.add_argument("--fp64-tracer-steps", type=int, default=10000)
@@ -603,6 +750,8 @@ def main():
         run_reference(args)
     elif args.workload == "tracer":
         run_tracer(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_mine(args)
 

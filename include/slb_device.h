@@ -178,6 +178,19 @@ int slbc_mp_zero_ads(slbc_tracer *t);
 /* dst p += src p on fluid nodes (reference src/mpmisc.c:233-246). */
 int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src);
 
+/* Batches (no counterpart in the reference: its drivers step one lattice at
+ * a time).  A batch advances FP32 or FP64 lattices of one precision, each of
+ * any size, by n fused steps in ONE persistent launch: every block owns
+ * whole lattices (largest first to the least loaded block) and runs all
+ * their steps with block barriers only.  Each lattice keeps its own device
+ * state, so every other call works on it before and after; its stream waits
+ * for the batch.  The lattices must outlive the batch. */
+typedef struct slbc_batch slbc_batch;
+int slbc_batch_create(slbc_batch **out, slbc_lattice *const *lats, int n);
+int slbc_batch_step(slbc_batch *b, int nsteps);
+int slbc_batch_workers(const slbc_batch *b);  /* blocks of the launch */
+void slbc_batch_destroy(slbc_batch *b);
+
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need
  * the result: an application that hands out all device memory from its own

@@ -324,6 +324,19 @@ LBReal mptotal(MPSys, char *);
  * the plane has no fluid node): the breakthrough curve of a front. */
 LBReal mpplane(MPSys, char *, int);
 
+/* Batches (no counterpart in the reference): many independent lattices of
+ * one precision (FP32 or FP64), each set up as usual, advanced together by
+ * batchsteps in one persistent GPU launch; afterwards each lattice is used
+ * as before (measure, lbpull, lbsave ...).  batchsteps(b, n) gives every
+ * lattice the same state as lbsteps(lb, n).  A lattice must outlive the
+ * batches it is in. */
+typedef struct LBBatch_struct *LBBatch;
+LBBatch newbatch(void);
+void batchadd(LBBatch, LBSys);
+void batchsteps(LBBatch, int);
+int batchsize(LBBatch);
+void freebatch(LBBatch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -132,7 +132,9 @@ PROTOS = {
     "lbpull": ("v", "L"), "lbpush": ("v", "L"), "lbsteps": ("v", "Li"),
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
     "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "freemp": ("v", "M"),
-    "lbsetvel": ("v", "LDDDD"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"), "mppull": ("v", "M"), "mppush": ("v", "M"),
+    "lbsetvel": ("v", "LDDDD"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
+    "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"),
+    "freebatch": ("v", "p"), "mppull": ("v", "M"), "mppush": ("v", "M"),
 }
 
 

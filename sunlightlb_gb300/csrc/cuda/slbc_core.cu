@@ -1122,4 +1122,75 @@ int slbc_mp_scale(slbc_tracer *t, double fac) { return mp_misc(t, nullptr, 0, fa
 int slbc_mp_zero_ads(slbc_tracer *t) { return t->h->L.ads ? mp_misc(t, nullptr, 1, 0.0) : 0; }
 int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src) { return mp_misc(dst, src, 2, 0.0); }
 
+// ---- batches of lattices ------------------------------------------------------
+
+struct slbc_batch {
+  BatchState B;
+};
+
+void slbc_batch_destroy(slbc_batch *b) {
+  if (!b) return;
+  BatchState &B = b->B;
+  if (B.stream) cudaStreamSynchronize(B.stream);
+  if (B.doms) cudaFree(B.doms);
+  if (B.work_off) cudaFree(B.work_off);
+  if (B.work) cudaFree(B.work);
+  if (B.done) cudaEventDestroy(B.done);
+  if (B.stream) cudaStreamDestroy(B.stream);
+  delete b;
+}
+
+int slbc_batch_create(slbc_batch **out, slbc_lattice *const *lats, int n) {
+  *out = nullptr;
+  if (n < 1 || lats == nullptr) return fail_msg("slbc_batch_create: a batch needs at least one lattice");
+  const int prec = lats[0] ? lats[0]->L.precision : -1;
+  for (int d = 0; d < n; d++) {
+    if (!lats[d]) return fail_msg("slbc_batch_create: null lattice");
+    if (lats[d]->L.precision != prec)
+      return fail_msg("slbc_batch_create: the lattices of a batch share one precision");
+    for (int e = 0; e < d; e++)
+      if (lats[e] == lats[d]) return fail_msg("slbc_batch_create: a lattice appears twice");
+  }
+  if (prec == 2) return fail_msg("slbc_batch_create: BF16 lattices are not batched (FP32 or FP64 only)");
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  slbc_batch *b = new slbc_batch();
+  BatchState &B = b->B;
+  for (int d = 0; d < n; d++) B.lats.push_back(&lats[d]->L);
+  B.precision = prec;
+  B.sms = sms;
+  cudaError_t e = cudaMalloc(&B.doms, (size_t)n * std::max(sizeof(BatchDom<double>), sizeof(BatchDom<float>)));
+  // block offsets of up to four launches (n + 4 entries) and the lattices
+  if (e == cudaSuccess) e = cudaMalloc(&B.work_off, (n + 4) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&B.work, n * sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    slbc_batch_destroy(b);
+    return fail("slbc_batch_create", e);
+  }
+  *out = b;
+  return 0;
+}
+
+int slbc_batch_workers(const slbc_batch *b) { return b ? b->B.nworkers : 0; }
+
+int slbc_batch_step(slbc_batch *b, int nsteps) {
+  if (nsteps <= 0) return 0;
+  BatchState &B = b->B;
+  for (Lattice *L : B.lats) {
+    if (L->precision != B.precision) return fail_msg("slbc_batch_step: a lattice changed precision");
+    if (to_aa(*L)) return 1;
+    CK(cudaStreamSynchronize(L->stream));  // the batch stream follows every lattice's work
+  }
+  CK(B.precision == 0 ? launch_batch_f64(B, nsteps) : launch_batch_f32(B, nsteps));
+  CK(cudaEventRecord(B.done, B.stream));
+  for (Lattice *L : B.lats) {
+    CK(cudaStreamWaitEvent(L->stream, B.done, 0));  // later work on a lattice follows the batch
+    if (nsteps & 1) L->layout = L->layout == SLBC_LAYOUT_C0 ? SLBC_LAYOUT_C1 : SLBC_LAYOUT_C0;
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "slb_device.h"
@@ -137,7 +138,23 @@ struct ForceArgs {
 };
 
 // Per-precision launchers (defined in slbc_f64.cu / slbc_f32.cu).
+// Device side of a batch of lattices advanced by one persistent launch.
+// Lattices of one batch launch share whether walls move and whether the
+// body force is uniform (the kernel is compiled for each combination); a
+// batch step makes one launch per combination present.
+struct BatchState {
+  std::vector<Lattice *> lats;
+  int precision = 1;
+  int sms = 0;
+  int nworkers = 0;                 // blocks of the last launch
+  void *doms = nullptr;             // BatchDom<T> per lattice
+  int *work_off = nullptr, *work = nullptr;  // lattices of each block (CSR)
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
 #define SLBC_DECLARE_LAUNCHERS(SUFFIX)                                          \
+  cudaError_t launch_batch_##SUFFIX(BatchState &B, int nsteps);                 \
   cudaError_t launch_step_##SUFFIX(Lattice &L, int odd);                        \
   cudaError_t launch_force_##SUFFIX(Lattice &L);                                \
   cudaError_t launch_vsum_##SUFFIX(Lattice &L, double fac, const double *psi,   \

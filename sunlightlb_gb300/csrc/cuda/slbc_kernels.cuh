@@ -175,60 +175,105 @@ __device__ __forceinline__ void apply_wall(T (&t)[15], uint16_t fl, bool solid, 
   }
 }
 
-// One fused update step (bounce-back + streaming + collision) of every node.
+// Fused update (bounce-back + streaming + collision) of node (i, j, k).
 // ODD = false: C1 -> C0 (local), ODD = true: C0 -> C1 (pull and push).
 // MOVING compiles the wall terms in, BFU selects a uniform body force (a
-// kernel constant) over per-node arrays, NPT is the number of rows along j
+// kernel constant) over per-node arrays.
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+__device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, int k) {
+  T *__restrict__ P = a.p.pop;
+  const long long S = a.p.npad;
+  const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, a.p.esk);
+  const int x = nb.at(0, 0, 0);
+  const uint16_t fl = __ldg(a.p.flags + x);
+  const bool solid = (fl & FLAG_SOLID) != 0;
+  T t[15];
+  if (!ODD) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
+  } else {
+    t[0] = P[x];
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> q) & 1;
+      const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+      const int slot = bnd ? q : OPP(q);
+      t[q] = P[slot * S + src];
+    }
+  }
+  if (MOVING && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
+  if (!(a.skip_solid && solid)) {
+    T bx = a.bfx, by = a.bfy, bz = a.bfz;
+    if (!BFU) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
+    collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
+  }
+  if (!ODD) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
+  } else {
+    P[x] = t[0];
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> OPP(q)) & 1;
+      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+      const int slot = bnd ? OPP(q) : q;
+      P[slot * S + dst] = t[q];
+    }
+  }
+}
+
+// One fused update step of every node.  NPT is the number of rows along j
 // one thread updates (more memory requests in flight per thread).
 // Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).
 template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT>
 __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.z;
-  const int esk = a.p.esk;
-  if (k >= esk) return;
-  T *__restrict__ P = a.p.pop;
-  const long long S = a.p.npad;
+  if (k >= a.p.esk) return;
 #pragma unroll
   for (int r = 0; r < NPT; r++) {
     const int j = blockIdx.y * NPT + r;
     if (NPT > 1 && j >= a.p.esj) break;
-    const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, esk);
-    const int x = nb.at(0, 0, 0);
-    const uint16_t fl = __ldg(a.p.flags + x);
-    const bool solid = (fl & FLAG_SOLID) != 0;
-    T t[15];
-    if (!ODD) {
-#pragma unroll
-      for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
-    } else {
-      t[0] = P[x];
-#pragma unroll
-      for (int q = 1; q < 15; q++) {
-        const bool bnd = (fl >> q) & 1;
-        const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
-        const int slot = bnd ? q : OPP(q);
-        t[q] = P[slot * S + src];
-      }
-    }
-    if (MOVING && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
-    if (!(a.skip_solid && solid)) {
-      T bx = a.bfx, by = a.bfy, bz = a.bfz;
-      if (!BFU) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
-      collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
-    }
-    if (!ODD) {
-#pragma unroll
-      for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
-    } else {
-      P[x] = t[0];
-#pragma unroll
-      for (int q = 1; q < 15; q++) {
-        const bool bnd = (fl >> OPP(q)) & 1;
-        const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
-        const int slot = bnd ? OPP(q) : q;
-        P[slot * S + dst] = t[q];
-      }
+    step_node<T, ODD, EXACT, MOVING, BFU>(a, i, j, k);
+  }
+}
+
+// ---- batches of independent lattices ----------------------------------------
+// One persistent launch advances many lattices ("domains") by nsteps fused
+// steps each (the parity of each domain's first step follows its layout).  Block b owns the domains
+// work[work_off[b] .. work_off[b+1]) outright and runs all their steps, one
+// domain after another, with a block barrier between steps: no other block
+// touches a domain, so no block ever waits for another.
+constexpr int kBatchThreads = 512;
+
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+__device__ __forceinline__ void batch_sweep(const StepArgs<T> &a) {
+  const int esj = a.p.esj, esk = a.p.esk;
+  const int n = a.p.esi * esj * esk;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int r = e / esk;
+    step_node<T, ODD, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
+  }
+}
+
+// A domain of a batch: its step arguments and the parity of its first step
+// (1: the domain starts in C0, 0: in C1).
+template <typename T>
+struct BatchDom {
+  StepArgs<T> a;
+  int odd0;
+};
+
+template <typename T, bool EXACT, bool MOVING, bool BFU>
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchDom<T> *doms, const int *work_off,
+                                                            const int *work, int nsteps) {
+  for (int w = work_off[blockIdx.x]; w < work_off[blockIdx.x + 1]; w++) {
+    const StepArgs<T> a = doms[work[w]].a;
+    const int odd0 = doms[work[w]].odd0;
+    for (int s = 0; s < nsteps; s++) {
+      if (((s + odd0) & 1) == 1) batch_sweep<T, true, EXACT, MOVING, BFU>(a);
+      else batch_sweep<T, false, EXACT, MOVING, BFU>(a);
+      __syncthreads();
     }
   }
 }

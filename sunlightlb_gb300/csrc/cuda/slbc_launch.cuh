@@ -3,6 +3,9 @@
 // (f64 / f32) and SLBC_EXACT (follow the reference's division forms).
 #pragma once
 
+#include <algorithm>
+#include <vector>
+
 #include "slbc_kernels.cuh"
 #include "slbc_mp.cuh"
 
@@ -62,6 +65,65 @@ static void step_dispatch(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
     if (a.bf_uniform) step_variant<ODD, false, true>(L, a, npt, bx);
     else step_variant<ODD, false, false>(L, a, npt, bx);
   }
+}
+
+// All lattices of a batch by nsteps steps: descriptors and the block
+// assignment are rebuilt per call (parameter changes between calls are
+// picked up), one launch per (moving walls, uniform body force) class.
+// Assignment: longest processing time first, the largest lattice to the
+// least loaded block, at most two blocks per SM.
+cudaError_t SLBC_FN(launch_batch)(BatchState &B, int nsteps) {
+  const int n = (int)B.lats.size();
+  std::vector<BatchDom<T_>> h(n);
+  std::vector<int> cls(n);
+  for (int d = 0; d < n; d++) {
+    h[d].a = step_args(*B.lats[d]);
+    h[d].odd0 = B.lats[d]->layout == SLBC_LAYOUT_C0 ? 1 : 0;
+    cls[d] = (h[d].a.moving ? 2 : 0) + (h[d].a.bf_uniform ? 1 : 0);
+  }
+  cudaError_t e = cudaMemcpy(B.doms, h.data(), n * sizeof(BatchDom<T_>), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  std::vector<int> off, work;
+  int base_off = 0, base_work = 0;
+  for (int c = 0; c < 4; c++) {
+    std::vector<int> order;
+    for (int d = 0; d < n; d++) if (cls[d] == c) order.push_back(d);
+    if (order.empty()) continue;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return B.lats[a]->nnodes > B.lats[b]->nnodes; });
+    const int W = std::max(1, std::min((int)order.size(), 2 * B.sms));
+    std::vector<long long> load(W, 0);
+    std::vector<std::vector<int>> owned(W);
+    for (int d : order) {
+      int w = 0;
+      for (int v = 1; v < W; v++) if (load[v] < load[w]) w = v;
+      load[w] += B.lats[d]->nnodes;
+      owned[w].push_back(d);
+    }
+    std::vector<int> o(W + 1, 0), wk;
+    for (int w = 0; w < W; w++) {
+      o[w + 1] = o[w] + (int)owned[w].size();
+      wk.insert(wk.end(), owned[w].begin(), owned[w].end());
+    }
+    e = cudaMemcpy(B.work_off + base_off, o.data(), (W + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(B.work + base_work, wk.data(), wk.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    const BatchDom<T_> *D = (const BatchDom<T_> *)B.doms;
+    const int *O = B.work_off + base_off, *K = B.work + base_work;
+    switch (c) {
+      case 0: k_batch<T_, SLBC_EXACT, false, false><<<W, kBatchThreads, 0, B.stream>>>(D, O, K, nsteps); break;
+      case 1: k_batch<T_, SLBC_EXACT, false, true><<<W, kBatchThreads, 0, B.stream>>>(D, O, K, nsteps); break;
+      case 2: k_batch<T_, SLBC_EXACT, true, false><<<W, kBatchThreads, 0, B.stream>>>(D, O, K, nsteps); break;
+      default: k_batch<T_, SLBC_EXACT, true, true><<<W, kBatchThreads, 0, B.stream>>>(D, O, K, nsteps); break;
+    }
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    B.nworkers = W;
+    base_off += W + 1;
+    base_work += (int)wk.size();
+  }
+  return cudaSuccess;
 }
 
 // One fused step with the tuned (rows per thread, threads along k) of this

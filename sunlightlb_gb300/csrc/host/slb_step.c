@@ -7,6 +7,7 @@
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include "slb_private.h"
 
 static void out_of_position(LBSys lb, const char *what) {
@@ -109,6 +110,88 @@ void lbsteps(LBSys lb, int n) {
   slb_device_changed(lb);
   lb->step += n;
   after_collide(lb);
+}
+
+/* ---- batches (appended API) -------------------------------------------- */
+
+struct LBBatch_struct {
+  int n, cap;
+  LBSys *lbs;
+  slbc_batch *dev;          /* device batch of ... */
+  slbc_lattice **dev_lats;  /* ... these device lattices */
+  int dev_n;
+};
+
+LBBatch newbatch(void) {
+  LBBatch b = (LBBatch)calloc(1, sizeof(struct LBBatch_struct));
+  if (b == NULL) error("No room for a batch");
+  return b;
+}
+
+void batchadd(LBBatch b, LBSys lb) {
+  int k;
+  for (k = 0; k < b->n; k++) if (b->lbs[k] == lb) return;
+  if (b->n == b->cap) {
+    b->cap = b->cap ? 2 * b->cap : 16;
+    b->lbs = (LBSys *)realloc(b->lbs, b->cap * sizeof(LBSys));
+    if (b->lbs == NULL) error("No room for a batch");
+  }
+  b->lbs[b->n++] = lb;
+}
+
+int batchsize(LBBatch b) { return b->n; }
+
+void freebatch(LBBatch b) {
+  if (b == NULL) return;
+  if (b->dev) slbc_batch_destroy(b->dev);
+  free(b->dev_lats);
+  free(b->lbs);
+  free(b);
+}
+
+/* every member by n update steps: members out of the collide-stream cycle,
+ * or whose precision differs from the first member's, step on their own */
+void batchsteps(LBBatch b, int n) {
+  slbc_lattice **devs;
+  LBSys *members;
+  int k, m = 0, prec = -1;
+  if (n <= 0 || b->n == 0) return;
+  devs = (slbc_lattice **)malloc(b->n * sizeof(slbc_lattice *));
+  members = (LBSys *)malloc(b->n * sizeof(LBSys));
+  if (devs == NULL || members == NULL) error("No room for a batch");
+  for (k = 0; k < b->n; k++) {
+    LBSys lb = b->lbs[k];
+    if (lb->changed_objects) syncobjs(lb);
+    if (lb->status != POST_COLLIDE || lb->precision == SLB_BF16 || (prec >= 0 && lb->precision != prec)) {
+      lbsteps(lb, n);
+      continue;
+    }
+    prec = lb->precision;
+    devs[m] = slb_device(lb);
+    members[m++] = lb;
+  }
+  if (m > 0) {
+    /* a new device batch when the device lattices changed */
+    int same = b->dev != NULL && b->dev_n == m && memcmp(b->dev_lats, devs, m * sizeof(slbc_lattice *)) == 0;
+    if (!same) {
+      if (b->dev) slbc_batch_destroy(b->dev);
+      b->dev = NULL;
+      slb_check(slbc_batch_create(&b->dev, devs, m), "batch set-up");
+      free(b->dev_lats);
+      b->dev_lats = (slbc_lattice **)malloc(m * sizeof(slbc_lattice *));
+      if (b->dev_lats == NULL) error("No room for a batch");
+      memcpy(b->dev_lats, devs, m * sizeof(slbc_lattice *));
+      b->dev_n = m;
+    }
+    slb_check(slbc_batch_step(b->dev, n), "batch steps");
+    for (k = 0; k < m; k++) {
+      slb_device_changed(members[k]);
+      members[k]->step += n;
+      after_collide(members[k]);
+    }
+  }
+  free(devs);
+  free(members);
 }
 
 /* ---- measurement: reference src/lbmeasure.c ------------------------------ */
