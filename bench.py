@@ -658,6 +658,8 @@ def run_batch(args):
     for lb in batch:
         L.batchadd(b, lb)
     L.batchsteps(b, 2)  # set-up, warm-up
+    for lb in alone:
+        L.lbsteps(lb, 2)  # the same step count
     torch.cuda.synchronize()
     k0 = L.lbkernelcount()
     with Clocks(local) as clk:
@@ -680,18 +682,30 @@ def run_batch(args):
         drags.append(d1)
         scale = max(abs(c) for c in d2) or 1.0
         worst = max(worst, max(abs(x - y) for x, y in zip(d1, d2)) / scale)
+    # the other batch mode (one persistent launch, blocks owning whole
+    # lattices), timed on the same lattices after the drag comparison
+    psteps = max(2, steps // 10)
+    L.batchmode(b, 1)
+    L.batchsteps(b, 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L.batchsteps(b, psteps)
+    torch.cuda.synchronize()
+    t_pers = time.perf_counter() - t0
     peak, peak_kind = measured_peak()
     gbs = BYTES_PER_UPDATE[1] * nodes * steps / t_batch / 1e9
     line = {
         "workload": f"batched ensemble: {args.domains} periodic moving-sphere domains, sides {list(BATCH_SIDES)}",
-        "metric": "MLUPS of all domains together, batched (one persistent launch) vs one domain at a time",
+        "metric": "MLUPS of all domains together, batched vs one domain at a time",
         "config": {"domains": args.domains, "cells": nodes, "steps": steps, "radii": [BATCH_RMIN, BATCH_RMAX],
                    "speed": BATCH_SPEED, "seed": BATCH_SEED, "tau": 1.0, "flow": "Stokes",
                    "populations": "fp32", "boundary": "moving-wall link bounce-back on the fixed node map (vspread)"},
         "build_s": round(t_build, 1),
-        "batched": {"wall_s": round(t_batch, 3), "MLUPS": round(nodes * steps / t_batch / 1e6, 1),
+        "batched": {"mode": "packed tiles, one launch per step, CUDA graph", "wall_s": round(t_batch, 3), "MLUPS": round(nodes * steps / t_batch / 1e6, 1),
                     "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
                     "gpu_launches": launches, "clocks": clk.summary()},
+        "batched_persistent_mode": {"steps": psteps, "wall_s": round(t_pers, 3),
+                                    "MLUPS": round(nodes * psteps / t_pers / 1e6, 1)},
         "one_at_a_time": {"wall_s": round(t_alone, 3), "MLUPS": round(nodes * steps / t_alone / 1e6, 1)},
         "speedup": round(t_alone / t_batch, 2),
         "drag_max_rel_diff_batched_vs_one_at_a_time": worst,

@@ -180,15 +180,20 @@ int slbc_mp_add(slbc_tracer *dst, const slbc_tracer *src);
 
 /* Batches (no counterpart in the reference: its drivers step one lattice at
  * a time).  A batch advances FP32 or FP64 lattices of one precision, each of
- * any size, by n fused steps in ONE persistent launch: every block owns
- * whole lattices (largest first to the least loaded block) and runs all
- * their steps with block barriers only.  Each lattice keeps its own device
+ * any size, by n fused steps.  Persistent mode: ONE launch per class for all
+ * the steps, every block owns whole lattices (largest first to the least
+ * loaded block) and runs all their steps with block barriers only.  Each lattice keeps its own device
  * state, so every other call works on it before and after; its stream waits
  * for the batch.  The lattices must outlive the batch. */
 typedef struct slbc_batch slbc_batch;
 int slbc_batch_create(slbc_batch **out, slbc_lattice *const *lats, int n);
 int slbc_batch_step(slbc_batch *b, int nsteps);
-int slbc_batch_workers(const slbc_batch *b);  /* blocks of the launch */
+int slbc_batch_workers(const slbc_batch *b);  /* blocks of the last persistent launch */
+/* mode 0 (default): each step is one launch per class over the packed cell
+ * index of all lattices (tiles of 256 cells), steps replayed from a CUDA
+ * graph; mode 1: the persistent launch described above.  A class is the
+ * lattices sharing moving walls (or not) and a uniform body force (or not). */
+int slbc_batch_set_mode(slbc_batch *b, int mode);
 void slbc_batch_destroy(slbc_batch *b);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no

@@ -335,6 +335,10 @@ LBBatch newbatch(void);
 void batchadd(LBBatch, LBSys);
 void batchsteps(LBBatch, int);
 int batchsize(LBBatch);
+/* 0 (default): one launch per step over the packed cell index of all the
+ * lattices, replayed from a CUDA graph; 1: one persistent launch for all
+ * the steps, every GPU block owning whole lattices. */
+void batchmode(LBBatch, int);
 void freebatch(LBBatch);
 
 #ifdef __cplusplus

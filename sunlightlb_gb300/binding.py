@@ -133,7 +133,7 @@ PROTOS = {
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
     "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "freemp": ("v", "M"),
     "lbsetvel": ("v", "LDDDD"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
-    "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"),
+    "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"), "batchmode": ("v", "pi"),
     "freebatch": ("v", "p"), "mppull": ("v", "M"), "mppush": ("v", "M"),
 }
 

@@ -1135,6 +1135,7 @@ void slbc_batch_destroy(slbc_batch *b) {
   if (B.doms) cudaFree(B.doms);
   if (B.work_off) cudaFree(B.work_off);
   if (B.work) cudaFree(B.work);
+  if (B.tiles) cudaFree(B.tiles);
   if (B.done) cudaEventDestroy(B.done);
   if (B.stream) cudaStreamDestroy(B.stream);
   delete b;
@@ -1176,6 +1177,12 @@ int slbc_batch_create(slbc_batch **out, slbc_lattice *const *lats, int n) {
 
 int slbc_batch_workers(const slbc_batch *b) { return b ? b->B.nworkers : 0; }
 
+int slbc_batch_set_mode(slbc_batch *b, int mode) {
+  if (mode != 0 && mode != 1) return fail_msg("slbc_batch_set_mode: mode is 0 (tiles) or 1 (persistent)");
+  b->B.mode = mode;
+  return 0;
+}
+
 int slbc_batch_step(slbc_batch *b, int nsteps) {
   if (nsteps <= 0) return 0;
   BatchState &B = b->B;
@@ -1184,7 +1191,39 @@ int slbc_batch_step(slbc_batch *b, int nsteps) {
     if (to_aa(*L)) return 1;
     CK(cudaStreamSynchronize(L->stream));  // the batch stream follows every lattice's work
   }
-  CK(B.precision == 0 ? launch_batch_f64(B, nsteps) : launch_batch_f32(B, nsteps));
+  if (B.mode == 1) {
+    CK(B.precision == 0 ? launch_batch_f64(B, nsteps) : launch_batch_f32(B, nsteps));
+  } else {
+    CK(B.precision == 0 ? prepare_tiles_f64(B) : prepare_tiles_f32(B));
+    auto one = [&](int s) { return B.precision == 0 ? launch_tiles_f64(B, s) : launch_tiles_f32(B, s); };
+    // 50 steps (an even number: the parity pattern repeats) per graph replay
+    const int G = 50;
+    int done = 0;
+    if (nsteps >= 2 * G) {
+      cudaGraph_t g;
+      cudaGraphExec_t ge = nullptr;
+      CK(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = cudaSuccess;
+      for (int s = 0; s < G && ce == cudaSuccess; s++) ce = one(s);
+      const cudaError_t ee = cudaStreamEndCapture(B.stream, &g);
+      if (ce != cudaSuccess) return fail("slbc_batch_step: capture", ce);
+      if (ee != cudaSuccess) return fail("slbc_batch_step: cudaStreamEndCapture", ee);
+      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail("slbc_batch_step: cudaGraphInstantiate", ie);
+      int nclass = 0;
+      for (int c = 0; c < 4; c++) nclass += B.class_tiles[c] > 0;
+      count_launch(-G * nclass);  // the captured launches run only in the replays
+      for (; done + G <= nsteps; done += G) {
+        const cudaError_t le = cudaGraphLaunch(ge, B.stream);
+        if (le != cudaSuccess) { cudaGraphExecDestroy(ge); return fail("slbc_batch_step: cudaGraphLaunch", le); }
+        count_launch(G * nclass);
+      }
+      CK(cudaStreamSynchronize(B.stream));
+      cudaGraphExecDestroy(ge);
+    }
+    for (; done < nsteps; done++) CK(one(done));
+  }
   CK(cudaEventRecord(B.done, B.stream));
   for (Lattice *L : B.lats) {
     CK(cudaStreamWaitEvent(L->stream, B.done, 0));  // later work on a lattice follows the batch

@@ -142,19 +142,29 @@ struct ForceArgs {
 // Lattices of one batch launch share whether walls move and whether the
 // body force is uniform (the kernel is compiled for each combination); a
 // batch step makes one launch per combination present.
+// Two ways to run it: mode 0 (tiles), one launch per class and step over the
+// packed cell index of all lattices, steps replayed from a CUDA graph;
+// mode 1 (persistent), one launch per class for all the steps, every block
+// owning whole lattices.
 struct BatchState {
   std::vector<Lattice *> lats;
   int precision = 1;
+  int mode = 0;
   int sms = 0;
-  int nworkers = 0;                 // blocks of the last launch
+  int nworkers = 0;                 // blocks of the last persistent launch
   void *doms = nullptr;             // BatchDom<T> per lattice
-  int *work_off = nullptr, *work = nullptr;  // lattices of each block (CSR)
+  int *work_off = nullptr, *work = nullptr;  // persistent: lattices of each block (CSR)
+  int2 *tiles = nullptr;            // tiles: (lattice, first cell), grouped by class
+  long long tiles_cap = 0;
+  int class_tiles[4] = {0, 0, 0, 0};
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
 };
 
 #define SLBC_DECLARE_LAUNCHERS(SUFFIX)                                          \
   cudaError_t launch_batch_##SUFFIX(BatchState &B, int nsteps);                 \
+  cudaError_t prepare_tiles_##SUFFIX(BatchState &B);                             \
+  cudaError_t launch_tiles_##SUFFIX(BatchState &B, int step);                    \
   cudaError_t launch_step_##SUFFIX(Lattice &L, int odd);                        \
   cudaError_t launch_force_##SUFFIX(Lattice &L);                                \
   cudaError_t launch_vsum_##SUFFIX(Lattice &L, double fac, const double *psi,   \

@@ -278,6 +278,28 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchDom<T> *d
   }
 }
 
+// Packed cell index of a batch: every domain is cut into tiles of
+// kBatchTile consecutive cells, tile t = (domain, first cell).  One launch
+// updates every tile of one (moving walls, uniform force) class by one step;
+// a domain's parity follows its first-step parity odd0 and the step number.
+constexpr int kBatchTile = 256;
+
+template <typename T, bool EXACT, bool MOVING, bool BFU>
+__global__ void __launch_bounds__(kBatchTile) k_batch_tiles(const BatchDom<T> *doms, const int2 *tiles,
+                                                            int step) {
+  __shared__ BatchDom<T> dom;
+  const int2 tile = tiles[blockIdx.x];
+  if (threadIdx.x == 0) dom = doms[tile.x];
+  __syncthreads();
+  const StepArgs<T> &a = dom.a;
+  const int esj = a.p.esj, esk = a.p.esk;
+  const int e = tile.y + threadIdx.x;
+  if (e >= a.p.esi * esj * esk) return;
+  const int r = e / esk;
+  if (((step + dom.odd0) & 1) == 1) step_node<T, true, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
+  else step_node<T, false, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
+}
+
 // Explicitly rounded add / multiply: never contracted into FMA, so the
 // reduction kernels give the same bits whatever -fmad a translation unit uses.
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }

@@ -126,6 +126,58 @@ cudaError_t SLBC_FN(launch_batch)(BatchState &B, int nsteps) {
   return cudaSuccess;
 }
 
+// Tiles mode: descriptors and the tile table of every class (rebuilt per
+// batch step call).
+cudaError_t SLBC_FN(prepare_tiles)(BatchState &B) {
+  const int n = (int)B.lats.size();
+  std::vector<BatchDom<T_>> h(n);
+  std::vector<int2> tiles;
+  for (int d = 0; d < n; d++) {
+    h[d].a = step_args(*B.lats[d]);
+    h[d].odd0 = B.lats[d]->layout == SLBC_LAYOUT_C0 ? 1 : 0;
+  }
+  for (int c = 0; c < 4; c++) {
+    const size_t first = tiles.size();
+    for (int d = 0; d < n; d++) {
+      if ((h[d].a.moving ? 2 : 0) + (h[d].a.bf_uniform ? 1 : 0) != c) continue;
+      for (long long e = 0; e < B.lats[d]->nnodes; e += kBatchTile) tiles.push_back(make_int2(d, (int)e));
+    }
+    B.class_tiles[c] = (int)(tiles.size() - first);
+  }
+  cudaError_t e = cudaMemcpy(B.doms, h.data(), n * sizeof(BatchDom<T_>), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  if ((long long)tiles.size() > B.tiles_cap) {
+    if (B.tiles) cudaFree(B.tiles);
+    B.tiles = nullptr;
+    B.tiles_cap = 0;
+    e = cudaMalloc(&B.tiles, tiles.size() * sizeof(int2));
+    if (e != cudaSuccess) return e;
+    B.tiles_cap = (long long)tiles.size();
+  }
+  return cudaMemcpy(B.tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice);
+}
+
+// Tiles mode: one step (step = position in the sequence, for the parity).
+cudaError_t SLBC_FN(launch_tiles)(BatchState &B, int step) {
+  const BatchDom<T_> *D = (const BatchDom<T_> *)B.doms;
+  const int2 *t = B.tiles;
+  for (int c = 0; c < 4; c++) {
+    const int nt = B.class_tiles[c];
+    if (nt == 0) continue;
+    switch (c) {
+      case 0: k_batch_tiles<T_, SLBC_EXACT, false, false><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
+      case 1: k_batch_tiles<T_, SLBC_EXACT, false, true><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
+      case 2: k_batch_tiles<T_, SLBC_EXACT, true, false><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
+      default: k_batch_tiles<T_, SLBC_EXACT, true, true><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
+    }
+    count_launch();
+    t += nt;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // One fused step with the tuned (rows per thread, threads along k) of this
 // parity; small lattices use one row per thread and the block width that
 // fits esk.

@@ -116,6 +116,7 @@ void lbsteps(LBSys lb, int n) {
 
 struct LBBatch_struct {
   int n, cap;
+  int mode;
   LBSys *lbs;
   slbc_batch *dev;          /* device batch of ... */
   slbc_lattice **dev_lats;  /* ... these device lattices */
@@ -140,6 +141,11 @@ void batchadd(LBBatch b, LBSys lb) {
 }
 
 int batchsize(LBBatch b) { return b->n; }
+
+void batchmode(LBBatch b, int mode) {
+  if (mode != 0 && mode != 1) { printf("Batch mode is 0 (packed tiles) or 1 (persistent)\n"); return; }
+  b->mode = mode;
+}
 
 void freebatch(LBBatch b) {
   if (b == NULL) return;
@@ -183,6 +189,7 @@ void batchsteps(LBBatch b, int n) {
       memcpy(b->dev_lats, devs, m * sizeof(slbc_lattice *));
       b->dev_n = m;
     }
+    slb_check(slbc_batch_set_mode(b->dev, b->mode), "batch mode");
     slb_check(slbc_batch_step(b->dev, n), "batch steps");
     for (k = 0; k < m; k++) {
       slb_device_changed(members[k]);

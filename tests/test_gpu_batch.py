@@ -40,10 +40,14 @@ def build(L, precision, **kw):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("steps", [37, 120])
-def test_batch_equals_one_at_a_time(gpu, precision, steps):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_equals_one_at_a_time(gpu, precision, steps, mode):
+    """mode 0: packed tiles (120 steps include two graph replays); mode 1:
+    persistent launch."""
     batch = build(gpu, precision)
     alone = build(gpu, precision)
     b = gpu.newbatch()
+    gpu.batchmode(b, mode)
     for lb in batch:
         gpu.batchadd(b, lb)
     assert gpu.batchsize(b) == len(DOMAINS)
@@ -68,6 +72,7 @@ def test_batch_fp64_equals_oracle(gpu, orc):
     for lb in batch:
         gpu.batchadd(b, lb)
     gpu.batchsteps(b, 25)
+    gpu.batchmode(b, 1)
     gpu.batchsteps(b, 30)  # the batch is reused, each lattice continues
     for lb in ref:
         for _ in range(55):
