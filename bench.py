@@ -31,6 +31,7 @@ The JSON line carries:
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -680,8 +681,7 @@ def run_batch(args):
         L.measure(lb2)
         d1, d2 = drag(lb1), drag(lb2)
         drags.append(d1)
-        scale = max(abs(c) for c in d2) or 1.0
-        worst = max(worst, max(abs(x - y) for x, y in zip(d1, d2)) / scale)
+        worst = max(worst, max(abs(x - y) for x, y in zip(d1, d2)))
     # the other batch mode (one persistent launch, blocks owning whole
     # lattices), timed on the same lattices after the drag comparison
     psteps = max(2, steps // 10)
@@ -708,7 +708,7 @@ def run_batch(args):
                                     "MLUPS": round(nodes * psteps / t_pers / 1e6, 1)},
         "one_at_a_time": {"wall_s": round(t_alone, 3), "MLUPS": round(nodes * steps / t_alone / 1e6, 1)},
         "speedup": round(t_alone / t_batch, 2),
-        "drag_max_rel_diff_batched_vs_one_at_a_time": worst,
+        "drag_max_abs_diff_batched_vs_one_at_a_time": worst,
         "measured_peak_gbs": peak, "peak_kind": peak_kind,
     }
     if args.cpu_subset > 0:
@@ -722,14 +722,17 @@ def run_batch(args):
         for t in ts:
             t.join()
         t_cpu = time.perf_counter() - t0
+        # the drag decays as the periodic fluid picks up the sphere's motion,
+        # so differences are scaled by the Stokes drag 6 pi eta a |v|
+        eta = 72.0 * (1.0 - 0.5) / 3.0
         rel = []
         for n, d in enumerate(sub):
             ref = out[n]
-            scale = max(abs(c) for c in ref) or 1.0
+            scale = 6.0 * math.pi * eta * specs[d][1] * BATCH_SPEED
             rel.append(max(abs(x - y) for x, y in zip(drags[d], ref)) / scale)
         line["cpu_subset"] = {"domains": sub, "steps": steps + 4, "wall_s": round(t_cpu, 2), "cores": len(sub),
                               "MLUPS": round(sum(specs[d][0] ** 3 for d in sub) * (steps + 4) / t_cpu / 1e6, 2),
-                              "kind": "port", "drag_max_rel_diff_gpu_fp32_vs_cpu_fp64": max(rel)}
+                              "kind": "port", "drag_max_diff_over_stokes_drag_gpu_fp32_vs_cpu_fp64": max(rel)}
     print(json.dumps(line), flush=True)
     L.freebatch(b)
 

@@ -196,6 +196,16 @@ int slbc_batch_workers(const slbc_batch *b);  /* blocks of the last persistent l
 int slbc_batch_set_mode(slbc_batch *b, int mode);
 void slbc_batch_destroy(slbc_batch *b);
 
+/* Tensor-core kernels of the learned warm start (no counterpart in the
+ * reference).  slbc_tc_gemm: D[M x N] (FP32, row-major, leading dimension
+ * ldd) = A[M x K] * B[N x K]^T, A and B BF16 row-major; M and N multiples of
+ * 128, K of 64, device pointers 16-byte aligned; launched on `stream`.
+ * slbc_tc_status synchronises the device and returns (and clears) the error
+ * flag of these kernels: 0 fine, 1 a pipeline wait gave up, 2 a load never
+ * landed, -1 the device could not be read. */
+int slbc_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, int ldd, void *stream);
+int slbc_tc_status(void);
+
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need
  * the result: an application that hands out all device memory from its own
