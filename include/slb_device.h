@@ -205,6 +205,20 @@ void slbc_batch_destroy(slbc_batch *b);
  * landed, -1 the device could not be read. */
 int slbc_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, int ldd, void *stream);
 int slbc_tc_status(void);
+/* Periodic 3x3x3 convolution (implicit GEMM on the tensor cores).  Buffers
+ * are channels-last BF16 with a one-voxel periodic halo,
+ * buf[n][z + 1][y + 1][x + 1][c] of B x (D+2) x (H+2) x (W+2) x ctot.
+ * Reads input channels [in_coff, in_coff + cin) (cin a multiple of 32),
+ * weights w[tap][cin/32][cout][32] (tap = 9 dz + 3 dy + dx for the neighbour
+ * offset (dx-1, dy-1, dz-1)), adds bias (or none), applies ReLU if relu,
+ * multiplies by (mask > 0) if mask is given (same layout as out), and writes
+ * the interior of output channels [out_coff, out_coff + cout) (cout a
+ * multiple of 16 up to 256).  D, H, W powers of two with D*H*W >= 128. */
+int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin, const void *wgt,
+                   const float *bias, int cout, void *out, int out_ctot, int out_coff, int relu, const void *mask,
+                   void *stream);
+/* Fill the periodic halo of channels [coff, coff + nch) of such a buffer. */
+int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int nch, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

@@ -46,3 +46,77 @@ def test_gemm_rejects_bad_shapes(gpu):
     D = torch.zeros(128, 128, device="cuda")
     assert gemm(A.data_ptr(), A.data_ptr(), D.data_ptr(), 100, 128, 64, 128, None) != 0
     assert gemm(A.data_ptr(), A.data_ptr(), D.data_ptr(), 128, 128, 48, 128, None) != 0
+
+
+def conv_fns(gpu):
+    f = gpu.dll.slbc_tc_conv3d
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p] + [C.c_int] * 7 + [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                                   C.c_int, C.c_void_p, C.c_void_p]
+    h = gpu.dll.slbc_tc_halo
+    h.restype = C.c_int
+    h.argtypes = [C.c_void_p] + [C.c_int] * 7 + [C.c_void_p]
+    return f, h
+
+
+def to_padded(torch, x, ctot, coff):
+    """(B, C, D, H, W) -> channels-last buffer with a 1-voxel halo (interior
+    filled at channels [coff, coff + C), the rest zero)."""
+    B, Cc, D, H, W = x.shape
+    buf = torch.zeros(B, D + 2, H + 2, W + 2, ctot, device="cuda", dtype=torch.bfloat16)
+    buf[:, 1:-1, 1:-1, 1:-1, coff:coff + Cc] = x.permute(0, 2, 3, 4, 1).to(torch.bfloat16)
+    return buf
+
+
+def gemm_weights(torch, wt):
+    """torch weight (cout, cin, 3, 3, 3) -> w[tap][cin/32][cout][32], tap = 9 kz + 3 ky + kx."""
+    cout, cin = wt.shape[:2]
+    w = wt.permute(2, 3, 4, 0, 1).reshape(27, cout, cin // 32, 32).permute(0, 2, 1, 3)
+    return w.contiguous().to(torch.bfloat16)
+
+
+CONV_CASES = [  # B, D, H, W, cin, cout, in_ctot, in_coff, out_ctot, out_coff, relu, mask
+    (2, 8, 8, 8, 32, 32, 32, 0, 32, 0, 0, 0),
+    (1, 16, 16, 16, 64, 48, 96, 32, 64, 8, 1, 0),
+    (1, 8, 32, 32, 96, 128, 96, 0, 128, 0, 1, 1),
+    (1, 4, 4, 64, 32, 256, 32, 0, 256, 0, 0, 0),
+    (1, 2, 2, 128, 32, 16, 40, 8, 24, 8, 0, 0),
+]
+
+
+@pytest.mark.parametrize("case", CONV_CASES)
+def test_conv3d_matches_torch(gpu, case):
+    torch = pytest.importorskip("torch")
+    F = torch.nn.functional
+    conv, halo = conv_fns(gpu)
+    B, D, H, W, cin, cout, in_ctot, in_coff, out_ctot, out_coff, relu, use_mask = case
+    g = torch.Generator(device="cuda").manual_seed(sum(case))
+    x = torch.randn(B, cin, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
+    wt = (torch.randn(cout, cin, 3, 3, 3, device="cuda", generator=g) / (27 * cin) ** 0.5).to(torch.bfloat16).float()
+    bias = torch.randn(cout, device="cuda", generator=g) * 0.1
+    st = torch.cuda.current_stream().cuda_stream
+    xin = to_padded(torch, x, in_ctot, in_coff)
+    assert halo(xin.data_ptr(), B, D, H, W, in_ctot, 0, in_ctot, st) == 0
+    ref_pad = F.pad(x, (1, 1, 1, 1, 1, 1), mode="circular").permute(0, 2, 3, 4, 1)
+    assert torch.equal(xin[..., in_coff:in_coff + cin].float(), ref_pad)  # the halo
+    w = gemm_weights(torch, wt)
+    out = torch.full((B, D + 2, H + 2, W + 2, out_ctot), 7.0, device="cuda", dtype=torch.bfloat16)
+    ref = F.conv3d(F.pad(x, (1, 1, 1, 1, 1, 1), mode="circular"), wt, bias)
+    if relu:
+        ref = ref.clamp_min(0.0)
+    mask_buf = None
+    if use_mask:
+        mk = torch.randn(B, cout, D, H, W, device="cuda", generator=g)
+        mask_buf = to_padded(torch, mk, out_ctot, out_coff)
+        ref = ref * (mk.to(torch.bfloat16).float() > 0)
+    rc = conv(xin.data_ptr(), B, D, H, W, in_ctot, in_coff, cin, w.data_ptr(), bias.data_ptr(), cout,
+              out.data_ptr(), out_ctot, out_coff, relu, mask_buf.data_ptr() if use_mask else None, st)
+    assert rc == 0, gpu.dll.slbc_last_error
+    assert gpu.dll.slbc_tc_status() == 0
+    got = out[:, 1:-1, 1:-1, 1:-1, out_coff:out_coff + cout].float().permute(0, 4, 1, 2, 3)
+    scale = ref.abs().max().item()
+    assert ((got - ref).abs() <= 4e-3 * ref.abs() + 2e-3 * scale).all()
+    # nothing outside the written interior slice
+    untouched = out.clone()
+    untouched[:, 1:-1, 1:-1, 1:-1, out_coff:out_coff + cout] = 7.0
+    assert (untouched.float() == 7.0).all()
