@@ -219,6 +219,22 @@ int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int 
                    void *stream);
 /* Fill the periodic halo of channels [coff, coff + nch) of such a buffer. */
 int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int nch, void *stream);
+/* Channel-major flat copy of channels [coff, coff + nch) of such a buffer
+ * for the weight gradients: dst[c][n * pstride + (z * (H+2) + y) * Wp + x] =
+ * src[n][z][y][x - shift][coff + c] (0 outside; zero_halo keeps interior
+ * voxels only).  Wp a multiple of 8 >= W + 2, pstride a multiple of 64 >=
+ * (D+2) * (H+2) * Wp, shift -1, 0 or 1. */
+int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
+                   long long pstride, int shift, int zero_halo, void *dst, void *stream);
+/* Weight gradient of slbc_tc_conv3d: dw[tap][cout][cin] (FP32) = sum over
+ * voxels u of dY[u - off(tap)][co] * X[u][ci], from channel-major copies:
+ * dy0, dy1, dy2 = dY with its periodic halo at shift -1, 0, 1 (shift =
+ * dx - 1 for the taps of dx = 0, 1, 2), xt = X with a zero halo at shift 0.  K is split over `splits`
+ * blocks into partial (splits * 27 * cout * cin floats) summed in order.
+ * cout 32, 64, 128 or a multiple of 128; cin a multiple of 16. */
+int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
+                  int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
+                  float *dw, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

@@ -350,6 +350,176 @@ bool make_map_rows32(CUtensorMap *map, const void *ptr, long long rows, int box_
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// ---- weight gradients ------------------------------------------------------------
+// dW[tap][co][ci] = sum_u dY[u - off(tap)][co] * X[u][ci] over all voxels u
+// of all samples.  Both operands are channel-major with K = voxels flattened
+// over the padded volume: row pitch Wp (a multiple of 8, >= W + 2), plane
+// (H + 2) * Wp, sample stride pstride (a multiple of 64).  X's copy has a
+// zero halo, so halo positions add nothing; dY's three copies S_dx (dx =
+// 0, 1, 2) carry the periodic halo and the x part of the tap offset, so the
+// y and z parts are aligned flat shifts of the TMA box.  Taps are stacked
+// along M (128 rows = taps x output channels); K is split over blocks into
+// FP32 partial sums, added in a fixed order afterwards.
+struct WgradArgs {
+  int cin, cout, co_rows, taps_per_tile, co_tiles;
+  int ntile;
+  int Wp;
+  int plane;
+  long long k_tiles;
+  int splits;
+  int tmem_cols;
+  float *partial;  // [splits][27][cout][cin]
+};
+
+constexpr int kWgTileA = 128 * 128;  // 128 rows x 64 K x 2 B
+constexpr int kWgTileB = 256 * 128;  // up to 256 rows
+constexpr int kWgSmem = kStages * (kWgTileA + kWgTileB) + 1024;
+
+__global__ void __launch_bounds__(128, 1)
+k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap a1,
+        const __grid_constant__ CUtensorMap a2, const __grid_constant__ CUtensorMap tb, WgradArgs w, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *tA = smem_raw + pad;
+  uint8_t *tB = tA + kStages * kWgTileA;
+  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint32_t tmem_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int group = blockIdx.x / w.co_tiles, cot = blockIdx.x % w.co_tiles;
+  const int tap0 = group * w.taps_per_tile, co0 = cot * w.co_rows, ci0 = blockIdx.y * w.ntile;
+  const long long per = (w.k_tiles + w.splits - 1) / w.splits;
+  const long long k_lo = (long long)blockIdx.z * per;
+  const long long k_hi = k_lo + per < w.k_tiles ? k_lo + per : w.k_tiles;
+  const int nk = k_hi > k_lo ? (int)(k_hi - k_lo) : 0;
+  const uint32_t bytes_a = 128u * 128u, bytes_b = (uint32_t)w.ntile * 128u;
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, (uint32_t)w.tmem_cols);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < kStages; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  int issued = 0;
+  if (threadIdx.x == 0) {
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (kt >= kStages && !tc::mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      const int k0 = (int)((k_lo + kt) * 64);
+      tc::mbar_expect_tx(&full[s], bytes_a + bytes_b);
+      for (int tl = 0; tl < w.taps_per_tile; tl++) {
+        const int tap = tap0 + tl < 27 ? tap0 + tl : 26;  // rows past tap 26 are discarded
+        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+        const int x = k0 - (dy - 1) * w.Wp - (dz - 1) * w.plane;
+        const CUtensorMap *am = dx == 0 ? &a0 : (dx == 1 ? &a1 : &a2);
+        tc::tma_load_2d(tA + s * kWgTileA + tl * w.co_rows * 128, am, &full[s], x, co0);
+      }
+      tc::tma_load_2d(tB + s * kWgTileB, &tb, &full[s], k0, ci0);
+      issued = kt + 1;
+    }
+  } else if (threadIdx.x == 32) {
+    const uint32_t idesc = tc::idesc_bf16(128, w.ntile);
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (!tc::mbar_wait(&full[s], (kt / kStages) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const uint64_t ad = tc::smem_desc(tA + s * kWgTileA, tc::kSwizzle128, 128);
+      const uint64_t bd = tc::smem_desc(tB + s * kWgTileB, tc::kSwizzle128, 128);
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, idesc, (kt | kk) != 0);
+      tc::mma_commit(&empty[s]);
+    }
+    tc::mma_commit(&done);
+  }
+  __syncwarp();
+  const bool okd = __all_sync(0xffffffffu, tc::mbar_wait(&done, 0, kWaitLimit));
+  tc::fence_after_sync();
+  if (okd) {
+    const int r = warp * 32 + lane;
+    const int tap = tap0 + r / w.co_rows, co = co0 + r % w.co_rows;
+    float *dst = w.partial + (((long long)blockIdx.z * 27 + tap) * w.cout + co) * w.cin + ci0;
+#pragma unroll 1
+    for (int c = 0; c < w.ntile; c += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (nk == 0) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = 0.0f;
+      }
+      if (tap < 27) {
+        ((float4 *)(dst + c))[0] = make_float4(v[0], v[1], v[2], v[3]);
+        ((float4 *)(dst + c))[1] = make_float4(v[4], v[5], v[6], v[7]);
+      }
+    }
+  }
+  if (!ok || !okd) atomicExch(err, 1);
+  if (threadIdx.x == 0) {
+    for (int kt = issued > kStages ? issued - kStages : 0; kt < issued; kt++)
+      if (!tc::mbar_wait(&full[kt % kStages], (kt / kStages) & 1, kWaitLimit)) atomicExch(err, 2);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)w.tmem_cols);
+}
+
+// dw[i] = sum over splits of partial[s][i], in split order
+__global__ void k_sum_splits(const float *partial, long long n, int splits, float *dw) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = 0.0f;
+    for (int s = 0; s < splits; s++) v += partial[(long long)s * n + i];
+    dw[i] = v;
+  }
+}
+
+// Channel-major flat copy of channels [coff, coff + nch) of a padded
+// channels-last buffer: dst[c][n * pstride + (z * (H + 2) + y) * Wp + x] =
+// src[n][z][y][x - shift][coff + c] for 0 <= x - shift <= W + 1 (0 beyond;
+// zero_halo: interior voxels only, every halo position 0).
+__global__ void k_cmajor(const __nv_bfloat16 *src, int B, int D, int H, int W, int ctot, int coff, int nch,
+                         int Wp, long long pstride, int shift, int zero_halo, __nv_bfloat16 *dst) {
+  const long long plane = (long long)(H + 2) * Wp;
+  const long long per_sample = (long long)(D + 2) * plane;
+  const long long total = (long long)B * pstride;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(e / pstride);
+    const long long f = e % pstride;
+    bool in = f < per_sample;
+    int z = 0, y = 0, x = 0;
+    if (in) {
+      z = (int)(f / plane);
+      const long long r = f % plane;
+      y = (int)(r / Wp);
+      x = (int)(r % Wp) - shift;
+      in = x >= 0 && x <= W + 1;
+      if (zero_halo) in = in && x >= 1 && x <= W && y >= 1 && y <= H && z >= 1 && z <= D;
+    }
+    const __nv_bfloat16 *sp = in ? src + ((((long long)n * (D + 2) + z) * (H + 2) + y) * (W + 2) + x) * ctot + coff
+                                 : nullptr;
+    for (int c = 0; c < nch; c++) dst[(long long)c * total + e] = in ? sp[c] : __float2bfloat16(0.0f);
+  }
+}
+
+// 2-D map: rows x cols BF16 (cols contiguous), box 64 x box_rows (128-byte swizzle)
+bool make_map_k64(CUtensorMap *map, const void *ptr, long long rows, long long cols, int box_rows) {
+  return make_map_2d(map, ptr, rows, cols, box_rows);
+}
+
 // M tile of 128 voxels for a D x H x W grid: false when the grid does not
 // tile (sides powers of two with W * H * D >= 128 do)
 bool tile_shape(int D, int H, int W, int &wbox, int &hbox, int &dbox) {
@@ -440,6 +610,76 @@ int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int 
   slbc::count_launch();
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_halo: ") + cudaGetErrorString(e)), 1;
+  return 0;
+}
+
+int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
+                   long long pstride, int shift, int zero_halo, void *dst, void *stream) {
+  if (B < 1 || nch < 1 || coff < 0 || coff + nch > ctot || Wp < W + 2 || Wp % 8 || pstride % 64 ||
+      pstride < (long long)(D + 2) * (H + 2) * Wp || shift < -1 || shift > 1)
+    return slbc::set_error("slbc_tc_cmajor: bad geometry"), 1;
+  const long long total = (long long)B * pstride;
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+  k_cmajor<<<blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, B, D, H, W, ctot, coff, nch, Wp,
+                                                     pstride, shift, zero_halo, (__nv_bfloat16 *)dst);
+  slbc::count_launch();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_cmajor: ") + cudaGetErrorString(e)), 1;
+  return 0;
+}
+
+int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
+                  int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
+                  float *dw, void *stream) {
+  WgradArgs w;
+  if (cout < 32 || (cout > 128 && cout % 128) || (cout <= 128 && 128 % cout) || cin < 16 || cin % 16)
+    return slbc::set_error("slbc_tc_wgrad: cout must be 32, 64, 128 or a multiple of 128; cin a multiple of 16"), 1;
+  if (Wp < W + 2 || Wp % 8 || pstride % 64 || pstride < (long long)(D + 2) * (H + 2) * Wp || splits < 1)
+    return slbc::set_error("slbc_tc_wgrad: bad geometry"), 1;
+  w.cin = cin; w.cout = cout;
+  w.co_rows = cout < 128 ? cout : 128;
+  w.taps_per_tile = 128 / w.co_rows;
+  w.co_tiles = cout / w.co_rows;
+  w.ntile = cin;
+  while (w.ntile > 256) w.ntile /= 2;
+  if (cin % w.ntile || w.ntile % 16) return slbc::set_error("slbc_tc_wgrad: cin does not split into N tiles"), 1;
+  w.Wp = Wp;
+  w.plane = (H + 2) * Wp;
+  w.k_tiles = (long long)B * pstride / 64;
+  w.splits = splits;
+  w.tmem_cols = 32;
+  while (w.tmem_cols < w.ntile) w.tmem_cols *= 2;
+  w.partial = partial;
+  if (partial_floats < (long long)splits * 27 * cout * cin)
+    return slbc::set_error("slbc_tc_wgrad: partial buffer too small"), 1;
+  if (!aligned16(dy0) || !aligned16(dy1) || !aligned16(dy2) || !aligned16(xt) || !aligned16(partial) ||
+      !aligned16(dw))
+    return slbc::set_error("slbc_tc_wgrad: buffers must be 16-byte aligned"), 1;
+  int *err = tc_err_flag();
+  if (!err) return slbc::set_error("slbc_tc_wgrad: no device error flag"), 1;
+  const long long cols = (long long)B * pstride;
+  CUtensorMap m0, m1, m2, mb;
+  if (!make_map_k64(&m0, dy0, cout, cols, w.co_rows) || !make_map_k64(&m1, dy1, cout, cols, w.co_rows) ||
+      !make_map_k64(&m2, dy2, cout, cols, w.co_rows) || !make_map_k64(&mb, xt, cin, cols, w.ntile))
+    return slbc::set_error("slbc_tc_wgrad: tensor map encoding failed"), 1;
+  static std::once_flag attr;
+  cudaError_t e = cudaSuccess;
+  std::call_once(attr, [&] {
+    e = cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem);
+  });
+  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
+  const dim3 grid((unsigned)(((27 + w.taps_per_tile - 1) / w.taps_per_tile) * w.co_tiles), (unsigned)(cin / w.ntile),
+                  (unsigned)splits);
+  k_wgrad<<<grid, 128, kWgSmem, (cudaStream_t)stream>>>(m0, m1, m2, mb, w, err);
+  slbc::count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
+  const long long n = 27LL * cout * cin;
+  k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(partial, n,
+                                                                                                        splits, dw);
+  slbc::count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
   return 0;
 }
 

@@ -120,3 +120,63 @@ def test_conv3d_matches_torch(gpu, case):
     untouched = out.clone()
     untouched[:, 1:-1, 1:-1, 1:-1, out_coff:out_coff + cout] = 7.0
     assert (untouched.float() == 7.0).all()
+
+
+def wgrad_fns(gpu):
+    cm = gpu.dll.slbc_tc_cmajor
+    cm.restype = C.c_int
+    cm.argtypes = [C.c_void_p] + [C.c_int] * 8 + [C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    wg = gpu.dll.slbc_tc_wgrad
+    wg.restype = C.c_int
+    wg.argtypes = [C.c_void_p] * 4 + [C.c_int] * 5 + [C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
+                                                     C.c_int, C.c_void_p, C.c_void_p]
+    return cm, wg
+
+
+def flat_geometry(D, H, W):
+    Wp = (W + 2 + 7) // 8 * 8
+    pstride = ((D + 2) * (H + 2) * Wp + 63) // 64 * 64
+    return Wp, pstride
+
+
+WGRAD_CASES = [  # B, D, H, W, cin, cout, splits
+    (1, 8, 8, 8, 32, 32, 3),
+    (2, 16, 16, 16, 96, 64, 7),
+    (1, 8, 16, 32, 64, 128, 5),
+    (1, 8, 8, 8, 384, 256, 2),
+    (1, 16, 16, 16, 32, 32, 40),
+]
+
+
+@pytest.mark.parametrize("case", WGRAD_CASES)
+def test_wgrad_matches_torch(gpu, case):
+    torch = pytest.importorskip("torch")
+    F = torch.nn.functional
+    _, halo = conv_fns(gpu)
+    cm, wg = wgrad_fns(gpu)
+    B, D, H, W, cin, cout, splits = case
+    g = torch.Generator(device="cuda").manual_seed(sum(case) + 11)
+    x = torch.randn(B, cin, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
+    dy = torch.randn(B, cout, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
+    st = torch.cuda.current_stream().cuda_stream
+    xb = to_padded(torch, x, cin, 0)
+    yb = to_padded(torch, dy, cout, 0)
+    assert halo(xb.data_ptr(), B, D, H, W, cin, 0, cin, st) == 0
+    assert halo(yb.data_ptr(), B, D, H, W, cout, 0, cout, st) == 0
+    Wp, pstride = flat_geometry(D, H, W)
+    xt = torch.empty(cin, B * pstride, device="cuda", dtype=torch.bfloat16)
+    assert cm(xb.data_ptr(), B, D, H, W, cin, 0, cin, Wp, pstride, 0, 1, xt.data_ptr(), st) == 0
+    dys = []
+    for shift in (-1, 0, 1):
+        t = torch.empty(cout, B * pstride, device="cuda", dtype=torch.bfloat16)
+        assert cm(yb.data_ptr(), B, D, H, W, cout, 0, cout, Wp, pstride, shift, 0, t.data_ptr(), st) == 0
+        dys.append(t)
+    partial = torch.empty(splits * 27 * cout * cin, device="cuda")
+    dw = torch.empty(27, cout, cin, device="cuda")
+    rc = wg(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), B, D, H, W, Wp, pstride, cin,
+            cout, partial.data_ptr(), partial.numel(), splits, dw.data_ptr(), st)
+    assert rc == 0, gpu.dll.slbc_last_error
+    assert gpu.dll.slbc_tc_status() == 0
+    ref = torch.nn.grad.conv3d_weight(F.pad(x, (1, 1, 1, 1, 1, 1), mode="circular"), (cout, cin, 3, 3, 3), dy)
+    ref = ref.permute(2, 3, 4, 0, 1).reshape(27, cout, cin)
+    assert (dw - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
