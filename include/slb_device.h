@@ -196,6 +196,15 @@ int slbc_batch_workers(const slbc_batch *b);  /* blocks of the last persistent l
 int slbc_batch_set_mode(slbc_batch *b, int mode);
 void slbc_batch_destroy(slbc_batch *b);
 
+/* Velocity field of the post-collision state into three device FP32 arrays
+ * u[0..n), u[n..2n), u[2n..3n): (sum_q c_q a_q + fac * b) / (rho0 + sum_q a_q)
+ * on fluid nodes (the per-node accvmean term, reference
+ * src/lbmeasure.c:58-106), 0 on solid nodes.  FP32 and FP64 lattices. */
+int slbc_get_velocity_dev(slbc_lattice *h, double fac, float *u);
+/* Velocity warm start from three device FP32 arrays (as slbc_set_velocity
+ * with rho = rho0; velocities already rescaled): layout N. */
+int slbc_set_velocity_dev(slbc_lattice *h, const float *u, int skip_solid);
+
 /* Tensor-core kernels of the learned warm start (no counterpart in the
  * reference).  slbc_tc_gemm: D[M x N] (FP32, row-major, leading dimension
  * ldd) = A[M x K] * B[N x K]^T, A and B BF16 row-major; M and N multiples of
@@ -217,6 +226,11 @@ int slbc_tc_status(void);
 int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin, const void *wgt,
                    const float *bias, int cout, void *out, int out_ctot, int out_coff, int relu, const void *mask,
                    void *stream);
+/* The same with FP32 output (out_ctot a multiple of 4), no ReLU, no mask:
+ * the network's last layer. */
+int slbc_tc_conv3d_f32(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin,
+                       const void *wgt, const float *bias, int cout, float *out, int out_ctot, int out_coff,
+                       void *stream);
 /* Fill the periodic halo of channels [coff, coff + nch) of such a buffer. */
 int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int nch, void *stream);
 /* Channel-major flat copy of channels [coff, coff + nch) of such a buffer
@@ -235,6 +249,41 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream);
+
+/* Network glue of the learned warm start (same buffers; channel slices
+ * [coff, coff + C) with C, coff, ctot multiples of 8; D, H, W the fine grid).
+ * pool: 2x2x2 average fine -> coarse interior.  pool_bwd: dfine = (dcoarse
+ * / 8 + add) * (mask > 0), add and mask optional.  up: nearest upsampling
+ * coarse -> fine interior.  up_bwd: dcoarse = sum of the 8 children *
+ * (mask > 0).  bias_grad: db[c] += sum of g over interior voxels (C / 8
+ * dividing 256).  wfwd: forward weights w[tap][cin/32][cout][32] from
+ * master[tap][cout][cin] (FP32).  wdgrad: weights of the input gradient for
+ * input channels [ci0, ci0 + nci): w[t][cout/32][nci][32] =
+ * master[26 - t][32 ck + j][ci0 + ci].  adam: Adam step t >= 1.  mse: loss
+ * += mean (pred[0..2] - label)^2 (pred FP32 channels 0..2 of a padded
+ * buffer, label [n][D][H][W][3]), grad (BF16, gctot channels) = its
+ * derivative in channels 0..2, 0 in the others.  encode: channel 0 = 1 on
+ * solid nodes, the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
+ * solid) into u[c * N + e], the layout of lbsetveldev. */
+int slbc_nn_pool(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
+                 int W, int C, void *stream);
+int slbc_nn_pool_bwd(const void *dcoarse, int dc_ctot, int dc_coff, void *dfine, int df_ctot, int df_coff,
+                     const void *add, int a_ctot, int a_coff, const void *mask, int m_ctot, int m_coff, int B, int D,
+                     int H, int W, int C, void *stream);
+int slbc_nn_up(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
+               int W, int C, void *stream);
+int slbc_nn_up_bwd(const void *dfine, int df_ctot, int df_coff, void *dcoarse, int dc_ctot, int dc_coff,
+                   const void *mask, int m_ctot, int m_coff, int B, int D, int H, int W, int C, void *stream);
+int slbc_nn_bias_grad(const void *g, int ctot, int coff, int B, int D, int H, int W, int C, float *db, void *stream);
+int slbc_nn_wfwd(const float *master, int cout, int cin, void *w, void *stream);
+int slbc_nn_wdgrad(const float *master, int cout, int cin, int ci0, int nci, void *w, void *stream);
+int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
+                 int t, void *stream);
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, void *grad, int gctot,
+                double *loss, void *stream);
+int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, void *stream);
+int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
+                   float *u, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

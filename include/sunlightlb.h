@@ -314,6 +314,13 @@ void mppush(MPSys);
  * rho = rho0): the population rebuild of lbloadvel (reference
  * src/lbstore.c:340-401) followed by a collision. */
 void lbsetvel(LBSys, LBReal *, LBReal *, LBReal *, LBReal *);
+/* The same from three FP32 device arrays u[0..n), u[n..2n), u[2n..3n) with
+ * rho = rho0 (a velocity field computed on the GPU, e.g. a learned
+ * prediction, never crosses to the host). */
+void lbsetveldev(LBSys, void *);
+/* Velocity field (the per-node accvmean term, half-force corrected when
+ * lb->vel_corrected) into three FP32 device arrays laid out as above. */
+void lbvelocity(LBSys, void *);
 /* Tracer totals over "fluid", "solid", "adsorbed" or "all" nodes (the sums
  * that mpcheck and adtotal print, reference src/mpmisc.c:121-136), or
  * "injected": the tracer that mpall, mpslab, mpwall, mpsph and mpcyl have
@@ -323,6 +330,11 @@ LBReal mptotal(MPSys, char *);
 /* Mean tracer over the fluid nodes of the plane "x"/"y"/"z" = pos (0 when
  * the plane has no fluid node): the breakthrough curve of a front. */
 LBReal mpplane(MPSys, char *, int);
+
+/* One object made of the nodes where mask[inode] != 0, inode =
+ * esk*(esj*i+j)+k: the node list of insertlist (reference
+ * src/lbobjs.c:128-165) held in memory instead of a file. */
+LBObj insertmask(LBSys, unsigned char *);
 
 /* Batches (no counterpart in the reference): many independent lattices of
  * one precision (FP32 or FP64), each set up as usual, advanced together by

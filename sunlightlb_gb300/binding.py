@@ -105,7 +105,7 @@ PROTOS = {
     "lbstep": ("v", "L"), "bbl": ("v", "L"), "bblforce": ("v", "L"),
     "propagate": ("v", "L"), "collide": ("v", "L"),
     "lookupobj": ("O", "Li"), "addobj": ("O", "L"), "zeroobj": ("v", "O"),
-    "insertsubs": ("O", "Lsiiiiii"), "insertlist": ("O", "Ls"),
+    "insertsubs": ("O", "Lsiiiiii"), "insertlist": ("O", "Ls"), "insertmask": ("O", "Lp"),
     "insertslab": ("O", "Ldddddd"), "insertsph": ("O", "Ldddd"),
     "insertcyl": ("O", "Lsddd"), "insertwall": ("O", "Lsi"),
     "flattenobj": ("O", "L"), "invertobj": ("O", "L"), "removeobjs": ("v", "L"),
@@ -132,7 +132,7 @@ PROTOS = {
     "lbpull": ("v", "L"), "lbpush": ("v", "L"), "lbsteps": ("v", "Li"),
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
     "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "freemp": ("v", "M"),
-    "lbsetvel": ("v", "LDDDD"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
+    "lbsetvel": ("v", "LDDDD"), "lbsetveldev": ("v", "Lp"), "lbvelocity": ("v", "Lp"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
     "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"), "batchmode": ("v", "pi"),
     "freebatch": ("v", "p"), "mppull": ("v", "M"), "mppush": ("v", "M"),
 }

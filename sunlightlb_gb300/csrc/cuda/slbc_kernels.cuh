@@ -640,4 +640,41 @@ __global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long l
   for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = t[q];
 }
 
+// Velocity field u = (sum_q c_q a_q + fac * b) / (rho0 + sum_q a_q) of the
+// post-collision state (any layout) on fluid nodes, 0 on solid nodes, as
+// three FP32 arrays (the per-node form of the accvmean sum).
+template <typename T>
+__global__ void k_velocity(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double b0, double b1,
+                           double b2, const T *bf, float *u) {
+  const long long n = (long long)p.esi * p.esj * p.esk;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)e;
+    const uint16_t fl = p.flags[x];
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    if (!(fl & FLAG_SOLID)) {
+      int i, j, k;
+      decode(x, p.esj, p.esk, i, j, k);
+      const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+      double r = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+#pragma unroll
+      for (int q = 0; q < 15; q++) {
+        const double v = (double)post_value<T>(p.pop, p.npad, layout, q, x, fl, nb);
+        r += v;
+        mx += CX(q) * v;
+        my += CY(q) * v;
+        mz += CZ(q) * v;
+      }
+      double bx = b0, by = b1, bz = b2;
+      if (!bf_uniform) { bx = bf[x]; by = bf[p.npad + x]; bz = bf[2 * p.npad + x]; }
+      const double inv = 1.0 / (rho0 + r);
+      ux = (float)((mx + fac * bx) * inv);
+      uy = (float)((my + fac * by) * inv);
+      uz = (float)((mz + fac * bz) * inv);
+    }
+    u[x] = ux;
+    u[n + x] = uy;
+    u[2 * n + x] = uz;
+  }
+}
+
 }  // namespace slbc

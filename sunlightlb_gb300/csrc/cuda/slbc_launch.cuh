@@ -270,6 +270,14 @@ cudaError_t SLBC_FN(launch_setvel)(Lattice &L, const double *stage, long long x0
   return cudaGetLastError();
 }
 
+cudaError_t SLBC_FN(launch_velocity)(Lattice &L, double fac, float *u) {
+  const int blocks = (int)std::min<long long>((L.nnodes + 255) / 256, 152LL * 16);
+  k_velocity<T_><<<blocks, 256, 0, L.stream>>>(pop_args(L), L.layout, L.par.rho0, fac, L.bf_uniform, L.bf_const[0],
+                                               L.bf_const[1], L.bf_const[2], (const T_ *)L.bf, u);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t SLBC_FN(launch_mp_rhoinit)(Lattice &L) {
   k_mp_rhoinit<T_><<<flat_blocks(L.nnodes, 256), 256, 0, L.stream>>>(
       pop_args(L), L.layout, L.par.rho0, L.mp_rho64, L.mp_rho32);

@@ -1,0 +1,411 @@
+// Glue kernels of the learned warm start's network: pooling and
+// upsampling between resolution levels (with their gradients, the ReLU masks
+// and the skip-connection sums fused in), bias gradients, weight layouts for
+// the tensor-core convolutions, Adam, the loss and the input encoding.
+//
+// Activation buffers are channels-last BF16 with a one-voxel periodic halo,
+// buf[n][z + 1][y + 1][x + 1][c], total channels ctot, and a kernel works on
+// a channel slice [coff, coff + C); C and coff multiples of 8 (16-byte
+// vectors of 8 channels).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <string>
+
+#include "slbc_internal.cuh"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+struct Slice {
+  bf16 *p;
+  int ctot, coff;
+};
+
+__device__ __forceinline__ long long vox(int n, int z, int y, int x, int D, int H, int W) {
+  return (((long long)n * (D + 2) + z + 1) * (H + 2) + y + 1) * (W + 2) + x + 1;
+}
+
+__device__ __forceinline__ void load8(const bf16 *p, float (&v)[8]) {
+  const uint4 u = *(const uint4 *)p;
+  const __nv_bfloat162 *h = (const __nv_bfloat162 *)&u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 f = __bfloat1622float2(h[i]);
+    v[2 * i] = f.x;
+    v[2 * i + 1] = f.y;
+  }
+}
+
+__device__ __forceinline__ void store8(bf16 *p, const float (&v)[8]) {
+  uint4 u;
+  __nv_bfloat162 *h = (__nv_bfloat162 *)&u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+  *(uint4 *)p = u;
+}
+
+int grid_for(long long n) { return (int)std::min<long long>((n + 255) / 256, 152LL * 32); }
+
+// 2x2x2 average of the fine interior (D, H, W) into the coarse interior
+__global__ void k_pool(Slice in, Slice out, int B, int D, int H, int W, int C) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2, nv = C / 8;
+  const long long total = (long long)B * Dc * Hc * Wc * nv;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int cv = (int)(e % nv);
+    long long r = e / nv;
+    const int x = (int)(r % Wc); r /= Wc;
+    const int y = (int)(r % Hc); r /= Hc;
+    const int z = (int)(r % Dc);
+    const int n = (int)(r / Dc);
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      float v[8];
+      load8(in.p + vox(n, 2 * z + (c >> 2), 2 * y + ((c >> 1) & 1), 2 * x + (c & 1), D, H, W) * in.ctot + in.coff +
+                8 * cv,
+            v);
+#pragma unroll
+      for (int i = 0; i < 8; i++) acc[i] += v[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[i] *= 0.125f;
+    store8(out.p + vox(n, z, y, x, Dc, Hc, Wc) * out.ctot + out.coff + 8 * cv, acc);
+  }
+}
+
+// gradient of k_pool: dfine = (dcoarse / 8 + add) * (mask > 0); add and mask
+// optional (null pointers)
+__global__ void k_pool_bwd(Slice dcoarse, Slice dfine, Slice add, Slice mask, int B, int D, int H, int W, int C) {
+  const int nv = C / 8;
+  const long long total = (long long)B * D * H * W * nv;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int cv = (int)(e % nv);
+    long long r = e / nv;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    float g[8];
+    load8(dcoarse.p + vox(n, z / 2, y / 2, x / 2, D / 2, H / 2, W / 2) * dcoarse.ctot + dcoarse.coff + 8 * cv, g);
+#pragma unroll
+    for (int i = 0; i < 8; i++) g[i] *= 0.125f;
+    const long long v = vox(n, z, y, x, D, H, W);
+    if (add.p) {
+      float a[8];
+      load8(add.p + v * add.ctot + add.coff + 8 * cv, a);
+#pragma unroll
+      for (int i = 0; i < 8; i++) g[i] += a[i];
+    }
+    if (mask.p) {
+      float m[8];
+      load8(mask.p + v * mask.ctot + mask.coff + 8 * cv, m);
+#pragma unroll
+      for (int i = 0; i < 8; i++) g[i] = m[i] > 0.0f ? g[i] : 0.0f;
+    }
+    store8(dfine.p + v * dfine.ctot + dfine.coff + 8 * cv, g);
+  }
+}
+
+// nearest upsampling: fine (D, H, W) interior = coarse parent
+__global__ void k_up(Slice in, Slice out, int B, int D, int H, int W, int C) {
+  const int nv = C / 8;
+  const long long total = (long long)B * D * H * W * nv;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int cv = (int)(e % nv);
+    long long r = e / nv;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    *(uint4 *)(out.p + vox(n, z, y, x, D, H, W) * out.ctot + out.coff + 8 * cv) =
+        *(const uint4 *)(in.p + vox(n, z / 2, y / 2, x / 2, D / 2, H / 2, W / 2) * in.ctot + in.coff + 8 * cv);
+  }
+}
+
+// gradient of k_up: dcoarse = sum of the 8 children * (mask > 0) (coarse mask)
+__global__ void k_up_bwd(Slice dfine, Slice dcoarse, Slice mask, int B, int D, int H, int W, int C) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2, nv = C / 8;
+  const long long total = (long long)B * Dc * Hc * Wc * nv;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int cv = (int)(e % nv);
+    long long r = e / nv;
+    const int x = (int)(r % Wc); r /= Wc;
+    const int y = (int)(r % Hc); r /= Hc;
+    const int z = (int)(r % Dc);
+    const int n = (int)(r / Dc);
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      float v[8];
+      load8(dfine.p + vox(n, 2 * z + (c >> 2), 2 * y + ((c >> 1) & 1), 2 * x + (c & 1), D, H, W) * dfine.ctot +
+                dfine.coff + 8 * cv,
+            v);
+#pragma unroll
+      for (int i = 0; i < 8; i++) acc[i] += v[i];
+    }
+    const long long v = vox(n, z, y, x, Dc, Hc, Wc);
+    if (mask.p) {
+      float m[8];
+      load8(mask.p + v * mask.ctot + mask.coff + 8 * cv, m);
+#pragma unroll
+      for (int i = 0; i < 8; i++) acc[i] = m[i] > 0.0f ? acc[i] : 0.0f;
+    }
+    store8(dcoarse.p + v * dcoarse.ctot + dcoarse.coff + 8 * cv, acc);
+  }
+}
+
+// db[c] += sum over interior voxels of g.  The grid stride is a multiple of
+// C / 8, so a thread always handles the same 8 channels: it sums in
+// registers and adds to the block's shared sums once.
+__global__ void k_bias_grad(Slice g, int B, int D, int H, int W, int C, float *db) {
+  extern __shared__ float sh[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) sh[c] = 0.0f;
+  __syncthreads();
+  const int nv = C / 8;
+  const long long total = (long long)B * D * H * W * nv;
+  const long long start = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int cv = (int)(start % nv);
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long e = start; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e / nv;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    float v[8];
+    load8(g.p + vox(n, z, y, x, D, H, W) * g.ctot + g.coff + 8 * cv, v);
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[i] += v[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 8; i++) atomicAdd(&sh[8 * cv + i], acc[i]);
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sh[c]);
+}
+
+// forward weights: w[tap][cin/32][cout][32] from master m[tap][cout][cin]
+__global__ void k_wfwd(const float *m, int cout, int cin, bf16 *w) {
+  const long long n = 27LL * cout * cin;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % 32);
+    long long r = e / 32;
+    const int co = (int)(r % cout); r /= cout;
+    const int ck = (int)(r % (cin / 32));
+    const int tap = (int)(r / (cin / 32));
+    w[e] = __float2bfloat16(m[((long long)tap * cout + co) * cin + ck * 32 + j]);
+  }
+}
+
+// dgrad weights for input channels [ci0, ci0 + nci): the forward kernel with
+// these weights maps dY (cout channels) to dX: w[t][cout/32][nci][32] =
+// m[26 - t][32 ck + j][ci0 + ci]
+__global__ void k_wdgrad(const float *m, int cout, int cin, int ci0, int nci, bf16 *w) {
+  const long long n = 27LL * nci * cout;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % 32);
+    long long r = e / 32;
+    const int ci = (int)(r % nci); r /= nci;
+    const int ck = (int)(r % (cout / 32));
+    const int t = (int)(r / (cout / 32));
+    w[e] = __float2bfloat16(m[((long long)(26 - t) * cout + ck * 32 + j) * cin + ci0 + ci]);
+  }
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// loss = mean over voxels and the 3 components of (pred - label)^2, pred in
+// FP32 channels 0..2 of a padded buffer (ctot_p channels), label
+// [n][D][H][W][3] FP32; grad (BF16, gctot channels, padded) = d loss /
+// d pred in channels 0..2, 0 in the others.  loss[0] += the sum / count.
+__global__ void k_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, bf16 *grad,
+                      int gctot, double *loss) {
+  __shared__ double sh[256];
+  const long long total = (long long)B * D * H * W;
+  const double inv = 1.0 / (3.0 * (double)total);
+  double acc = 0.0;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    const long long v = vox(n, z, y, x, D, H, W);
+    bf16 *gp = grad + v * gctot;
+    for (int c = 0; c < gctot; c += 8) *(uint4 *)(gp + c) = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float d = pred[v * ctot_p + c] - label[e * 3 + c];
+      acc += (double)d * d;
+      gp[c] = __float2bfloat16((float)(2.0 * inv) * d);
+    }
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, sh[0] * inv);
+}
+
+// input encoding: channel 0 = 1 on solid nodes, 0 on fluid; channels
+// 1 .. ctot-1 zero (interior; the halo is filled afterwards)
+__global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W, bf16 *out, int ctot) {
+  const long long total = (long long)B * D * H * W;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    bf16 *p = out + vox(n, z, y, x, D, H, W) * ctot;
+    for (int c = 0; c < ctot; c += 8) *(uint4 *)(p + c) = make_uint4(0, 0, 0, 0);
+    p[0] = __float2bfloat16(solid[e] ? 1.0f : 0.0f);
+  }
+}
+
+// prediction (FP32 channels 0..2 of a padded buffer) * scale on fluid
+// nodes into three FP32 arrays u[c * N + e] (0 on solid nodes), the layout
+// of lbsetveldev
+__global__ void k_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
+                         float *u) {
+  const long long total = (long long)D * H * W;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H);
+    const int z = (int)(r / H);
+    const long long v = vox(0, z, y, x, D, H, W);
+#pragma unroll
+    for (int c = 0; c < 3; c++) u[c * total + e] = solid[e] ? 0.0f : scale * pred[v * ctot_p + c];
+  }
+}
+
+bool ok8(int ctot, int coff, int C) { return ctot % 8 == 0 && coff % 8 == 0 && C % 8 == 0 && C > 0 && coff + C <= ctot; }
+
+int launched(const char *what) {
+  slbc::count_launch();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    slbc::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return 1;
+  }
+  return 0;
+}
+
+int bad(const char *msg) {
+  slbc::set_error(msg);
+  return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int slbc_nn_pool(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
+                 int W, int C, void *stream) {
+  if (!ok8(in_ctot, in_coff, C) || !ok8(out_ctot, out_coff, C) || D % 2 || H % 2 || W % 2)
+    return bad("slbc_nn_pool: channel slices must be multiples of 8 and the grid even");
+  const long long n = (long long)B * (D / 2) * (H / 2) * (W / 2) * (C / 8);
+  k_pool<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Slice{(bf16 *)in, in_ctot, in_coff},
+                                                        Slice{(bf16 *)out, out_ctot, out_coff}, B, D, H, W, C);
+  return launched("slbc_nn_pool");
+}
+
+int slbc_nn_pool_bwd(const void *dcoarse, int dc_ctot, int dc_coff, void *dfine, int df_ctot, int df_coff,
+                     const void *add, int a_ctot, int a_coff, const void *mask, int m_ctot, int m_coff, int B, int D,
+                     int H, int W, int C, void *stream) {
+  if (!ok8(dc_ctot, dc_coff, C) || !ok8(df_ctot, df_coff, C) || (add && !ok8(a_ctot, a_coff, C)) ||
+      (mask && !ok8(m_ctot, m_coff, C)) || D % 2 || H % 2 || W % 2)
+    return bad("slbc_nn_pool_bwd: channel slices must be multiples of 8 and the grid even");
+  const long long n = (long long)B * D * H * W * (C / 8);
+  k_pool_bwd<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(
+      Slice{(bf16 *)dcoarse, dc_ctot, dc_coff}, Slice{(bf16 *)dfine, df_ctot, df_coff},
+      Slice{(bf16 *)add, a_ctot, a_coff}, Slice{(bf16 *)mask, m_ctot, m_coff}, B, D, H, W, C);
+  return launched("slbc_nn_pool_bwd");
+}
+
+int slbc_nn_up(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
+               int W, int C, void *stream) {
+  if (!ok8(in_ctot, in_coff, C) || !ok8(out_ctot, out_coff, C) || D % 2 || H % 2 || W % 2)
+    return bad("slbc_nn_up: channel slices must be multiples of 8 and the grid even");
+  const long long n = (long long)B * D * H * W * (C / 8);
+  k_up<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Slice{(bf16 *)in, in_ctot, in_coff},
+                                                      Slice{(bf16 *)out, out_ctot, out_coff}, B, D, H, W, C);
+  return launched("slbc_nn_up");
+}
+
+int slbc_nn_up_bwd(const void *dfine, int df_ctot, int df_coff, void *dcoarse, int dc_ctot, int dc_coff,
+                   const void *mask, int m_ctot, int m_coff, int B, int D, int H, int W, int C, void *stream) {
+  if (!ok8(df_ctot, df_coff, C) || !ok8(dc_ctot, dc_coff, C) || (mask && !ok8(m_ctot, m_coff, C)) || D % 2 ||
+      H % 2 || W % 2)
+    return bad("slbc_nn_up_bwd: channel slices must be multiples of 8 and the grid even");
+  const long long n = (long long)B * (D / 2) * (H / 2) * (W / 2) * (C / 8);
+  k_up_bwd<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Slice{(bf16 *)dfine, df_ctot, df_coff},
+                                                          Slice{(bf16 *)dcoarse, dc_ctot, dc_coff},
+                                                          Slice{(bf16 *)mask, m_ctot, m_coff}, B, D, H, W, C);
+  return launched("slbc_nn_up_bwd");
+}
+
+int slbc_nn_bias_grad(const void *g, int ctot, int coff, int B, int D, int H, int W, int C, float *db, void *stream) {
+  if (!ok8(ctot, coff, C) || C > 1024 || 256 % (C / 8)) return bad("slbc_nn_bias_grad: bad channel slice");
+  const long long n = (long long)B * D * H * W * (C / 8);
+  k_bias_grad<<<std::min(grid_for(n), 152 * 4), 256, C * sizeof(float), (cudaStream_t)stream>>>(
+      Slice{(bf16 *)g, ctot, coff}, B, D, H, W, C, db);
+  return launched("slbc_nn_bias_grad");
+}
+
+int slbc_nn_wfwd(const float *master, int cout, int cin, void *w, void *stream) {
+  if (cin % 32 || cout < 1) return bad("slbc_nn_wfwd: cin must be a multiple of 32");
+  k_wfwd<<<grid_for(27LL * cout * cin), 256, 0, (cudaStream_t)stream>>>(master, cout, cin, (bf16 *)w);
+  return launched("slbc_nn_wfwd");
+}
+
+int slbc_nn_wdgrad(const float *master, int cout, int cin, int ci0, int nci, void *w, void *stream) {
+  if (cout % 32 || ci0 < 0 || nci < 1 || ci0 + nci > cin) return bad("slbc_nn_wdgrad: bad channel range");
+  k_wdgrad<<<grid_for(27LL * cout * nci), 256, 0, (cudaStream_t)stream>>>(master, cout, cin, ci0, nci, (bf16 *)w);
+  return launched("slbc_nn_wdgrad");
+}
+
+int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
+                 int t, void *stream) {
+  if (t < 1) return bad("slbc_nn_adam: step count starts at 1");
+  const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
+  k_adam<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  return launched("slbc_nn_adam");
+}
+
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, void *grad, int gctot,
+                double *loss, void *stream) {
+  if (ctot_p < 3 || gctot % 8 || gctot < 8) return bad("slbc_nn_mse: bad channel counts");
+  k_mse<<<std::min(grid_for((long long)B * D * H * W), 152 * 4), 256, 0, (cudaStream_t)stream>>>(
+      pred, ctot_p, label, B, D, H, W, (bf16 *)grad, gctot, loss);
+  return launched("slbc_nn_mse");
+}
+
+int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, void *stream) {
+  if (ctot % 8 || ctot < 8) return bad("slbc_nn_encode: bad channel count");
+  k_encode<<<grid_for((long long)B * D * H * W), 256, 0, (cudaStream_t)stream>>>(solid, B, D, H, W, (bf16 *)out, ctot);
+  return launched("slbc_nn_encode");
+}
+
+int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
+                   float *u, void *stream) {
+  if (ctot_p < 3) return bad("slbc_nn_decode: bad channel count");
+  k_decode<<<grid_for((long long)D * H * W), 256, 0, (cudaStream_t)stream>>>(pred, ctot_p, solid, D, H, W, scale, u);
+  return launched("slbc_nn_decode");
+}
+
+}  // extern "C"

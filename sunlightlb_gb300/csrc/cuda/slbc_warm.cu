@@ -180,6 +180,7 @@ struct ConvArgs {
   const float *bias;         // cout values or null
   const __nv_bfloat16 *mask; // or null: output *= (mask > 0), same layout as out
   __nv_bfloat16 *out;
+  float *out_f32;            // or null: FP32 output (same layout) instead of out
 };
 
 constexpr int kConvTileA = 128 * 64;       // 128 voxels x 32 channels x 2 B
@@ -278,11 +279,17 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
 #pragma unroll
         for (int i = 0; i < 8; i++) v[i] = __bfloat162float(mb[i]) > 0.0f ? v[i] : 0.0f;
       }
-      uint4 o;
-      __nv_bfloat162 *ob = (__nv_bfloat162 *)&o;
+      if (a.out_f32) {
+        float4 *fd = (float4 *)(a.out_f32 + vox * a.out_ctot + a.out_coff + c);
+        fd[0] = make_float4(v[0], v[1], v[2], v[3]);
+        fd[1] = make_float4(v[4], v[5], v[6], v[7]);
+      } else {
+        uint4 o;
+        __nv_bfloat162 *ob = (__nv_bfloat162 *)&o;
 #pragma unroll
-      for (int i = 0; i < 4; i++) ob[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-      *(uint4 *)(dst + c) = o;
+        for (int i = 0; i < 4; i++) ob[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        *(uint4 *)(dst + c) = o;
+      }
     }
   }
   if (!ok || !okd) atomicExch(err, 1);
@@ -558,10 +565,13 @@ int slbc_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, in
   return 0;
 }
 
-int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin, const void *wgt,
-                   const float *bias, int cout, void *out, int out_ctot, int out_coff, int relu, const void *mask,
-                   void *stream) {
+static int conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin, const void *wgt,
+                  const float *bias, int cout, void *out, float *out_f32, int out_ctot, int out_coff, int relu,
+                  const void *mask, void *stream) {
   ConvArgs a;
+  if (!out == !out_f32) return slbc::set_error("slbc_tc_conv3d: exactly one output buffer"), 1;
+  if (out_f32 && out_ctot % 4) return slbc::set_error("slbc_tc_conv3d_f32: out_ctot must be a multiple of 4"), 1;
+  if (!out) out = out_f32;  // alignment checks below
   if (B < 1 || cin < 32 || cin % 32 || cout < 16 || cout > 256 || cout % 16)
     return slbc::set_error("slbc_tc_conv3d: cin must be a multiple of 32, cout a multiple of 16 up to 256"), 1;
   if (in_ctot % 8 || in_coff % 8 || in_coff + cin > in_ctot || out_ctot % 8 || out_coff % 8 ||
@@ -585,7 +595,8 @@ int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int 
   while (a.tmem_cols < cout) a.tmem_cols *= 2;
   a.bias = bias;
   a.mask = (const __nv_bfloat16 *)mask;
-  a.out = (__nv_bfloat16 *)out;
+  a.out = out_f32 ? nullptr : (__nv_bfloat16 *)out;
+  a.out_f32 = out_f32;
   static std::once_flag attr;
   cudaError_t e = cudaSuccess;
   std::call_once(attr, [&] {
@@ -598,6 +609,20 @@ int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int 
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_conv3d: ") + cudaGetErrorString(e)), 1;
   return 0;
+}
+
+int slbc_tc_conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin, const void *wgt,
+                   const float *bias, int cout, void *out, int out_ctot, int out_coff, int relu, const void *mask,
+                   void *stream) {
+  return conv3d(in, B, D, H, W, in_ctot, in_coff, cin, wgt, bias, cout, out, nullptr, out_ctot, out_coff, relu, mask,
+                stream);
+}
+
+int slbc_tc_conv3d_f32(const void *in, int B, int D, int H, int W, int in_ctot, int in_coff, int cin,
+                       const void *wgt, const float *bias, int cout, float *out, int out_ctot, int out_coff,
+                       void *stream) {
+  return conv3d(in, B, D, H, W, in_ctot, in_coff, cin, wgt, bias, cout, nullptr, out, out_ctot, out_coff, 0, nullptr,
+                stream);
 }
 
 int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int nch, void *stream) {

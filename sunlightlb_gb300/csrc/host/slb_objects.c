@@ -128,6 +128,25 @@ LBObj insertlist(LBSys lb, char *listfile) {
   return p;
 }
 
+/* appended: one object made of the nodes where mask[inode] != 0 (the node
+ * list of insertlist held in memory, inode = esk*(esj*i+j)+k) */
+LBObj insertmask(LBSys lb, unsigned char *mask) {
+  long x;
+  int ns = 0, overlap = 0;
+  LBObj p = addobj(lb);
+  zeroobj(p);
+  for (x = 0; x < lb->nnodes; x++)
+    if (mask[x]) set_node(lb, x, p, &ns, &overlap);
+  if (slb_verbosity & OBJECT_DETAILS) {
+    printf("Inserted node mask, id no = %i, # nodes = %i\n", p->id, ns);
+    if (overlap) printf("Overlaps occurred\n");
+  }
+  if (ns == 0) return drop_new(lb, p, 0);
+  map_changed(lb);
+  slb_trace(lb, "insertmask");
+  return p;
+}
+
 /* reference src/lbobjs.c:170-199 */
 LBObj insertslab(LBSys lb, LBReal x1, LBReal x2, LBReal y1, LBReal y2, LBReal z1, LBReal z2) {
   int i, j, k, ns = 0, overlap = 0;

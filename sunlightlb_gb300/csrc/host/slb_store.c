@@ -193,6 +193,27 @@ void lbsetvel(LBSys lb, LBReal *rho, LBReal *ux, LBReal *uy, LBReal *uz) {
   lb->rescale = 1.0;
 }
 
+/* appended: lbsetvel from three device FP32 arrays (rho = rho0), so a
+ * velocity field computed on the GPU never crosses to the host */
+void lbsetveldev(LBSys lb, void *u) {
+  if (lb->changed_objects) syncobjs(lb);
+  if (lb->rescale != 1.0) printf("lbsetveldev: lb->rescale ignored (velocities used as given)\n");
+  slb_check(slbc_set_velocity_dev(slb_device(lb), (const float *)u, lb->skip_solid), "velocity warm start");
+  slb_device_changed(lb);
+  lb->status = POST_PROPAGATE;
+  collide(lb);
+  lb->rescale = 1.0;
+}
+
+/* appended: the velocity field into three device FP32 arrays, with the
+ * half-force correction accvmean applies when lb->vel_corrected */
+void lbvelocity(LBSys lb, void *u) {
+  double fac = 0.0;
+  if (lb->vel_corrected) fac = lb->status == POST_PROPAGATE ? 0.5 : -0.5;
+  if (lb->changed_objects) syncobjs(lb);
+  slb_check(slbc_get_velocity_dev(slb_device(lb), fac, (float *)u), "velocity field");
+}
+
 /* reference src/lbstore.c:305-404 */
 void lbloadvel(LBSys lb, char *loadfile, char *type) {
   long x, n = lb->nnodes;

@@ -206,8 +206,11 @@ def insert_spheres(L, lb, spheres, flatten=True):
 
 
 def insert_solid(L, lb, solid):
-    """One object made of the given nodes, through insertlist (a node list
-    file, reference src/lbobjs.c:128-165)."""
+    """One object made of the given nodes: insertmask when the library has
+    it, else insertlist (a node list file, reference src/lbobjs.c:128-165)."""
+    if L.has("insertmask"):
+        m = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        return L.insertmask(lb, m.ctypes.data)
     idx = np.argwhere(solid)
     fd, path = tempfile.mkstemp(suffix=".lst", text=True)
     try:
