@@ -737,6 +737,102 @@ def run_batch(args):
     L.freebatch(b)
 
 
+# ---- learned warm start ------------------------------------------------------
+
+WARM_SEED, WARM_FORCE = 3, 1e-6
+
+
+def run_warmstart(args):
+    """Train the encoder-decoder on converged flows of seeded 64^3 packings
+    (labels from the solver's own batched lattices), then compare warm-started
+    and plain permeability runs on held-out 128^3 packings."""
+    import numpy as np
+    import torch
+    import sunlightlb_gb300
+    from sunlightlb_gb300 import warmstart as WS
+
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    L = sunlightlb_gb300.library()
+    side, ev_side, force = args.warm_side, args.eval_side, WARM_FORCE
+    specs = WS.packing_specs(args.train + args.eval, WARM_SEED)
+    tr_specs, ev_specs = specs[:args.train], specs[args.train:]
+    t0 = time.perf_counter()
+    solids = [WS.packing(side, phi, sd) for phi, sd in tr_specs]
+    t_pack = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fields, lsteps = WS.converged_flows(L, solids, force=force, tol=args.label_tol, maxsteps=args.label_maxsteps)
+    torch.cuda.synchronize()
+    t_labels = time.perf_counter() - t0
+    masks = torch.as_tensor(np.stack(solids).astype(np.uint8), device="cuda")
+    labels = torch.stack([WS.to_labels(f, (side, side, side)) for f in fields])
+    del fields
+    net = WS.UNet(L, side, side, side, batch=args.batch, seed=1)
+    iters = max(1, args.epochs * args.train // args.batch)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    # each sample's loss relative to its own label energy (labels span more
+    # than an order of magnitude with the solid fraction)
+    sample_w = 1.0 / labels.pow(2).mean(dim=(1, 2, 3, 4)).clamp_min(1e-12)
+    hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20), sample_w=sample_w)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    tc_status = net.status()
+    # held-out packings at the evaluation size
+    inf = WS.UNet(L, ev_side, ev_side, ev_side, batch=1, params=net.params)
+    rows = []
+    for phi, sd in ev_specs:
+        solid = WS.packing(ev_side, phi, sd)
+        traj = WS.permeability_run(L, solid, force)
+        k_conv = traj[-1][1]
+        plain = WS.first_within(traj, k_conv, 1e-4)
+        sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1)
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t0
+        trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u)
+        hitw = WS.first_within(trajw, k_conv, 1e-4)
+        rows.append({"phi": round(phi, 4), "k": k_conv, "plain_steps_to_1e-4": plain[0] if plain else None,
+                     "plain_wall_s": round(plain[1], 4) if plain else None,
+                     "plain_converged_steps": traj[-1][0],
+                     "warm_steps_to_1e-4": hitw[0] if hitw else None,
+                     "warm_wall_s": round(hitw[1] + t_inf, 4) if hitw else None,
+                     "inference_s": round(t_inf, 4),
+                     "warm_k_error_first_check": abs(trajw[0][1] - k_conv) / abs(k_conv),
+                     "plain_k_error_first_check": abs(traj[0][1] - k_conv) / abs(k_conv)})
+    ok = [r for r in rows if r["plain_wall_s"] and r["warm_wall_s"]]
+    speed = [r["plain_wall_s"] / r["warm_wall_s"] for r in ok]
+    steps_ratio = [r["plain_steps_to_1e-4"] / r["warm_steps_to_1e-4"] for r in ok]
+    line = {
+        "workload": f"learned warm start: U-Net trained on {args.train} converged {side}^3 packings, "
+                    f"evaluated on {args.eval} held-out {ev_side}^3 packings",
+        "metric": "wall time and steps to permeability within 1e-4 of the plain converged value, warm vs plain",
+        "config": {"train_side": side, "eval_side": ev_side, "train_samples": args.train, "eval_samples": args.eval,
+                   "phi": [0.1, 0.5], "radii": [3.0, 8.0], "spheres_overlap": True, "force": force, "tau": 1.0,
+                   "widths": list(net.widths), "batch": args.batch, "iterations": iters, "lr": args.lr,
+                   "labels": f"FP32 populations, converged to |d vmeanx|/vmeanx < {args.label_tol:g} per 200 steps",
+                   "precision": "BF16 weights/activations, FP32 accumulation (tcgen05)"},
+        "packing_s": round(t_pack, 1), "labels_s": round(t_labels, 1),
+        "label_steps": {"mean": float(np.mean(lsteps)), "max": int(np.max(lsteps))},
+        "train_s": round(t_train, 1), "train_ms_per_iteration": round(1e3 * t_train / iters, 2),
+        "loss": hist, "tc_status": tc_status,
+        "eval": rows,
+        "summary": {"samples": len(ok), "wall_speedup_mean": float(np.mean(speed)) if speed else None,
+                    "wall_speedup_median": float(np.median(speed)) if speed else None,
+                    "steps_ratio_mean": float(np.mean(steps_ratio)) if steps_ratio else None,
+                    "warm_faster_fraction": float(np.mean([s > 1 for s in speed])) if speed else None},
+    }
+    print(json.dumps(line), flush=True)
+    if args.save_weights:
+        torch.save({n: {k: v.cpu() for k, v in p.items() if k in ("w", "b")} for n, p in net.params.items()},
+                   args.save_weights)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -750,12 +846,22 @@ def main():
     ap.add_argument("--max-converge-steps", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="packed", choices=["packed", "tracer", "batch"],
+    ap.add_argument("--workload", default="packed", choices=["packed", "tracer", "batch", "warmstart"],
                     help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive "
                          "scalar; batch: many small moving-sphere domains in one launch")
     ap.add_argument("--domains", type=int, default=512, help="batch workload: number of domains")
     ap.add_argument("--batch-steps", type=int, default=20000)
     ap.add_argument("--cpu-subset", type=int, default=8, help="batch workload: domains checked on the CPU oracle")
+    ap.add_argument("--train", type=int, default=2000, help="warmstart workload: training packings")
+    ap.add_argument("--eval", type=int, default=100, help="warmstart workload: held-out packings")
+    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--warm-side", type=int, default=64)
+    ap.add_argument("--eval-side", type=int, default=128)
+    ap.add_argument("--label-tol", type=float, default=1e-5)
+    ap.add_argument("--label-maxsteps", type=int, default=20000)
+    ap.add_argument("--save-weights", default="")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")
     ap.add_argument("--tracer-steps", type=int, default=50000)
     ap.add_argument("--fp64-tracer-steps", type=int, default=10000)
@@ -769,6 +875,8 @@ def main():
         run_tracer(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "warmstart":
+        run_warmstart(args)
     else:
         run_mine(args)
 

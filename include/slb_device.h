@@ -260,9 +260,10 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
  * master[tap][cout][cin] (FP32).  wdgrad: weights of the input gradient for
  * input channels [ci0, ci0 + nci): w[t][cout/32][nci][32] =
  * master[26 - t][32 ck + j][ci0 + ci].  adam: Adam step t >= 1.  mse: loss
- * += mean (pred[0..2] - label)^2 (pred FP32 channels 0..2 of a padded
- * buffer, label [n][D][H][W][3]), grad (BF16, gctot channels) = its
- * derivative in channels 0..2, 0 in the others.  encode: channel 0 = 1 on
+ * += mean w[n] (pred[0..2] - label)^2 (pred FP32 channels 0..2 of a padded
+ * buffer, label [n][D][H][W][3], per-sample weights w or null for 1), grad
+ * (BF16, gctot channels) = its derivative in channels 0..2, 0 in the
+ * others.  encode: channel 0 = 1 on
  * solid nodes, the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
  * solid) into u[c * N + e], the layout of lbsetveldev. */
 int slbc_nn_pool(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
@@ -279,8 +280,8 @@ int slbc_nn_wfwd(const float *master, int cout, int cin, void *w, void *stream);
 int slbc_nn_wdgrad(const float *master, int cout, int cin, int ci0, int nci, void *w, void *stream);
 int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
                  int t, void *stream);
-int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, void *grad, int gctot,
-                double *loss, void *stream);
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
+                void *grad, int gctot, double *loss, void *stream);
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
                    float *u, void *stream);

@@ -229,8 +229,8 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, long long n
 // FP32 channels 0..2 of a padded buffer (ctot_p channels), label
 // [n][D][H][W][3] FP32; grad (BF16, gctot channels, padded) = d loss /
 // d pred in channels 0..2, 0 in the others.  loss[0] += the sum / count.
-__global__ void k_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, bf16 *grad,
-                      int gctot, double *loss) {
+__global__ void k_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H,
+                      int W, bf16 *grad, int gctot, double *loss) {
   __shared__ double sh[256];
   const long long total = (long long)B * D * H * W;
   const double inv = 1.0 / (3.0 * (double)total);
@@ -242,13 +242,14 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, int B, 
     const int z = (int)(r % D);
     const int n = (int)(r / D);
     const long long v = vox(n, z, y, x, D, H, W);
+    const float sw = sample_w ? sample_w[n] : 1.0f;
     bf16 *gp = grad + v * gctot;
     for (int c = 0; c < gctot; c += 8) *(uint4 *)(gp + c) = make_uint4(0, 0, 0, 0);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const float d = pred[v * ctot_p + c] - label[e * 3 + c];
-      acc += (double)d * d;
-      gp[c] = __float2bfloat16((float)(2.0 * inv) * d);
+      acc += (double)sw * d * d;
+      gp[c] = __float2bfloat16((float)(2.0 * inv) * sw * d);
     }
   }
   sh[threadIdx.x] = acc;
@@ -387,11 +388,11 @@ int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, floa
   return launched("slbc_nn_adam");
 }
 
-int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int B, int D, int H, int W, void *grad, int gctot,
-                double *loss, void *stream) {
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
+                void *grad, int gctot, double *loss, void *stream) {
   if (ctot_p < 3 || gctot % 8 || gctot < 8) return bad("slbc_nn_mse: bad channel counts");
   k_mse<<<std::min(grid_for((long long)B * D * H * W), 152 * 4), 256, 0, (cudaStream_t)stream>>>(
-      pred, ctot_p, label, B, D, H, W, (bf16 *)grad, gctot, loss);
+      pred, ctot_p, label, sample_w, B, D, H, W, (bf16 *)grad, gctot, loss);
   return launched("slbc_nn_mse");
 }
 

@@ -303,21 +303,39 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
 }
 
 // Periodic halo of channels [coff, coff + nch) (nch a multiple of 8): every
-// halo voxel gets its wrapped interior voxel.
+// halo voxel gets its wrapped interior voxel.  The halo voxels of a sample
+// are enumerated face by face: the planes z = 0 and z = D + 1 whole, then
+// for interior z the rows y = 0 and y = H + 1, then for interior z, y the
+// columns x = 0 and x = W + 1.
 __global__ void k_halo(__nv_bfloat16 *buf, int B, int D, int H, int W, int ctot, int coff, int nch) {
-  const long long P = (long long)(D + 2) * (H + 2) * (W + 2);
+  const long long Pz = 2LL * (H + 2) * (W + 2), Py = 2LL * D * (W + 2), Px = 2LL * D * H;
+  const long long per = Pz + Py + Px;
   const int nv = nch / 8;
-  const long long total = (long long)B * P * nv;
+  const long long total = (long long)B * per * nv;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
     const int cv = (int)(e % nv);
-    const long long v = e / nv;
-    const int n = (int)(v / P);
-    long long r = v % P;
-    const int x = (int)(r % (W + 2));
-    r /= (W + 2);
-    const int y = (int)(r % (H + 2)), z = (int)(r / (H + 2));
-    if (x >= 1 && x <= W && y >= 1 && y <= H && z >= 1 && z <= D) continue;
+    const long long h = e / nv;
+    const int n = (int)(h / per);
+    long long r = h % per;
+    int x, y, z;
+    if (r < Pz) {
+      z = r < Pz / 2 ? 0 : D + 1;
+      r %= Pz / 2;
+      y = (int)(r / (W + 2));
+      x = (int)(r % (W + 2));
+    } else if ((r -= Pz) < Py) {
+      y = r < Py / 2 ? 0 : H + 1;
+      r %= Py / 2;
+      z = 1 + (int)(r / (W + 2));
+      x = (int)(r % (W + 2));
+    } else {
+      r -= Py;
+      x = r < Px / 2 ? 0 : W + 1;
+      r %= Px / 2;
+      z = 1 + (int)(r / H);
+      y = 1 + (int)(r % H);
+    }
     const int sx = x == 0 ? W : (x == W + 1 ? 1 : x);
     const int sy = y == 0 ? H : (y == H + 1 ? 1 : y);
     const int sz = z == 0 ? D : (z == D + 1 ? 1 : z);
@@ -496,29 +514,54 @@ __global__ void k_sum_splits(const float *partial, long long n, int splits, floa
 // Channel-major flat copy of channels [coff, coff + nch) of a padded
 // channels-last buffer: dst[c][n * pstride + (z * (H + 2) + y) * Wp + x] =
 // src[n][z][y][x - shift][coff + c] for 0 <= x - shift <= W + 1 (0 beyond;
-// zero_halo: interior voxels only, every halo position 0).
-__global__ void k_cmajor(const __nv_bfloat16 *src, int B, int D, int H, int W, int ctot, int coff, int nch,
-                         int Wp, long long pstride, int shift, int zero_halo, __nv_bfloat16 *dst) {
+// zero_halo: interior voxels only, every halo position 0).  A block moves
+// 64 consecutive flat positions x 64 channels through shared memory, so
+// both the channel runs it reads and the position runs it writes are
+// 128-byte rows.
+__global__ void __launch_bounds__(256) k_cmajor(const __nv_bfloat16 *src, int B, int D, int H, int W, int ctot,
+                                                int coff, int nch, int Wp, long long pstride, int shift,
+                                                int zero_halo, __nv_bfloat16 *dst) {
+  __shared__ __nv_bfloat16 tile[64][64 + 8];
   const long long plane = (long long)(H + 2) * Wp;
   const long long per_sample = (long long)(D + 2) * plane;
   const long long total = (long long)B * pstride;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int n = (int)(e / pstride);
-    const long long f = e % pstride;
-    bool in = f < per_sample;
-    int z = 0, y = 0, x = 0;
-    if (in) {
-      z = (int)(f / plane);
-      const long long r = f % plane;
-      y = (int)(r / Wp);
-      x = (int)(r % Wp) - shift;
-      in = x >= 0 && x <= W + 1;
-      if (zero_halo) in = in && x >= 1 && x <= W && y >= 1 && y <= H && z >= 1 && z <= D;
+  const long long ntiles = total / 64;
+  const int nck = (nch + 63) / 64;
+  for (long long work = blockIdx.x; work < ntiles * nck; work += gridDim.x) {
+    const long long t = work / nck;
+    const int c0 = (int)(work % nck) * 64;
+    const int cw = nch - c0 < 64 ? nch - c0 : 64;
+    // load: 64 positions x cw channels, 8 channels (16 B) per thread access
+    for (int a = threadIdx.x; a < 64 * 8; a += blockDim.x) {
+      const int pos = a / 8, cv = a % 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (cv * 8 < cw) {
+        const long long e = t * 64 + pos;
+        const int n = (int)(e / pstride);
+        const long long f = e % pstride;
+        if (f < per_sample) {
+          const int z = (int)(f / plane);
+          const long long r = f % plane;
+          const int y = (int)(r / Wp);
+          const int x = (int)(r % Wp) - shift;
+          bool in = x >= 0 && x <= W + 1;
+          if (zero_halo) in = in && x >= 1 && x <= W && y >= 1 && y <= H && z >= 1 && z <= D;
+          if (in)
+            v = *(const uint4 *)(src + ((((long long)n * (D + 2) + z) * (H + 2) + y) * (W + 2) + x) * ctot + coff +
+                                 c0 + cv * 8);
+        }
+      }
+      const __nv_bfloat16 *vb = (const __nv_bfloat16 *)&v;
+#pragma unroll
+      for (int i = 0; i < 8; i++) tile[cv * 8 + i][pos] = vb[i];
     }
-    const __nv_bfloat16 *sp = in ? src + ((((long long)n * (D + 2) + z) * (H + 2) + y) * (W + 2) + x) * ctot + coff
-                                 : nullptr;
-    for (int c = 0; c < nch; c++) dst[(long long)c * total + e] = in ? sp[c] : __float2bfloat16(0.0f);
+    __syncthreads();
+    // store: per channel 64 positions = 128 B, 16 B per thread access
+    for (int a = threadIdx.x; a < 64 * 8; a += blockDim.x) {
+      const int c = a / 8, pv = a % 8;
+      if (c < cw) *(uint4 *)(dst + (long long)(c0 + c) * total + t * 64 + pv * 8) = *(const uint4 *)&tile[c][pv * 8];
+    }
+    __syncthreads();
   }
 }
 
@@ -629,7 +672,8 @@ int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int 
   if (B < 1 || D < 1 || H < 1 || W < 1 || ctot % 8 || coff % 8 || nch % 8 || nch < 8 || coff + nch > ctot)
     return slbc::set_error("slbc_tc_halo: channel counts and offsets must be multiples of 8 and fit"), 1;
   if (!aligned16(buf)) return slbc::set_error("slbc_tc_halo: buffer must be 16-byte aligned"), 1;
-  const long long total = (long long)B * (D + 2) * (H + 2) * (W + 2) * (nch / 8);
+  const long long per = 2LL * (H + 2) * (W + 2) + 2LL * D * (W + 2) + 2LL * D * H;
+  const long long total = (long long)B * per * (nch / 8);
   const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
   k_halo<<<blocks, 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16 *)buf, B, D, H, W, ctot, coff, nch);
   slbc::count_launch();
@@ -643,8 +687,10 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
   if (B < 1 || nch < 1 || coff < 0 || coff + nch > ctot || Wp < W + 2 || Wp % 8 || pstride % 64 ||
       pstride < (long long)(D + 2) * (H + 2) * Wp || shift < -1 || shift > 1)
     return slbc::set_error("slbc_tc_cmajor: bad geometry"), 1;
-  const long long total = (long long)B * pstride;
-  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+  if (nch % 8 || coff % 8 || ctot % 8 || !aligned16(src) || !aligned16(dst))
+    return slbc::set_error("slbc_tc_cmajor: channels in multiples of 8, 16-byte aligned buffers"), 1;
+  const long long work = (long long)B * pstride / 64 * ((nch + 63) / 64);
+  const int blocks = (int)std::min<long long>(work, 152LL * 16);
   k_cmajor<<<blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, B, D, H, W, ctot, coff, nch, Wp,
                                                      pstride, shift, zero_halo, (__nv_bfloat16 *)dst);
   slbc::count_launch();

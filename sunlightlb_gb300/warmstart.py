@@ -55,7 +55,7 @@ class Kernels:
             "slbc_nn_wfwd": [p, i, i, p, p],
             "slbc_nn_wdgrad": [p, i, i, i, i, p, p],
             "slbc_nn_adam": [p, p, p, p, ll, f, f, f, f, i, p],
-            "slbc_nn_mse": [p, i, p, i, i, i, i, p, i, p, p],
+            "slbc_nn_mse": [p, i, p, p, i, i, i, i, p, i, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, p, p],
             "slbc_tc_status": [],
@@ -284,16 +284,16 @@ class UNet:
                         o.data_ptr(), o.shape[-1], c0, 0, m.data_ptr() if m is not None else None, self.stream)
         self._halo(out_name)
 
-    def loss_and_backward(self, labels):
-        """labels: device FP32 (B, D, H, W, 3).  Returns the loss (device
-        scalar, FP64)."""
+    def loss_and_backward(self, labels, sample_w=None):
+        """labels: device FP32 (B, D, H, W, 3); sample_w: optional device
+        FP32 (B,) loss weights.  Returns the loss (device scalar, FP64)."""
         if self.grad is None:
             self._alloc_grads()
         k, G, X = self.k, self.grad, self.buf
         B, (w0, w1, w2, w3) = self.B, self.widths
         self.loss_acc.zero_()
-        k.nn_mse(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), B, self.D, self.H, self.W, G["gOUT"].data_ptr(),
-                 OUT_CH, self.loss_acc.data_ptr(), self.stream)
+        k.nn_mse(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), sample_w.data_ptr() if sample_w is not None else None,
+                 B, self.D, self.H, self.W, G["gOUT"].data_ptr(), OUT_CH, self.loss_acc.data_ptr(), self.stream)
         self._halo("gOUT")
         # level 0 decoder
         self._wgrad("out", "gOUT", "D0")
@@ -487,10 +487,11 @@ def first_within(traj, k_ref, rel):
     return None
 
 
-def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0):
+def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None):
     """Adam on mini-batches of net.B samples drawn (seeded) from masks
-    (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)).
-    Returns the loss every log_every iterations (and the last)."""
+    (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)),
+    optional per-sample loss weights (device FP32 (N,)).  Returns the loss
+    every log_every iterations (and the last)."""
     import torch
     rng = np.random.default_rng(seed)
     n = masks.shape[0]
@@ -499,9 +500,10 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0):
         idx = torch.as_tensor(rng.choice(n, size=net.B, replace=n < net.B), device=masks.device)
         mb = masks.index_select(0, idx).contiguous()
         lab = labels.index_select(0, idx).contiguous()
+        sw = sample_w.index_select(0, idx).contiguous() if sample_w is not None else None
         net.encode(mb)
         net.forward()
-        loss = net.loss_and_backward(lab)
+        loss = net.loss_and_backward(lab, sw)
         net.adam(lr)
         if (log_every and it % log_every == 0) or it == iters:
             hist.append((it, float(loss.item())))

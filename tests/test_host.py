@@ -184,3 +184,17 @@ def test_host_mirror_without_device(gpu):
     gpu.lbpull(lb)              # allocates the mirror, no device needed
     a = lb.array("a")
     assert a.shape == (120, 15) and not a.any()
+
+
+def test_packings_are_seeded_and_stable():
+    """The seeded packings every workload builds (the block-vectorised random
+    sequential addition must keep the sequential decisions)."""
+    import hashlib
+    from sunlightlb_gb300 import workloads as W
+    cases = [((128, 0.30, 4.0, 8.0, 1), {}, 986, "314597b4e685bbfd036c5c3fae1816ec"),
+             ((64, 0.45, 3.0, 8.0, 12345), {"overlap": True}, 202, "c29cdae16782366f7e94f4213f942fd7")]
+    for args, kw, n, digest in cases:
+        spheres, solid = W.rsa_packing(*args, **kw)
+        assert len(spheres) == n
+        assert hashlib.sha256(np.packbits(solid).tobytes()).hexdigest()[:32] == digest
+        assert solid.mean() >= args[1]
