@@ -777,7 +777,8 @@ def run_warmstart(args):
     # each sample's loss relative to its own label energy (labels span more
     # than an order of magnitude with the solid fraction)
     sample_w = 1.0 / labels.pow(2).mean(dim=(1, 2, 3, 4)).clamp_min(1e-12)
-    hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20), sample_w=sample_w)
+    hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20), sample_w=sample_w,
+                    lr_min=args.lr * 0.01)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     tc_status = net.status()
@@ -814,7 +815,9 @@ def run_warmstart(args):
         "metric": "wall time and steps to permeability within 1e-4 of the plain converged value, warm vs plain",
         "config": {"train_side": side, "eval_side": ev_side, "train_samples": args.train, "eval_samples": args.eval,
                    "phi": [0.1, 0.5], "radii": [3.0, 8.0], "spheres_overlap": True, "force": force, "tau": 1.0,
-                   "widths": list(net.widths), "batch": args.batch, "iterations": iters, "lr": args.lr,
+                   "widths": list(net.widths), "batch": args.batch, "iterations": iters,
+                   "lr": f"{args.lr:g} -> {args.lr * 0.01:g} (half cosine)",
+                   "input": "solid mask + periodic wall distance d/5 and (d/5)^2 (d capped at 5)",
                    "labels": f"FP32 populations, converged to |d vmeanx|/vmeanx < {args.label_tol:g} per 200 steps",
                    "precision": "BF16 weights/activations, FP32 accumulation (tcgen05)"},
         "packing_s": round(t_pack, 1), "labels_s": round(t_labels, 1),
@@ -859,7 +862,7 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--warm-side", type=int, default=64)
     ap.add_argument("--eval-side", type=int, default=128)
-    ap.add_argument("--label-tol", type=float, default=1e-5)
+    ap.add_argument("--label-tol", type=float, default=1e-7)
     ap.add_argument("--label-maxsteps", type=int, default=20000)
     ap.add_argument("--save-weights", default="")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")

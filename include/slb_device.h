@@ -85,6 +85,11 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
 /* Populations in the reference AoS order a[15*inode + q] (FP64). put sets
  * layout N; get reads from any layout. */
 int slbc_put_pops(slbc_lattice *h, const double *a);
+/* Page-locked, zero-filled host memory for population mirrors (copies from
+ * and to it run as DMA without a staging copy); NULL when it cannot be had,
+ * in which case the caller uses ordinary memory.  Free with slbc_host_free. */
+void *slbc_host_alloc(size_t bytes);
+void slbc_host_free(void *p);
 int slbc_get_pops(slbc_lattice *h, double *a);
 int slbc_layout(slbc_lattice *h);
 /* Launch shape of the fused step per parity, cfg = {even rows per thread,
@@ -264,7 +269,9 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
  * buffer, label [n][D][H][W][3], per-sample weights w or null for 1), grad
  * (BF16, gctot channels) = its derivative in channels 0..2, 0 in the
  * others.  encode: channel 0 = 1 on
- * solid nodes, the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
+ * solid nodes; with features, channels 1 and 2 = d / 5 and (d / 5)^2, d the
+ * periodic distance of a fluid node to the nearest solid node (capped at
+ * 5); the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
  * solid) into u[c * N + e], the layout of lbsetveldev. */
 int slbc_nn_pool(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
                  int W, int C, void *stream);
@@ -282,7 +289,8 @@ int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, floa
                  int t, void *stream);
 int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
                 void *grad, int gctot, double *loss, void *stream);
-int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, void *stream);
+int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
+                   void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
                    float *u, void *stream);
 

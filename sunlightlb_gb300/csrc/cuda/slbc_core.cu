@@ -1,3 +1,7 @@
+#include <mutex>
+#include <tuple>
+#include <array>
+#include <map>
 // extern "C" device layer of GB300 SunlightLB (declared in slb_device.h):
 // lattice state, geometry, host transfers, layout conversions, dispatch to
 // the per-precision kernels, reductions, CUDA-graph replay and tracers.
@@ -361,7 +365,35 @@ int one_step(Lattice &L) {
 // shape (rows per thread, threads along k) on a copy of the populations --
 // the lattice's own state is not touched -- and keep the fastest.  Lattices
 // below 2^20 nodes use the default shape; SLB_AUTOTUNE=0 disables tuning.
+// Launch shapes chosen so far, per lattice shape and precision: a later
+// lattice of the same shape starts from them instead of timing candidates.
+struct TuneKey {
+  int esi, esj, esk, precision;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(esi, esj, esk, precision) < std::tie(o.esi, o.esj, o.esk, o.precision);
+  }
+};
+std::map<TuneKey, std::array<StepConfig, 2>> g_tuned;
+std::mutex g_tuned_lock;
+
+int autotune_time(Lattice &L);
+
 int autotune(Lattice &L) {
+  {
+    std::lock_guard<std::mutex> guard(g_tuned_lock);
+    auto it = g_tuned.find(TuneKey{L.esi, L.esj, L.esk, L.precision});
+    if (it != g_tuned.end()) {
+      L.tuned[0] = it->second[0];
+      L.tuned[1] = it->second[1];
+      L.tune_state = 1;
+      L.generation++;
+      return 0;
+    }
+  }
+  return autotune_time(L);
+}
+
+int autotune_time(Lattice &L) {
   // FP64/FP32: {rows per thread, threads along k}; BF16: {planes per block, 32}
   static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
   static const int cand_bf[][2] = {{1, 32}, {2, 32}, {4, 32}, {8, 32}, {16, 32}};
@@ -432,6 +464,8 @@ int autotune(Lattice &L) {
   if (rc) return fail_msg("autotune: a candidate launch failed");
   L.tune_state = 1;
   L.generation++;
+  std::lock_guard<std::mutex> guard(g_tuned_lock);
+  g_tuned[TuneKey{L.esi, L.esj, L.esk, L.precision}] = {L.tuned[0], L.tuned[1]};
   return 0;
 }
 
@@ -745,11 +779,26 @@ int slbc_get_pops(slbc_lattice *h, double *a) {
   for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
     const long long n = std::min(chunk, L.nnodes - x0);
     CK(DISPATCH3(L, launch_get, L, L.staging, x0, n));
+    // stream order keeps the next chunk's kernel behind this copy
     CK(cudaMemcpyAsync(a + 15 * x0, L.staging, (size_t)(15 * n) * sizeof(double),
                        cudaMemcpyDeviceToHost, L.stream));
-    CK(cudaStreamSynchronize(L.stream));
   }
+  CK(cudaStreamSynchronize(L.stream));
   return 0;
+}
+
+void *slbc_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();  // clear: the caller falls back to pageable memory
+    return nullptr;
+  }
+  memset(p, 0, bytes);
+  return p;
+}
+
+void slbc_host_free(void *p) {
+  if (p) cudaFreeHost(p);
 }
 
 int slbc_step(slbc_lattice *h, int n, int use_graph) {

@@ -261,9 +261,14 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, const f
   if (threadIdx.x == 0) atomicAdd(loss, sh[0] * inv);
 }
 
-// input encoding: channel 0 = 1 on solid nodes, 0 on fluid; channels
-// 1 .. ctot-1 zero (interior; the halo is filled afterwards)
-__global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W, bf16 *out, int ctot) {
+// input encoding: channel 0 = 1 on solid nodes, 0 on fluid; with
+// features, channel 1 = d / R and channel 2 = (d / R)^2 where d is the
+// periodic distance from a fluid node to the nearest solid node, searched
+// over a cube of half-width R (d = R when none is that close; 0 on solid
+// nodes); other channels zero (interior; the halo is filled afterwards)
+constexpr int kDistR = 5;
+
+__global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W, bf16 *out, int ctot, int features) {
   const long long total = (long long)B * D * H * W;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -273,7 +278,26 @@ __global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W,
     const int n = (int)(r / D);
     bf16 *p = out + vox(n, z, y, x, D, H, W) * ctot;
     for (int c = 0; c < ctot; c += 8) *(uint4 *)(p + c) = make_uint4(0, 0, 0, 0);
-    p[0] = __float2bfloat16(solid[e] ? 1.0f : 0.0f);
+    const bool s = solid[e] != 0;
+    p[0] = __float2bfloat16(s ? 1.0f : 0.0f);
+    if (features && !s) {
+      const unsigned char *sn = solid + (long long)n * D * H * W;
+      int best = kDistR * kDistR;
+      for (int dz = -kDistR; dz <= kDistR; dz++) {
+        const int zz = ((z + dz) % D + D) % D;
+        for (int dy = -kDistR; dy <= kDistR; dy++) {
+          const int yy = ((y + dy) % H + H) % H;
+          const unsigned char *row = sn + ((long long)zz * H + yy) * W;
+          for (int dx = -kDistR; dx <= kDistR; dx++) {
+            const int d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < best && row[((x + dx) % W + W) % W]) best = d2;
+          }
+        }
+      }
+      const float d = sqrtf((float)best) * (1.0f / kDistR);
+      p[1] = __float2bfloat16(d);
+      p[2] = __float2bfloat16(d * d);
+    }
   }
 }
 
@@ -396,9 +420,11 @@ int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *
   return launched("slbc_nn_mse");
 }
 
-int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, void *stream) {
+int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
+                   void *stream) {
   if (ctot % 8 || ctot < 8) return bad("slbc_nn_encode: bad channel count");
-  k_encode<<<grid_for((long long)B * D * H * W), 256, 0, (cudaStream_t)stream>>>(solid, B, D, H, W, (bf16 *)out, ctot);
+  k_encode<<<grid_for((long long)B * D * H * W), 256, 0, (cudaStream_t)stream>>>(solid, B, D, H, W, (bf16 *)out, ctot,
+                                                                                features);
   return launched("slbc_nn_encode");
 }
 

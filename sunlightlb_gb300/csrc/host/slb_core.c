@@ -130,7 +130,12 @@ LBSys newlb(int reqesi, int reqesj, int reqesk, char *name) {
 slb_priv *slb_state(LBSys lb) { return (slb_priv *)lb->priv; }
 
 LBReal *slb_host_a(LBSys lb) {
-  if (lb->a == NULL) lb->a = (LBReal *)xcalloc(15 * (size_t)lb->nnodes, sizeof(LBReal));
+  if (lb->a == NULL) {
+    /* page-locked when possible: uploads and downloads then run as DMA */
+    lb->a = (LBReal *)slbc_host_alloc(15 * (size_t)lb->nnodes * sizeof(LBReal));
+    slb_state(lb)->a_pinned = lb->a != NULL;
+    if (lb->a == NULL) lb->a = (LBReal *)xcalloc(15 * (size_t)lb->nnodes, sizeof(LBReal));
+  }
   return lb->a;
 }
 
@@ -359,10 +364,11 @@ void freelb(LBSys lb) {
   if (lb == NULL) return;
   st = slb_state(lb);
   if (st->dev) slbc_destroy(st->dev);
+  if (st->a_pinned) slbc_host_free(lb->a); else free(lb->a);
   free(st->objs); free(st->bnd_node); free(st->bnd_obj); free(st);
   p = lb->obj_head;
   while (p != NULL) { pp = p; p = p->next_obj; free(pp); }
-  free(lb->a); free(lb->mask); free(lb->obj);
+  free(lb->mask); free(lb->obj);
   free(lb->ux); free(lb->uy); free(lb->uz); free(lb->fx); free(lb->fy); free(lb->fz);
   free(lb->bx); free(lb->by); free(lb->bz); free(lb->rho); free(lb->name);
   free(lb->c); free(lb->w);

@@ -22,6 +22,7 @@ typedef struct slb_priv {
   int host_a_valid;           /* lb->a equals the device populations */
   int host_f_valid;           /* lb->fx/fy/fz equal the device node forces */
   int host_rho_valid;         /* lb->rho equals the device density snapshot */
+  int a_pinned;               /* lb->a is page-locked (slbc_host_alloc) */
   /* dense object table of the last geometry upload */
   int nobj;
   LBObj *objs;                /* index -> object */

@@ -56,7 +56,7 @@ class Kernels:
             "slbc_nn_wdgrad": [p, i, i, i, i, p, p],
             "slbc_nn_adam": [p, p, p, p, ll, f, f, f, f, i, p],
             "slbc_nn_mse": [p, i, p, p, i, i, i, i, p, i, p, p],
-            "slbc_nn_encode": [p, i, i, i, i, p, i, p],
+            "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, p, p],
             "slbc_tc_status": [],
         }
@@ -87,9 +87,10 @@ class UNet:
     """The encoder-decoder on a batch of B grids D x H x W (powers of two,
     the coarsest level D*H*W/512 >= 128 voxels)."""
 
-    def __init__(self, lib, D, H, W_, batch, widths=(32, 64, 128, 256), seed=0, params=None):
+    def __init__(self, lib, D, H, W_, batch, widths=(32, 64, 128, 256), seed=0, params=None, features=1):
         import torch
         self.torch = torch
+        self.features = features  # input: mask (0) or mask + wall-distance channels (1)
         self.k = Kernels(lib.dll)
         self.D, self.H, self.W, self.B = D, H, W_, batch
         self.widths = w0, w1, w2, w3 = widths
@@ -146,7 +147,7 @@ class UNet:
         for name, lv, cin, cout, *_ in self.layers:
             std = math.sqrt(2.0 / (27 * cin))
             if name == "e0a":
-                std = math.sqrt(2.0 / 27)    # one live input channel
+                std = math.sqrt(2.0 / (27 * (1 + 2 * self.features)))  # live input channels
             w = torch.randn(27, cout, cin, generator=g) * std
             b = torch.zeros(cout)
             if name == "out":
@@ -187,7 +188,8 @@ class UNet:
     def encode(self, solid_u8):
         """solid_u8: device uint8 tensor (B, D, H, W)."""
         k = self.k
-        k.nn_encode(solid_u8.data_ptr(), self.B, self.D, self.H, self.W, self.buf["IN"].data_ptr(), IN_CH, self.stream)
+        k.nn_encode(solid_u8.data_ptr(), self.B, self.D, self.H, self.W, self.buf["IN"].data_ptr(), IN_CH,
+                    self.features, self.stream)
         self._halo("IN")
 
     def forward(self):
@@ -487,11 +489,12 @@ def first_within(traj, k_ref, rel):
     return None
 
 
-def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None):
+def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None):
     """Adam on mini-batches of net.B samples drawn (seeded) from masks
     (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)),
-    optional per-sample loss weights (device FP32 (N,)).  Returns the loss
-    every log_every iterations (and the last)."""
+    optional per-sample loss weights (device FP32 (N,)); with lr_min the
+    learning rate decays from lr to lr_min along a half cosine.  Returns the
+    loss every log_every iterations (and the last)."""
     import torch
     rng = np.random.default_rng(seed)
     n = masks.shape[0]
@@ -504,7 +507,8 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None
         net.encode(mb)
         net.forward()
         loss = net.loss_and_backward(lab, sw)
-        net.adam(lr)
+        rate = lr if lr_min is None else lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * (it - 1) / iters))
+        net.adam(rate)
         if (log_every and it % log_every == 0) or it == iters:
             hist.append((it, float(loss.item())))
     return hist

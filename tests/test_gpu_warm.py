@@ -26,7 +26,7 @@ def test_unet_gradients_match_cpu_oracle(gpu):
     from sunlightlb_gb300 import warmstart as WS
     orc = oracle()
     B, D, H, W = 2, 32, 32, 64
-    net = WS.UNet(gpu, D, H, W, batch=B, widths=(32, 32, 32, 32), seed=3)
+    net = WS.UNet(gpu, D, H, W, batch=B, widths=(32, 32, 32, 32), seed=3, features=0)
     rng = np.random.default_rng(5)
     solid = (rng.random((B, D, H, W)) > 0.7).astype(np.uint8)
     zz, yy, xx = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
@@ -54,6 +54,33 @@ def test_unet_gradients_match_cpu_oracle(gpu):
         rw, rb = ref[name]
         assert np.linalg.norm(gw - rw) <= 0.05 * np.linalg.norm(rw), name
         assert np.linalg.norm(gb - rb) <= 0.05 * np.linalg.norm(rb) + 1e-12, name
+
+
+def test_wall_distance_features(gpu):
+    """Input channels 1 and 2: periodic distance to the nearest solid node
+    (searched within 5, capped there) / 5 and its square; 0 on solid nodes."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    B, D, H, W = 1, 32, 32, 64
+    net = WS.UNet(gpu, D, H, W, batch=B, widths=(32, 32, 32, 32), seed=3)
+    rng = np.random.default_rng(9)
+    solid = (rng.random((B, D, H, W)) > 0.97).astype(np.uint8)
+    net.encode(torch.as_tensor(solid, device="cuda"))
+    got = net.buf["IN"][0, 1:-1, 1:-1, 1:-1, :3].float().cpu().numpy()
+    best = np.full((D, H, W), 25.0)
+    s = solid[0].astype(bool)
+    for dz in range(-5, 6):
+        for dy in range(-5, 6):
+            for dx in range(-5, 6):
+                d2 = dx * dx + dy * dy + dz * dz
+                if d2 >= 25:
+                    continue
+                hit = np.roll(s, shift=(-dz, -dy, -dx), axis=(0, 1, 2))
+                best = np.where(hit & (d2 < best), d2, best)
+    d = np.where(s, 0.0, np.sqrt(best) / 5.0)
+    assert np.array_equal(got[..., 0], s.astype(np.float32))
+    assert np.abs(got[..., 1] - d).max() <= 4e-3
+    assert np.abs(got[..., 2] - np.where(s, 0.0, d * d)).max() <= 4e-3
 
 
 def test_training_lowers_the_loss(gpu):
