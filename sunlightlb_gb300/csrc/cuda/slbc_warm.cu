@@ -39,6 +39,20 @@ int *tc_err_flag() {
   return g_tc_err[dev];
 }
 
+// Opt a kernel into `bytes` of dynamic shared memory on the current device;
+// the attribute is per device, so `done` keeps one bit per device index.
+cudaError_t smem_opt_in(const void *fn, int bytes, unsigned long long &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> guard(g_tc_lock);
+  if (done >> dev & 1ull) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done |= 1ull << dev;
+  return e;
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point
 typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -184,16 +198,28 @@ struct ConvArgs {
 };
 
 constexpr int kConvTileA = 128 * 64;       // 128 voxels x 32 channels x 2 B
-constexpr int kConvTileB = 256 * 64;       // up to 256 output channels x 32 x 2 B
-constexpr int kConvSmem = kStages * (kConvTileA + kConvTileB) + 1024;
 
-__global__ void __launch_bounds__(128, 1)
+// Pipeline depth by output width: a stage is one A tile and one B tile of
+// cout rows x 64 B, and every depth below keeps the stages within 96 KB, so
+// two CTAs share an SM.
+__host__ __device__ constexpr int conv_stages(int cout) { return cout <= 64 ? 8 : (cout <= 128 ? 6 : 4); }
+__host__ __device__ constexpr int conv_smem(int nst, int cout) { return nst * (kConvTileA + cout * 64) + 1024; }
+constexpr int kConvSmemMax = conv_smem(8, 64);
+static_assert(conv_smem(6, 128) <= kConvSmemMax && conv_smem(4, 256) <= kConvSmemMax, "stage budget");
+
+// The producer (thread 0) and the MMA issuer (thread 32) step through
+// (tap, channel chunk, stage, round) with counters instead of divisions:
+// for the narrow layers an MMA pair takes a few tens of cycles, so the
+// single-thread loops set the pace.
+template <int NST>
+__global__ void __launch_bounds__(128, 2)
 k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tw, ConvArgs a, int *err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
   uint8_t *tA = smem_raw + pad;
-  uint8_t *tB = tA + kStages * kConvTileA;
-  __shared__ uint64_t full[kStages], empty[kStages], done;
+  const uint32_t tile_b = (uint32_t)a.cout * 64u;
+  uint8_t *tB = tA + NST * kConvTileA;
+  __shared__ uint64_t full[NST], empty[NST], done;
   __shared__ uint32_t tmem_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = blockIdx.y;
@@ -208,7 +234,7 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
     tc::tmem_relinquish();
   }
   if (threadIdx.x == 32) {
-    for (int s = 0; s < kStages; s++) {
+    for (int s = 0; s < NST; s++) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
@@ -222,33 +248,56 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
   bool ok = true;
   int issued = 0;
   if (threadIdx.x == 0) {
+    int s = 0, round = 0, ck = 0, dx = 0, dy = 0, dz = 0;
+    int c = a.in_coff, wrow = 0;
     for (int kt = 0; kt < nk; kt++) {
-      const int s = kt % kStages;
-      if (kt >= kStages && !tc::mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, kWaitLimit)) {
+      if (round > 0 && !tc::mbar_wait(&empty[s], (uint32_t)(round - 1) & 1u, kWaitLimit)) {
         ok = false;
         break;
       }
-      const int tap = kt / nck, ck = kt - tap * nck;
-      const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
       tc::mbar_expect_tx(&full[s], (uint32_t)kConvTileA + bytes_b);
-      tc::tma_load_5d(tA + s * kConvTileA, &tx, &full[s], a.in_coff + ck * 32, x0 + dx, y0 + dy, z0 + dz, n);
-      tc::tma_load_2d(tB + s * kConvTileB, &tw, &full[s], 0, kt * a.cout);
+      tc::tma_load_5d(tA + s * kConvTileA, &tx, &full[s], c, x0 + dx, y0 + dy, z0 + dz, n);
+      tc::tma_load_2d(tB + s * tile_b, &tw, &full[s], 0, wrow);
       issued = kt + 1;
+      wrow += a.cout;
+      c += 32;
+      if (++ck == nck) {
+        ck = 0;
+        c = a.in_coff;
+        if (++dx == 3) {
+          dx = 0;
+          if (++dy == 3) {
+            dy = 0;
+            ++dz;
+          }
+        }
+      }
+      if (++s == NST) {
+        s = 0;
+        ++round;
+      }
     }
   } else if (threadIdx.x == 32) {
     const uint32_t idesc = tc::idesc_bf16(128, a.cout);
+    const uint64_t ad0 = tc::smem_desc(tA, tc::kSwizzle64, 64);
+    const uint64_t bd0 = tc::smem_desc(tB, tc::kSwizzle64, 64);
+    int s = 0, round = 0;
     for (int kt = 0; kt < nk; kt++) {
-      const int s = kt % kStages;
-      if (!tc::mbar_wait(&full[s], (kt / kStages) & 1, kWaitLimit)) {
+      if (!tc::mbar_wait(&full[s], (uint32_t)round & 1u, kWaitLimit)) {
         ok = false;
         break;
       }
       tc::fence_after_sync();
-      const uint64_t ad = tc::smem_desc(tA + s * kConvTileA, tc::kSwizzle64, 64);
-      const uint64_t bd = tc::smem_desc(tB + s * kConvTileB, tc::kSwizzle64, 64);
+      // the start-address field counts 16-byte units
+      const uint64_t ad = ad0 + (uint64_t)(s * (kConvTileA >> 4));
+      const uint64_t bd = bd0 + (uint64_t)(s * (tile_b >> 4));
       tc::mma_bf16(tmem, ad, bd, idesc, kt != 0);
       tc::mma_bf16(tmem, ad + 2, bd + 2, idesc, 1);
       tc::mma_commit(&empty[s]);
+      if (++s == NST) {
+        s = 0;
+        ++round;
+      }
     }
     tc::mma_commit(&done);
   }
@@ -294,8 +343,8 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
   }
   if (!ok || !okd) atomicExch(err, 1);
   if (threadIdx.x == 0) {
-    for (int kt = issued > kStages ? issued - kStages : 0; kt < issued; kt++)
-      if (!tc::mbar_wait(&full[kt % kStages], (kt / kStages) & 1, kWaitLimit)) atomicExch(err, 2);
+    for (int kt = issued > NST ? issued - NST : 0; kt < issued; kt++)
+      if (!tc::mbar_wait(&full[kt % NST], (kt / NST) & 1, kWaitLimit)) atomicExch(err, 2);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -595,11 +644,8 @@ int slbc_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, in
   CUtensorMap ta, tb;
   if (!make_map_2d(&ta, A, M, K, kBM) || !make_map_2d(&tb, B, N, K, kBN))
     return slbc::set_error("slbc_tc_gemm: tensor map encoding failed"), 1;
-  static std::once_flag attr;
-  cudaError_t e = cudaSuccess;
-  std::call_once(attr, [&] {
-    e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
-  });
+  static unsigned long long attr_done = 0;
+  cudaError_t e = smem_opt_in((const void *)k_gemm_bf16, kGemmSmem, attr_done);
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_gemm: ") + cudaGetErrorString(e)), 1;
   k_gemm_bf16<<<dim3(N / kBN, M / kBM), 128, kGemmSmem, (cudaStream_t)stream>>>(ta, tb, D, ldd, K, err);
   slbc::count_launch();
@@ -640,14 +686,18 @@ static int conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int i
   a.mask = (const __nv_bfloat16 *)mask;
   a.out = out_f32 ? nullptr : (__nv_bfloat16 *)out;
   a.out_f32 = out_f32;
-  static std::once_flag attr;
-  cudaError_t e = cudaSuccess;
-  std::call_once(attr, [&] {
-    e = cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
-  });
+  static unsigned long long attr_done[3] = {0, 0, 0};
+  const int nst = conv_stages(cout), smem = conv_smem(nst, cout);
+  const void *fn = nst == 8 ? (const void *)k_conv_fwd<8> : (nst == 6 ? (const void *)k_conv_fwd<6> : (const void *)k_conv_fwd<4>);
+  cudaError_t e = smem_opt_in(fn, kConvSmemMax, attr_done[nst == 8 ? 0 : (nst == 6 ? 1 : 2)]);
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_conv3d: ") + cudaGetErrorString(e)), 1;
-  k_conv_fwd<<<dim3((unsigned)((long long)D * H * W / 128), (unsigned)B), 128, kConvSmem, (cudaStream_t)stream>>>(
-      tx, tw, a, err);
+  const dim3 grid((unsigned)((long long)D * H * W / 128), (unsigned)B);
+  if (nst == 8)
+    k_conv_fwd<8><<<grid, 128, smem, (cudaStream_t)stream>>>(tx, tw, a, err);
+  else if (nst == 6)
+    k_conv_fwd<6><<<grid, 128, smem, (cudaStream_t)stream>>>(tx, tw, a, err);
+  else
+    k_conv_fwd<4><<<grid, 128, smem, (cudaStream_t)stream>>>(tx, tw, a, err);
   slbc::count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_conv3d: ") + cudaGetErrorString(e)), 1;
@@ -733,11 +783,8 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
   if (!make_map_k64(&m0, dy0, cout, cols, w.co_rows) || !make_map_k64(&m1, dy1, cout, cols, w.co_rows) ||
       !make_map_k64(&m2, dy2, cout, cols, w.co_rows) || !make_map_k64(&mb, xt, cin, cols, w.ntile))
     return slbc::set_error("slbc_tc_wgrad: tensor map encoding failed"), 1;
-  static std::once_flag attr;
-  cudaError_t e = cudaSuccess;
-  std::call_once(attr, [&] {
-    e = cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem);
-  });
+  static unsigned long long attr_done = 0;
+  cudaError_t e = smem_opt_in((const void *)k_wgrad, kWgSmem, attr_done);
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
   const dim3 grid((unsigned)(((27 + w.taps_per_tile - 1) / w.taps_per_tile) * w.co_tiles), (unsigned)(cin / w.ntile),
                   (unsigned)splits);
