@@ -17,6 +17,11 @@
  *            pop[opp q][x] when the link x -> x + c_q is a boundary link
  *            (after an odd step);
  *     the in-place AA update alternates C0 -> C1 -> C0;
+ *     BF16 lattices hold each node's post-collision state instead, always in
+ *     the reference's layout (N): FP32 moments (drho, ru) and the BF16
+ *     deviations of the 8 pairs {q, opp q} from the zero-stress rebuild of
+ *     those moments (a collision makes q and opp q deviate equally), two
+ *     copies swapped by every step;
  *   - a per-node flag word (solid bit + 14 boundary-link bits);
  *   - the list of solid boundary nodes, sorted by object then node, with
  *     FP64 node forces accumulated during measurement;
@@ -83,7 +88,9 @@ int slbc_set_bodyforce(slbc_lattice *h, const double *bx, const double *by, cons
 int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const double *uz);
 
 /* Populations in the reference AoS order a[15*inode + q] (FP64). put sets
- * layout N; get reads from any layout. */
+ * layout N; get reads from any layout.  On a BF16 lattice put returns 2 when
+ * some node's populations deviate unequally within a pair {q, opp q} (more
+ * than BF16 rounding): that state needs FP32 or FP64 storage. */
 int slbc_put_pops(slbc_lattice *h, const double *a);
 /* Page-locked, zero-filled host memory for population mirrors (copies from
  * and to it run as DMA without a staging copy); NULL when it cannot be had,
@@ -94,8 +101,9 @@ int slbc_get_pops(slbc_lattice *h, double *a);
 int slbc_layout(slbc_lattice *h);
 /* Launch shape of the fused step per parity, cfg = {even rows per thread,
  * even threads along k, odd rows per thread, odd threads along k}; for BF16
- * lattices the "rows per thread" entries are planes per block (1..64) and
- * threads along k is 32.  The
+ * lattices the "rows per thread" entries are planes per block (1..64),
+ * threads along k is 32, and the even entries serve every step (one update
+ * kernel).  The
  * first slbc_step of a lattice of 2^20 nodes or more times the candidate
  * shapes on a copy of the populations and keeps the fastest (environment
  * SLB_AUTOTUNE=0 turns this off); get returns 1 tuned, -1 defaults, 0 not

@@ -59,7 +59,8 @@ typedef float LBStoreReal;
 /* Device population precision (appended; value of lb->precision) */
 #define SLB_FP64 0   /* FP64 populations, FP64 collision: parity path */
 #define SLB_FP32 1   /* FP32 populations, FP32 collision, FP64 reductions */
-#define SLB_BF16 2   /* BF16 scaled deviation from a reference equilibrium */
+#define SLB_BF16 2   /* FP32 moments + BF16 paired deviations from their equilibrium;
+                        needs skip_solid = 0 (else the lattice moves to FP32) */
 
 /* Lattice object (reference src/sunlightlb.h:53-64) */
 typedef struct LBObj_struct {

@@ -1,22 +1,29 @@
-// BF16 scaled-deviation populations.
+// BF16 paired-deviation populations.
 //
-// Storage of a lattice in this precision:
-//   M[x]   = (drho, rux, ruy, ruz) of node x after its last collision, FP32,
-//            one float4 per node, two buffers swapped every step;
-//   D[q][x]  BF16 of scale * (a_q - eq_q(M)), the deviation of each
-//            post-collision population from the equilibrium built from the
-//            node's own moments (eq = the collision's rebuild with zero
-//            stress, reference src/lbkernel.c:838-865), in the same AA
-//            layouts (N, C0, C1) as the FP32 and FP64 populations.
-// A population is reconstructed as eq_q(M[source]) + D / scale, where the
-// source is the node that produced it.  The equilibrium part carries FP32
-// precision; BF16 rounding touches only the non-equilibrium part, which is
-// zero for tau = 1 in Stokes flow (the collision then returns the
-// equilibrium exactly).  Collision arithmetic is FP32; sums are FP64.
+// A collision rebuilds the 15 populations of a node from its density
+// deviation, momentum and relaxed stress (reference src/lbkernel.c:838-865).
+// The rebuild is linear, so a post-collision population a_q minus the
+// zero-stress rebuild eq_q of the same (drho, ru) is the stress part of the
+// rebuild alone, and that part is even in c_q: a_q and a_opp(q) carry the
+// same deviation.  A node's post-collision state is therefore held as
+//   M[x]    = (drho, rux, ruy, ruz), FP32, one float4;
+//   P[x][p] = BF16 of scale * (a_q - eq_q(M[x])) for the 8 pairs
+//             p = pair_of(q): {0}, {1,2}, {3,4}, {5,6}, {7,14}, {8,13},
+//             {9,12}, {10,11}; one 16-byte vector;
+// 32 bytes per node, in two copies: a step reads one and writes the other.
+// A population is a_q(x) = eq_q(M[x]) + P[x][pair_of(q)] / scale.  The
+// equilibrium part keeps FP32 precision; BF16 rounding touches only the
+// stress part, which is zero at tau = 1 in Stokes flow.
 //
-// Traffic per node update: 15 x 2 B deviations read and written, one float4
-// of moments read and one written (94 B with the flag word, against 120 B
-// for FP32 populations).
+// The state is always the reference's post-collision array: a step gathers
+// a_q(x) from the state of x - c_q, or of x itself over a bounce-back link,
+// and writes the new state of x.  Two kinds of state cannot be held this
+// way, and the host moves such a lattice to FP32: solid nodes that are not
+// relaxed (skip_solid), whose streamed populations are not paired, and
+// uploaded populations whose deviations are not paired.
+//
+// Traffic per node update: 32 B of state read and 32 B written, plus the
+// 2-byte flag word (FP32 populations: 120 B of state).
 #include <cuda_bf16.h>
 
 #include "slbc_internal.cuh"
@@ -25,17 +32,25 @@
 
 namespace slbc {
 
-typedef __nv_bfloat16 bf16;
-
-struct Bf16Args {
-  bf16 *D;
-  long long npad;
-  const uint16_t *flags;
-  int esi, esj, esk;
+struct PairArgs {
+  const uint4 *Pin;    // paired deviations of the current state
+  uint4 *Pout;         // ... written by a step
   const float4 *Min;   // moments of the current state
-  float4 *Mout;        // moments written by a step
+  float4 *Mout;        // ... written by a step
+  const uint16_t *flags;
+  long long npad;
+  int esi, esj, esk;
   float scale, inv;    // stored = scale * deviation
 };
+
+// pair of direction q: q and opp(q) share one stored deviation
+__host__ __device__ constexpr int pair_of(int q) {
+  return q == 0 ? 0 : (q <= 6 ? (q + 1) / 2 : (q <= 10 ? q - 3 : 18 - q));
+}
+static_assert(pair_of(7) == pair_of(OPP(7)) && pair_of(8) == pair_of(OPP(8)) && pair_of(9) == pair_of(OPP(9)) &&
+                  pair_of(10) == pair_of(OPP(10)) && pair_of(1) == pair_of(OPP(1)) &&
+                  pair_of(3) == pair_of(OPP(3)) && pair_of(5) == pair_of(OPP(5)),
+              "pairs must join opposite directions");
 
 // equilibrium population q of moments (drho, ru): the rebuild with zero stress
 __device__ __forceinline__ float eq_pop(int q, float4 m) {
@@ -56,33 +71,60 @@ __device__ __forceinline__ float eq_pop(int q, float4 m) {
   }
 }
 
-__device__ __forceinline__ float dev_load(const Bf16Args &a, int slot, int node) {
-  return __bfloat162float(a.D[slot * a.npad + node]) * a.inv;
+// BF16 bits in the low 16 bits of u -> FP32 (exact)
+__device__ __forceinline__ float bf_bits(uint32_t u) { return __uint_as_float(u << 16); }
+
+// stored deviation of pair p in a packed vector
+__device__ __forceinline__ float pair_dev(const uint4 &v, int p) {
+  const uint32_t w = p < 2 ? v.x : (p < 4 ? v.y : (p < 6 ? v.z : v.w));
+  return (p & 1) ? __uint_as_float(w & 0xffff0000u) : __uint_as_float(w << 16);
 }
 
-// post-collision population q of node x, reconstructed, in a given layout
-__device__ __forceinline__ float bf_post(const Bf16Args &a, int layout, int q, int x, uint16_t fl,
-                                         const Nbr &nb, float4 mx) {
-  float d;
-  if (layout == SLBC_LAYOUT_N) d = dev_load(a, q, x);
-  else if (layout == SLBC_LAYOUT_C0 || q == 0 || ((fl >> OPP(q)) & 1)) d = dev_load(a, OPP(q), x);
-  else d = dev_load(a, q, nb.at(CX(q), CY(q), CZ(q)));
-  return eq_pop(q, mx) + d;
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// The fused step of k_step for deviation storage (same pull rule, same AA
-// layouts); also writes the new moments.
-//
-// Every population is reconstructed with the moments of the node that
-// produced it, so a node reads the moments of its 14 neighbours.  A block of
-// 32 (k) x 8 (j) threads marches along i over `planes` planes and keeps the
-// moments of three consecutive planes, with a one-node halo, in shared
-// memory; the plane after next is fetched into registers while the current
-// one is updated.  Moments then cross L2 about 1.7 times per node instead of
-// 15 times.
-template <bool ODD, bool MOVING, bool BFU>
-__global__ void __launch_bounds__(kTileThreads, 4) k_step_bf16(Bf16Args a, StepArgs<float> s, int planes) {
-  __shared__ float4 ring[3][kPlane];
+// Stored deviations of a collided node: the stress part of the rebuild,
+// pair by pair (trace part, then the diagonal and mixed stress terms).
+__device__ __forceinline__ uint4 pack_stress(const Relaxed<float> &r, float scale) {
+  const float tr = (r.sxx + r.syy + r.szz) * (1.0f / 3.0f);
+  const float h = 0.5f * scale, e = 0.125f * scale;
+  uint4 v;
+  v.x = pack2(-tr * scale, h * (r.sxx - tr));
+  v.y = pack2(h * (r.syy - tr), h * (r.szz - tr));
+  v.z = pack2(e * (tr + r.sxy + r.sxz + r.syz), e * (tr - r.sxy - r.sxz + r.syz));
+  v.w = pack2(e * (tr - r.sxy + r.sxz - r.syz), e * (tr + r.sxy - r.sxz - r.syz));
+  return v;
+}
+
+// post-collision population q of node x
+__device__ __forceinline__ float bf_post(const PairArgs &a, int q, long long x) {
+  return eq_pop(q, a.Min[x]) + pair_dev(a.Pin[x], pair_of(q)) * a.inv;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+constexpr int kPairSlots = 4;  // planes i-1, i, i+1 in use, i+2 arriving
+
+// The fused update of k_step (same pull rule) on paired-deviation storage.
+// A block of 32 (k) x 8 (j) threads marches along i over `planes` planes.
+// The state (moments and deviations) of four consecutive planes, with a
+// one-node halo, sits in shared memory: the three a node gathers from and
+// the next one, copied in by cp.async while the current plane is updated.
+// Every value a node gathers comes from shared memory; global memory sees
+// one 16-byte load of each state vector per node (plus the halo) and one
+// store of each.  Nodes are independent, so there is one barrier per plane.
+template <bool MOVING, bool BFU>
+__global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepArgs<float> s, int planes) {
+  __shared__ float4 ringM[kPairSlots][kPlane];
+  __shared__ uint4 ringP[kPairSlots][kPlane];
   const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
   const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
   const int np = min(planes, a.esi - i0);
@@ -95,103 +137,71 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_bf16(Bf16Args a, StepA
     off[e] = c < kPlane ? wrap_index(j0 - 1 + c / kHaloK, a.esj) * a.esk + wrap_index(k0 - 1 + c % kHaloK, a.esk)
                         : -1;
   }
-  // plane p sits in ring slot (p - i0 + 1) % 3
-  float4 pre[kPlaneLoads];
+  // plane p goes to ring slot (p - i0 + 1) % kPairSlots
+  auto fetch = [&](int plane, int slot) {
+    const long long base = (long long)wrap_index(plane, a.esi) * plane_nodes;
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const int base = wrap_index(i0 - 1 + h, a.esi) * plane_nodes;
-#pragma unroll
-    for (int e = 0; e < kPlaneLoads; e++)
-      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = __ldg(a.Min + base + off[e]);
-  }
-  {
-    const int base = wrap_index(i0 + 1, a.esi) * plane_nodes;
-#pragma unroll
-    for (int e = 0; e < kPlaneLoads; e++)
-      if (off[e] >= 0) pre[e] = __ldg(a.Min + base + off[e]);
-  }
-  const long long S = a.npad;
+    for (int e = 0; e < kPlaneLoads; e++) {
+      if (off[e] < 0) continue;
+      cp_async16(&ringM[slot][tid + kTileThreads * e], a.Min + base + off[e]);
+      cp_async16(&ringP[slot][tid + kTileThreads * e], a.Pin + base + off[e]);
+    }
+    cp_async_commit();
+  };
+  fetch(i0 - 1, 0);
+  fetch(i0, 1);
+  fetch(i0 + 1, 2);
+  const int j = j0 + tj, k = k0 + tk;
+  const bool mine = j < a.esj && k < a.esk;
+  const int own = j * a.esk + k;
+  const int c0 = (tj + 1) * kHaloK + tk + 1;
   for (int ii = 0; ii < np; ii++) {
     const int i = i0 + ii;
-    const int sm = ii % 3, s0 = (ii + 1) % 3, sp = (ii + 2) % 3;  // planes i-1, i, i+1
-    __syncthreads();  // slot sp held plane i-2, last read in the previous iteration
-#pragma unroll
-    for (int e = 0; e < kPlaneLoads; e++)
-      if (off[e] >= 0) ring[sp][tid + kTileThreads * e] = pre[e];
-    __syncthreads();
-    if (ii + 1 < np) {
-      const int base = wrap_index(i + 2, a.esi) * plane_nodes;
-#pragma unroll
-      for (int e = 0; e < kPlaneLoads; e++)
-        if (off[e] >= 0) pre[e] = __ldg(a.Min + base + off[e]);
-    }
-    const int j = j0 + tj, k = k0 + tk;
-    if (j >= a.esj || k >= a.esk) continue;
-    const float4 *P[3] = {ring[sm], ring[s0], ring[sp]};
-    const int c0 = (tj + 1) * kHaloK + tk + 1;
-    const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
-    const int x = nb.at(0, 0, 0);
+    cp_async_wait_all();
+    __syncthreads();  // plane i+1 has arrived; slot of plane i-2 is free
+    if (ii + 1 < np) fetch(i + 2, (ii + 3) % kPairSlots);
+    if (!mine) continue;
+    const float4 *RM[3] = {ringM[ii % kPairSlots], ringM[(ii + 1) % kPairSlots], ringM[(ii + 2) % kPairSlots]};
+    const uint4 *RP[3] = {ringP[ii % kPairSlots], ringP[(ii + 1) % kPairSlots], ringP[(ii + 2) % kPairSlots]};
+    const int x = i * plane_nodes + own;
     const uint16_t fl = __ldg(a.flags + x);
     const bool solid = (fl & FLAG_SOLID) != 0;
-    const float4 mx = P[1][c0];
-    // Branch-free selection of each population's cell and producer moments,
-    // so that all 15 loads are in flight together.  A bounce-back link
-    // (bit q) returns the node's own post-collision opp(q), held in slot q
-    // of x in both C0 and C1; its equilibrium eq_opp(q)(m) is eq_q of m with
-    // the momentum negated (exact: only signs change).  Otherwise the
-    // population was produced by y = x - c_q.
+    const float4 mx = RM[1][c0];
+    const uint4 px = RP[1][c0];
+    // A bounce-back link (bit q) returns the node's own post-collision
+    // opp(q): eq_opp(q)(m) is eq_q of m with the momentum negated (exact:
+    // only signs change) and the deviation is that of the same pair.
+    // Otherwise the population was produced by y = x - c_q.
     const float4 mneg = make_float4(mx.x, -mx.y, -mx.z, -mx.w);
     float t[15];
-    t[0] = eq_pop(0, mx) + dev_load(a, 0, x);
+    t[0] = eq_pop(0, mx) + pair_dev(px, 0) * a.inv;
 #pragma unroll
     for (int q = 1; q < 15; q++) {
       const bool bnd = (fl >> q) & 1;
-      const float4 my = P[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
+      const int c = c0 - CY(q) * kHaloK - CZ(q);
+      const float4 my = RM[1 - CX(q)][c];
+      const float dy = bf_bits(reinterpret_cast<const unsigned short *>(RP[1 - CX(q)] + c)[pair_of(q)]);
       const float4 m = bnd ? mneg : my;
-      int src = x, slot = q;
-      if (ODD) {
-        src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
-        slot = bnd ? q : OPP(q);
-      }
-      t[q] = eq_pop(q, m) + dev_load(a, slot, src);
+      const float d = bnd ? pair_dev(px, pair_of(q)) : dy;
+      t[q] = eq_pop(q, m) + d * a.inv;
     }
-    if (MOVING && (fl & FLAG_LINKS)) apply_wall<float>(t, fl, solid, nb, x, s.uw, s.p.npad);
-    if (!(s.skip_solid && solid)) {
-      float bx = s.bfx, by = s.bfy, bz = s.bfz;
-      if (!BFU) { bx = s.bf[x]; by = s.bf[s.p.npad + x]; bz = s.bf[2 * s.p.npad + x]; }
-      collide<float, false>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
+    if (MOVING && (fl & FLAG_LINKS)) {
+      const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
+      apply_wall<float>(t, fl, solid, nb, x, s.uw, s.p.npad);
     }
-    // moments of the post-collision populations (the collision conserves
-    // drho and sets ru; summing keeps skipped solid nodes exact too)
-    float4 mo;
-    {
-      const float p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
-      const float lo = t[7] + t[8] + t[9] + t[10], hi = t[11] + t[12] + t[13] + t[14];
-      mo.x = t[0] + p12 + p34 + p56 + lo + hi;
-      mo.y = t[1] - t[2] + (t[7] - t[8] + t[9] - t[10]) + (t[11] - t[12] + t[13] - t[14]);
-      mo.z = t[3] - t[4] + (t[7] + t[8] - t[9] - t[10]) + (t[11] + t[12] - t[13] - t[14]);
-      mo.w = t[5] - t[6] + lo - hi;
-    }
-    a.Mout[x] = mo;
-    if (!ODD) {
-#pragma unroll
-      for (int q = 0; q < 15; q++)
-        a.D[OPP(q) * S + x] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
-    } else {
-      a.D[x] = __float2bfloat16_rn((t[0] - eq_pop(0, mo)) * a.scale);
-#pragma unroll
-      for (int q = 1; q < 15; q++) {
-        const bool bnd = (fl >> OPP(q)) & 1;
-        const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
-        const int slot = bnd ? OPP(q) : q;
-        a.D[slot * S + dst] = __float2bfloat16_rn((t[q] - eq_pop(q, mo)) * a.scale);
-      }
-    }
+    float bx = s.bfx, by = s.bfy, bz = s.bfz;
+    if (!BFU) { bx = s.bf[x]; by = s.bf[s.p.npad + x]; bz = s.bf[2 * s.p.npad + x]; }
+    const Relaxed<float> r = relax<float>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
+    a.Mout[x] = make_float4(r.drho, r.rux, r.ruy, r.ruz);
+    a.Pout[x] = pack_stress(r, a.scale);
   }
 }
 
-// populations (host AoS staging, FP64) -> moments + deviations, layout N
-__global__ void k_put_bf16(Bf16Args a, const double *stage, long long x0, long long n) {
+// populations (host AoS staging, FP64) -> moments + paired deviations; a
+// node whose deviations differ within a pair by more than the BF16
+// rounding of the larger, or than 2^-20 of the two populations, is counted
+// in *unpaired (the host then keeps the lattice in FP32)
+__global__ void k_put_pair(PairArgs a, const double *stage, long long x0, long long n, int *unpaired) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const long long x = x0 + e;
@@ -204,41 +214,39 @@ __global__ void k_put_bf16(Bf16Args a, const double *stage, long long x0, long l
   m.y = t[1] - t[2] + (t[7] - t[8] + t[9] - t[10]) + (t[11] - t[12] + t[13] - t[14]);
   m.z = t[3] - t[4] + (t[7] + t[8] - t[9] - t[10]) + (t[11] + t[12] - t[13] - t[14]);
   m.w = t[5] - t[6] + lo - hi;
-  a.Mout[x] = m;
-#pragma unroll
-  for (int q = 0; q < 15; q++) a.D[q * a.npad + x] = __float2bfloat16_rn((t[q] - eq_pop(q, m)) * a.scale);
-}
-
-// any layout -> host AoS staging of the reference's array
-__global__ void k_get_bf16(Bf16Args a, int layout, double *stage, long long x0, long long n) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const int x = (int)(x0 + e);
-  int i, j, k;
-  decode(x, a.esj, a.esk, i, j, k);
-  const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
-  const uint16_t fl = a.flags[x];
-  const float4 mx = a.Min[x];
-#pragma unroll
-  for (int q = 0; q < 15; q++) stage[15 * e + q] = (double)bf_post(a, layout, q, x, fl, nb, mx);
-}
-
-// N <-> C0 slot swap of the deviations
-__global__ void k_swap_bf16(Bf16Args a, long long n) {
-  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= n) return;
+  float d[8];
+  d[0] = t[0] - eq_pop(0, m);
+  bool paired = true;
 #pragma unroll
   for (int q = 1; q < 15; q++) {
     if (OPP(q) < q) continue;
-    const bf16 u = a.D[q * a.npad + x], v = a.D[OPP(q) * a.npad + x];
-    a.D[q * a.npad + x] = v;
-    a.D[OPP(q) * a.npad + x] = u;
+    const float u = t[q] - eq_pop(q, m), v = t[OPP(q)] - eq_pop(OPP(q), m);
+    const float tol = fmaxf(0x1p-9f * fmaxf(fabsf(u), fabsf(v)), 0x1p-20f * (fabsf(t[q]) + fabsf(t[OPP(q)])));
+    if (fabsf(u - v) > tol) paired = false;
+    d[pair_of(q)] = 0.5f * (u + v);
   }
+  if (!paired) atomicAdd(unpaired, 1);
+  a.Mout[x] = m;
+  uint4 v;
+  v.x = pack2(d[0] * a.scale, d[1] * a.scale);
+  v.y = pack2(d[2] * a.scale, d[3] * a.scale);
+  v.z = pack2(d[4] * a.scale, d[5] * a.scale);
+  v.w = pack2(d[6] * a.scale, d[7] * a.scale);
+  a.Pout[x] = v;
+}
+
+// state -> host AoS staging of the reference's array
+__global__ void k_get_pair(PairArgs a, double *stage, long long x0, long long n) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const long long x = x0 + e;
+#pragma unroll
+  for (int q = 0; q < 15; q++) stage[15 * e + q] = (double)bf_post(a, q, x);
 }
 
 // mean-flow sums straight from the moments: u = (ru + fac*b) / (rho0 + drho)
 __global__ void __launch_bounds__(kReduceThreads)
-k_vsum_bf16(Bf16Args a, double rho0, double fac, int bf_uniform, double b0, double b1, double b2,
+k_vsum_pair(PairArgs a, double rho0, double fac, int bf_uniform, double b0, double b1, double b2,
             const float *bf, const double *psi, double *partials) {
   Acc<float> ax, ay, az;
   double wsum = 0.0;
@@ -273,7 +281,7 @@ k_vsum_bf16(Bf16Args a, double rho0, double fac, int bf_uniform, double b0, doub
 
 // node forces of one bblforce from reconstructed populations (FP32 terms,
 // compensated sums, FP64 store)
-__global__ void k_force_bf16(Bf16Args a, int layout, int moving, const float *uw, ForceArgs f) {
+__global__ void k_force_pair(PairArgs a, int moving, const float *uw, ForceArgs f) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= f.nbnd) return;
   const int s = f.bnd_node[e];
@@ -281,7 +289,6 @@ __global__ void k_force_bf16(Bf16Args a, int layout, int moving, const float *uw
   decode(s, a.esj, a.esk, i, j, k);
   const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
   const uint16_t fl = a.flags[s];
-  const float4 ms = a.Min[s];
   Acc<float> ax, ay, az;
   float ux = 0.f, uy = 0.f, uz = 0.f;
   if (moving) { ux = uw[s]; uy = uw[a.npad + s]; uz = uw[2 * a.npad + s]; }
@@ -289,16 +296,7 @@ __global__ void k_force_bf16(Bf16Args a, int layout, int moving, const float *uw
   for (int q = 1; q < 15; q++) {
     if (!((fl >> OPP(q)) & 1)) continue;
     const int n = nb.at(CX(q), CY(q), CZ(q));
-    const float4 mn = a.Min[n];
-    float av, bv;
-    if (layout == SLBC_LAYOUT_N) {
-      av = eq_pop(q, ms) + dev_load(a, q, s);
-      bv = eq_pop(OPP(q), mn) + dev_load(a, OPP(q), n);
-    } else {
-      av = eq_pop(q, ms) + dev_load(a, OPP(q), s);
-      bv = eq_pop(OPP(q), mn) + dev_load(a, q, n);
-    }
-    float dp = av - bv;
+    float dp = bf_post(a, q, s) - bf_post(a, OPP(q), n);
     if (moving) dp -= link_term<float>(q, ux, uy, uz);
     dp *= 2.f;
     if (CX(q) != 0) ax.add(CX(q) > 0 ? dp : -dp);
@@ -308,61 +306,45 @@ __global__ void k_force_bf16(Bf16Args a, int layout, int moving, const float *uw
   f.f[e] += ax.value(); f.f[f.nbnd + e] += ay.value(); f.f[2 * f.nbnd + e] += az.value();
 }
 
-// velocity warm start: rebuild from (rho, u) (reference src/lbstore.c:352-399)
-__global__ void k_setvel_bf16(Bf16Args a, const double *stage, long long x0, long long n, int has_rho,
+// velocity warm start: the rebuild from (rho, u) of reference
+// src/lbstore.c:352-399, as moments and paired stress deviations
+__global__ void k_setvel_pair(PairArgs a, const double *stage, long long x0, long long n, int has_rho,
                               double rho0, int stokes, int skip_solid) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const long long x = x0 + e;
-  float t[15];
-  float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (!(skip_solid && (a.flags[x] & FLAG_SOLID))) {
-    const float r = has_rho ? (float)stage[4 * e] : (float)rho0;
+  Relaxed<float> r{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (!(skip_solid && (a.flags[x] & FLAG_SOLID))) {  // else all populations zero
+    const float rho = has_rho ? (float)stage[4 * e] : (float)rho0;
     const float vx = (float)stage[4 * e + 1], vy = (float)stage[4 * e + 2], vz = (float)stage[4 * e + 3];
-    const float drho = r - (float)rho0, rux = r * vx, ruy = r * vy, ruz = r * vz;
-    float sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+    r.drho = rho - (float)rho0; r.rux = rho * vx; r.ruy = rho * vy; r.ruz = rho * vz;
     if (!stokes) {
-      sxx = vx * rux; sxy = vx * ruy; sxz = vx * ruz;
-      syy = vy * ruy; syz = vy * ruz; szz = vz * ruz;
+      r.sxx = vx * r.rux; r.sxy = vx * r.ruy; r.sxz = vx * r.ruz;
+      r.syy = vy * r.ruy; r.syz = vy * r.ruz; r.szz = vz * r.ruz;
     }
-    rebuild<float, false>(t, drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
-    m = make_float4(drho, rux, ruy, ruz);
-  } else {
-#pragma unroll
-    for (int q = 0; q < 15; q++) t[q] = 0.f;
   }
-  a.Mout[x] = m;
-#pragma unroll
-  for (int q = 0; q < 15; q++) a.D[q * a.npad + x] = __float2bfloat16_rn((t[q] - eq_pop(q, m)) * a.scale);
+  a.Mout[x] = make_float4(r.drho, r.rux, r.ruy, r.ruz);
+  a.Pout[x] = pack_stress(r, a.scale);
 }
 
-// collision of layout N in place (after an upload or a velocity warm start):
-// reconstruct, collide, store moments and deviations again
+// collision of the current state in place (the separate collide phase)
 template <bool BFU>
-__global__ void k_collide_bf16(Bf16Args a, StepArgs<float> s) {
+__global__ void k_collide_pair(PairArgs a, StepArgs<float> s) {
   const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= (long long)a.esi * a.esj * a.esk) return;
   const bool solid = (a.flags[x] & FLAG_SOLID) != 0;
-  if (s.skip_solid && solid) return;
-  float4 m = a.Min[x];
   float t[15];
 #pragma unroll
-  for (int q = 0; q < 15; q++) t[q] = eq_pop(q, m) + dev_load(a, q, (int)x);
+  for (int q = 0; q < 15; q++) t[q] = bf_post(a, q, x);
   float bx = s.bfx, by = s.bfy, bz = s.bfz;
   if (!BFU) { bx = s.bf[x]; by = s.bf[s.p.npad + x]; bz = s.bf[2 * s.p.npad + x]; }
-  collide<float, false>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
-  const float lo = t[7] + t[8] + t[9] + t[10], hi = t[11] + t[12] + t[13] + t[14];
-  m.x = t[0] + (t[1] + t[2]) + (t[3] + t[4]) + (t[5] + t[6]) + lo + hi;
-  m.y = t[1] - t[2] + (t[7] - t[8] + t[9] - t[10]) + (t[11] - t[12] + t[13] - t[14]);
-  m.z = t[3] - t[4] + (t[7] + t[8] - t[9] - t[10]) + (t[11] + t[12] - t[13] - t[14]);
-  m.w = t[5] - t[6] + lo - hi;
-  ((float4 *)a.Min)[x] = m;
-#pragma unroll
-  for (int q = 0; q < 15; q++) a.D[q * a.npad + x] = __float2bfloat16_rn((t[q] - eq_pop(q, m)) * a.scale);
+  const Relaxed<float> r = relax<float>(t, s.omega, s.comega, s.rho0, s.stokes, !solid, bx, by, bz);
+  a.Mout[x] = make_float4(r.drho, r.rux, r.ruy, r.ruz);
+  a.Pout[x] = pack_stress(r, a.scale);
 }
 
 // density snapshot of the tracer: rho0 + drho on fluid nodes
-__global__ void k_mp_rhoinit_bf16(Bf16Args a, double rho0, double *rho64, float *rho32) {
+__global__ void k_mp_rhoinit_pair(PairArgs a, double rho0, double *rho64, float *rho32) {
   const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= (long long)a.esi * a.esj * a.esk) return;
   double r = rho0;
@@ -373,16 +355,27 @@ __global__ void k_mp_rhoinit_bf16(Bf16Args a, double rho0, double *rho64, float 
 
 // ---- launchers ---------------------------------------------------------------
 
-static Bf16Args bf_args(Lattice &L) {
-  Bf16Args a;
-  a.D = (bf16 *)L.pop;
-  a.npad = L.npad;
-  a.flags = L.flags;
-  a.esi = L.esi; a.esj = L.esj; a.esk = L.esk;
+// current state: copy mom_cur; a step writes the other copy
+static PairArgs pair_args(Lattice &L) {
+  PairArgs a;
+  const uint4 *P = (const uint4 *)L.pop;
+  a.Pin = P + (size_t)L.mom_cur * L.npad;
+  a.Pout = const_cast<uint4 *>(P + (size_t)(1 - L.mom_cur) * L.npad);
   a.Min = (const float4 *)L.mom[L.mom_cur];
   a.Mout = (float4 *)L.mom[1 - L.mom_cur];
+  a.flags = L.flags;
+  a.npad = L.npad;
+  a.esi = L.esi; a.esj = L.esj; a.esk = L.esk;
   a.scale = (float)L.bf16_scale;
   a.inv = (float)(1.0 / L.bf16_scale);
+  return a;
+}
+
+// the current state as both input and output (node-local kernels)
+static PairArgs pair_args_inplace(Lattice &L) {
+  PairArgs a = pair_args(L);
+  a.Pout = const_cast<uint4 *>(a.Pin);
+  a.Mout = const_cast<float4 *>(a.Min);
   return a;
 }
 
@@ -402,20 +395,11 @@ static StepArgs<float> step_args_f(Lattice &L) {
 
 static int fblocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
-template <bool ODD>
-static void bf_step(Lattice &L, const Bf16Args &a, const StepArgs<float> &s, dim3 g, int planes) {
-  const dim3 b(kTileK, kTileJ);
-  if (s.moving) {
-    if (s.bf_uniform) k_step_bf16<ODD, true, true><<<g, b, 0, L.stream>>>(a, s, planes);
-    else k_step_bf16<ODD, true, false><<<g, b, 0, L.stream>>>(a, s, planes);
-  } else {
-    if (s.bf_uniform) k_step_bf16<ODD, false, true><<<g, b, 0, L.stream>>>(a, s, planes);
-    else k_step_bf16<ODD, false, false><<<g, b, 0, L.stream>>>(a, s, planes);
-  }
-}
+static const char *kSkipSolid =
+    "BF16 paired-deviation storage relaxes solid nodes too: set skip_solid = 0 or use FP32 populations";
 
-// planes per block: the tuned value (npt field of the parity's StepConfig),
-// else the largest of 1..8 that still gives about four blocks per SM
+// planes per block: the largest of 1..8 that still gives about four blocks
+// per SM
 int bf16_default_planes(const Lattice &L) {
   const long long tiles = (long long)((L.esk + kTileK - 1) / kTileK) * ((L.esj + kTileJ - 1) / kTileJ);
   int p = 8;
@@ -423,42 +407,52 @@ int bf16_default_planes(const Lattice &L) {
   return p;
 }
 
-cudaError_t launch_step_bf16(Lattice &L, int odd) {
-  int planes = L.tuned[odd ? 1 : 0].npt;
-  if (planes <= 0) planes = bf16_default_planes(L);
+// One update from the current state into the other copy; the caller swaps
+// the copies (mom_cur).
+cudaError_t launch_pair_step(Lattice &L, int planes) {
+  if (L.par.skip_solid) {
+    set_error(kSkipSolid);
+    return cudaErrorInvalidValue;
+  }
   const dim3 g((unsigned)((L.esk + kTileK - 1) / kTileK), (unsigned)((L.esj + kTileJ - 1) / kTileJ),
                (unsigned)((L.esi + planes - 1) / planes));
-  const Bf16Args a = bf_args(L);
+  const dim3 b(kTileK, kTileJ);
+  const PairArgs a = pair_args(L);
   const StepArgs<float> s = step_args_f(L);
-  if (odd) bf_step<true>(L, a, s, g, planes);
-  else bf_step<false>(L, a, s, g, planes);
+  if (s.moving) {
+    if (s.bf_uniform) k_step_pair<true, true><<<g, b, 0, L.stream>>>(a, s, planes);
+    else k_step_pair<true, false><<<g, b, 0, L.stream>>>(a, s, planes);
+  } else {
+    if (s.bf_uniform) k_step_pair<false, true><<<g, b, 0, L.stream>>>(a, s, planes);
+    else k_step_pair<false, false><<<g, b, 0, L.stream>>>(a, s, planes);
+  }
   count_launch();
-  L.mom_cur = 1 - L.mom_cur;
   return cudaGetLastError();
 }
 
-cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n) {
-  Bf16Args a = bf_args(L);
-  a.Mout = (float4 *)L.mom[L.mom_cur];  // defines the current state
-  k_put_bf16<<<fblocks(n, 256), 256, 0, L.stream>>>(a, stage, x0, n);
+// the state has one layout, so both parities run the same update
+cudaError_t launch_step_bf16(Lattice &L, int /*odd*/) {
+  int planes = L.tuned[0].npt;
+  if (planes <= 0) planes = bf16_default_planes(L);
+  const cudaError_t e = launch_pair_step(L, planes);
+  if (e == cudaSuccess) L.mom_cur = 1 - L.mom_cur;
+  return e;
+}
+
+cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n, int *unpaired) {
+  k_put_pair<<<fblocks(n, 256), 256, 0, L.stream>>>(pair_args_inplace(L), stage, x0, n, unpaired);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_get_bf16(Lattice &L, double *stage, long long x0, long long n) {
-  k_get_bf16<<<fblocks(n, 256), 256, 0, L.stream>>>(bf_args(L), L.layout, stage, x0, n);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_swap_bf16(Lattice &L) {
-  k_swap_bf16<<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(bf_args(L), L.nnodes);
+  k_get_pair<<<fblocks(n, 256), 256, 0, L.stream>>>(pair_args(L), stage, x0, n);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_vsum_bf16(Lattice &L, double fac, const double *psi, double *partials, int nblocks) {
-  k_vsum_bf16<<<nblocks, kReduceThreads, 0, L.stream>>>(bf_args(L), L.par.rho0, fac, L.bf_uniform,
+  k_vsum_pair<<<nblocks, kReduceThreads, 0, L.stream>>>(pair_args(L), L.par.rho0, fac, L.bf_uniform,
                                                          L.bf_const[0], L.bf_const[1], L.bf_const[2],
                                                          (const float *)L.bf, psi, partials);
   count_launch();
@@ -469,32 +463,33 @@ cudaError_t launch_force_bf16(Lattice &L) {
   if (L.nbnd == 0) return cudaSuccess;
   ForceArgs f{L.nbnd, L.bnd_node, L.bnd_f};
   const int moving = L.par.objects_moving && L.uw != nullptr;
-  k_force_bf16<<<fblocks(L.nbnd, 128), 128, 0, L.stream>>>(bf_args(L), L.layout, moving,
-                                                           (const float *)L.uw, f);
+  k_force_pair<<<fblocks(L.nbnd, 128), 128, 0, L.stream>>>(pair_args(L), moving, (const float *)L.uw, f);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_setvel_bf16(Lattice &L, const double *stage, long long x0, long long n, int has_rho,
                                int skip_solid) {
-  Bf16Args a = bf_args(L);
-  a.Mout = (float4 *)L.mom[L.mom_cur];
-  k_setvel_bf16<<<fblocks(n, 256), 256, 0, L.stream>>>(a, stage, x0, n, has_rho, L.par.rho0,
+  k_setvel_pair<<<fblocks(n, 256), 256, 0, L.stream>>>(pair_args_inplace(L), stage, x0, n, has_rho, L.par.rho0,
                                                        L.par.stokes_flow, skip_solid);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_collide_bf16(Lattice &L) {
+  if (L.par.skip_solid) {
+    set_error(kSkipSolid);
+    return cudaErrorInvalidValue;
+  }
   const StepArgs<float> s = step_args_f(L);
-  if (s.bf_uniform) k_collide_bf16<true><<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(bf_args(L), s);
-  else k_collide_bf16<false><<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(bf_args(L), s);
+  if (s.bf_uniform) k_collide_pair<true><<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(pair_args_inplace(L), s);
+  else k_collide_pair<false><<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(pair_args_inplace(L), s);
   count_launch();
   return cudaGetLastError();
 }
 
 cudaError_t launch_mp_rhoinit_bf16(Lattice &L) {
-  k_mp_rhoinit_bf16<<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(bf_args(L), L.par.rho0, L.mp_rho64,
+  k_mp_rhoinit_pair<<<fblocks(L.nnodes, 256), 256, 0, L.stream>>>(pair_args(L), L.par.rho0, L.mp_rho64,
                                                                   L.mp_rho32);
   count_launch();
   return cudaGetLastError();

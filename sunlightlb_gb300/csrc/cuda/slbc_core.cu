@@ -55,6 +55,12 @@ int fail_msg(const std::string &m) {
 // bytes of one stored population, and of the side arrays (body force, wall
 // velocity) that the kernels read in their arithmetic type
 size_t elem_size(int precision) { return precision == 0 ? 8 : precision == 1 ? 4 : 2; }
+
+// bytes of the population array: 15 values per node, or for BF16 two copies
+// of 8 paired deviations per node
+size_t pop_bytes(int precision, long long npad) {
+  return precision == 2 ? 2 * 16 * (size_t)npad : 15 * (size_t)npad * elem_size(precision);
+}
 size_t side_size(int precision) { return precision == 0 ? 8 : 4; }
 
 // kernels that do not depend on the population type -------------------------
@@ -317,7 +323,7 @@ int ensure_staging(Lattice &L, long long nodes, int per_node) {
 
 int ensure_scratch(Lattice &L) {
   if (L.scratch) return 0;
-  CK(cudaMalloc(&L.scratch, 15 * (size_t)L.npad * elem_size(L.precision)));
+  CK(cudaMalloc(&L.scratch, pop_bytes(L.precision, L.npad)));
   return 0;
 }
 
@@ -330,10 +336,12 @@ int ensure_partials(Lattice &L, int n) {
   return 0;
 }
 
-// put the state into a post-collision AA layout (C0 or C1)
+// put the state into a post-collision AA layout (C0 or C1); BF16 storage
+// has the reference's layout only
 int to_aa(Lattice &L) {
+  if (L.precision == 2) return 0;
   if (L.layout == SLBC_LAYOUT_N) {
-    CK(DISPATCH3(L, launch_swap, L));
+    CK(DISPATCH(L, launch_swap, L));
     L.layout = SLBC_LAYOUT_C0;
   }
   return 0;
@@ -354,7 +362,15 @@ int to_natural(Lattice &L) {
   return 0;
 }
 
+const char *kPairSkipSolid =
+    "BF16 paired-deviation storage relaxes solid nodes too: set skip_solid = 0 or use FP32 populations";
+
 int one_step(Lattice &L) {
+  if (L.precision == 2) {
+    if (L.par.skip_solid) return fail_msg(kPairSkipSolid);
+    CK(launch_step_bf16(L, 0));
+    return 0;
+  }
   const int odd = L.layout == SLBC_LAYOUT_C0;
   CK(DISPATCH3(L, launch_step, L, odd));
   L.layout = odd ? SLBC_LAYOUT_C1 : SLBC_LAYOUT_C0;
@@ -409,27 +425,20 @@ int autotune_time(Lattice &L) {
     L.tune_state = -1;
     return 0;
   }
-  if (ensure_scratch(L)) return 1;
-  const size_t bytes = 15 * (size_t)L.npad * elem_size(L.precision);
-  CK(cudaMemcpyAsync(L.scratch, L.pop, bytes, cudaMemcpyDeviceToDevice, L.stream));
-  std::swap(L.pop, L.scratch);  // kernels below run on the copy
-  // BF16 steps also write moments: run them on a copy of those too
-  void *mom_saved[2] = {L.mom[0], L.mom[1]};
-  const int mom_cur_saved = L.mom_cur;
-  void *mom_tmp = nullptr;
-  if (bf) {
-    CK(cudaMalloc(&mom_tmp, 2 * sizeof(float4) * (size_t)L.npad));
-    CK(cudaMemcpyAsync(mom_tmp, L.mom[L.mom_cur], sizeof(float4) * (size_t)L.npad, cudaMemcpyDeviceToDevice,
-                       L.stream));
-    L.mom[0] = mom_tmp;
-    L.mom[1] = (char *)mom_tmp + sizeof(float4) * (size_t)L.npad;
-    L.mom_cur = 0;
+  // FP64/FP32 candidates run on a copy of the populations; a BF16 update
+  // reads the current copy of the state and writes the other one, so it
+  // runs on the lattice itself without changing its state
+  if (!bf) {
+    if (ensure_scratch(L)) return 1;
+    CK(cudaMemcpyAsync(L.scratch, L.pop, pop_bytes(L.precision, L.npad), cudaMemcpyDeviceToDevice, L.stream));
+    std::swap(L.pop, L.scratch);
   }
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   int rc = 0;
-  for (int parity = 0; parity < 2 && !rc; parity++) {
+  const int nparity = bf ? 1 : 2;  // BF16: one update kernel for both parities
+  for (int parity = 0; parity < nparity && !rc; parity++) {
     float best = 1e30f;
     int besti = 1;
     for (int c = 0; c < ncand && !rc; c++) {
@@ -438,7 +447,8 @@ int autotune_time(Lattice &L) {
       float tmin = 1e30f;
       for (int rep = 0; rep < 4 && !rc; rep++) {
         cudaEventRecord(e0, L.stream);
-        if (DISPATCH3(L, launch_step, L, parity) != cudaSuccess) rc = 1;
+        const cudaError_t le = bf ? launch_pair_step(L, cand[c][0]) : DISPATCH(L, launch_step, L, parity);
+        if (le != cudaSuccess) rc = 1;
         cudaEventRecord(e1, L.stream);
         if (cudaEventSynchronize(e1) != cudaSuccess) rc = 1;
         float ms = 0.f;
@@ -450,17 +460,11 @@ int autotune_time(Lattice &L) {
     L.tuned[parity].npt = cand[besti][0];
     L.tuned[parity].block_k = cand[besti][1];
   }
-  g_launches -= 2 * ncand * 4;  // tuning launches are not part of the simulation
+  if (bf) L.tuned[1] = L.tuned[0];
+  g_launches -= nparity * ncand * 4;  // tuning launches are not part of the simulation
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  std::swap(L.pop, L.scratch);
-  if (bf) {
-    cudaStreamSynchronize(L.stream);
-    cudaFree(mom_tmp);
-    L.mom[0] = mom_saved[0];
-    L.mom[1] = mom_saved[1];
-    L.mom_cur = mom_cur_saved;
-  }
+  if (!bf) std::swap(L.pop, L.scratch);
   if (rc) return fail_msg("autotune: a candidate launch failed");
   L.tune_state = 1;
   L.generation++;
@@ -535,8 +539,8 @@ int slbc_create(slbc_lattice **out, int esi, int esj, int esk, int precision) {
   L.npad = (n + 63) / 64 * 64;
   L.par.tau = 0.75; L.par.rho0 = 72.0;
   h->solid_host.assign((size_t)n, 0);
-  cudaError_t e = cudaMalloc(&L.pop, 15 * (size_t)L.npad * elem_size(precision));
-  if (e == cudaSuccess) e = cudaMemset(L.pop, 0, 15 * (size_t)L.npad * elem_size(precision));
+  cudaError_t e = cudaMalloc(&L.pop, pop_bytes(precision, L.npad));
+  if (e == cudaSuccess) e = cudaMemset(L.pop, 0, pop_bytes(precision, L.npad));
   if (e == cudaSuccess) e = cudaMalloc(&L.flags, (size_t)n * sizeof(uint16_t));
   if (e == cudaSuccess) e = cudaMemset(L.flags, 0, (size_t)n * sizeof(uint16_t));
   if (e == cudaSuccess) e = cudaMalloc(&L.objidx, (size_t)n * sizeof(int));
@@ -760,15 +764,33 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
 int slbc_put_pops(slbc_lattice *h, const double *a) {
   Lattice &L = h->L;
   if (ensure_staging(L, L.nnodes, 15)) return 1;
+  if (L.precision == 2) {  // count of unpaired nodes
+    if (ensure_partials(L, 1)) return 1;
+    CK(cudaMemsetAsync(L.partials, 0, sizeof(double), L.stream));
+  }
   const long long chunk = L.staging_nodes / 15;
   for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
     const long long n = std::min(chunk, L.nnodes - x0);
     CK(cudaMemcpyAsync(L.staging, a + 15 * x0, (size_t)(15 * n) * sizeof(double),
                        cudaMemcpyHostToDevice, L.stream));
-    CK(DISPATCH3(L, launch_put, L, L.staging, x0, n));
+    if (L.precision == 2) {
+      CK(launch_put_bf16(L, L.staging, x0, n, (int *)L.partials));
+    } else {
+      CK(DISPATCH(L, launch_put, L, L.staging, x0, n));
+    }
   }
   CK(cudaStreamSynchronize(L.stream));
   L.layout = SLBC_LAYOUT_N;
+  if (L.precision == 2) {
+    int unpaired = 0;
+    CK(cudaMemcpy(&unpaired, L.partials, sizeof(int), cudaMemcpyDeviceToHost));
+    if (unpaired > 0) {
+      g_err = "slbc_put_pops: " + std::to_string(unpaired) +
+              " nodes hold populations whose deviations are not paired (q and opp(q) differ); "
+              "BF16 paired-deviation storage cannot hold them";
+      return 2;
+    }
+  }
   return 0;
 }
 
@@ -849,6 +871,7 @@ int slbc_propagate(slbc_lattice *h) {
 
 int slbc_collide(slbc_lattice *h) {
   Lattice &L = h->L;
+  if (L.precision == 2 && L.par.skip_solid) return fail_msg(kPairSkipSolid);
   if (to_natural(L)) return 1;
   CK(DISPATCH3(L, launch_collide, L));
   return 0;

@@ -94,8 +94,10 @@ struct Lattice {
   // moment propagation: density snapshot (FP64, and FP32 for FP32 tracers)
   double *mp_rho64 = nullptr;
   float *mp_rho32 = nullptr;
-  // BF16 deviation storage: post-collision moments (drho, ru), two float4
-  // buffers swapped every step, and the deviation scale
+  // BF16 paired-deviation storage: post-collision moments (drho, ru), two
+  // float4 buffers, and the deviation scale; the paired deviations are two
+  // copies of one 16-byte vector per node in pop.  mom_cur selects the
+  // current copy of both; a step writes the other one.
   void *mom[2] = {nullptr, nullptr};
   int mom_cur = 0;
   int graph_mom = 0;
@@ -190,12 +192,12 @@ struct BatchState {
 SLBC_DECLARE_LAUNCHERS(f64)
 SLBC_DECLARE_LAUNCHERS(f32)
 
-// BF16 deviation storage (slbc_bf16.cu): the operations it supports
+// BF16 paired-deviation storage (slbc_bf16.cu): the operations it supports
 cudaError_t launch_step_bf16(Lattice &L, int odd);
+cudaError_t launch_pair_step(Lattice &L, int planes);  // no swap of the state copies
 int bf16_default_planes(const Lattice &L);
-cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n);
+cudaError_t launch_put_bf16(Lattice &L, const double *stage, long long x0, long long n, int *unpaired);
 cudaError_t launch_get_bf16(Lattice &L, double *stage, long long x0, long long n);
-cudaError_t launch_swap_bf16(Lattice &L);
 cudaError_t launch_vsum_bf16(Lattice &L, double fac, const double *psi, double *partials, int nblocks);
 cudaError_t launch_force_bf16(Lattice &L);
 cudaError_t launch_setvel_bf16(Lattice &L, const double *stage, long long x0, long long n, int has_rho,

@@ -122,10 +122,18 @@ __device__ __forceinline__ void rebuild(T (&t)[15], T drho, T rux, T ruy, T ruz,
   t[10] = rhobyb - ru + st; t[11] = rhobyb + ru + st;
 }
 
-// Collision of one node: reference src/lbkernel.c:805-865.
-template <typename T, bool EXACT>
-__device__ __forceinline__ void collide(T (&t)[15], T omega, T comega, T rho0, int stokes,
-                                        bool fluid, T bx, T by, T bz) {
+// Moments of one node after relaxation: density deviation, momentum (with
+// the body force on fluid nodes) and the relaxed stress.
+template <typename T>
+struct Relaxed {
+  T drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz;
+};
+
+// The moment half of the collision: reference src/lbkernel.c:805-836, same
+// evaluation order.
+template <typename T>
+__device__ __forceinline__ Relaxed<T> relax(const T (&t)[15], T omega, T comega, T rho0, int stokes, bool fluid,
+                                            T bx, T by, T bz) {
   const T twoby3 = T(2.0 / 3.0);
   const T p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
   const T lo_sum = t[7] + t[8] + t[9] + t[10], hi_sum = t[11] + t[12] + t[13] + t[14];
@@ -133,27 +141,37 @@ __device__ __forceinline__ void collide(T (&t)[15], T omega, T comega, T rho0, i
   const T lo_y = t[7] + t[8] - t[9] - t[10], hi_y = t[11] + t[12] - t[13] - t[14];
   const T lo_xy = t[7] - t[8] - t[9] + t[10], hi_xy = t[11] - t[12] - t[13] + t[14];
   const T p06 = t[0] + p12 + p34 + p56;
-  const T drho = p06 + (lo_sum + hi_sum);
-  T rux = t[1] - t[2] + lo_x + hi_x;
-  T ruy = t[3] - t[4] + lo_y + hi_y;
-  T ruz = t[5] - t[6] + lo_sum - hi_sum;
-  if (fluid) { rux += bx; ruy += by; ruz += bz; }
-  const T sdiag = twoby3 * drho - p06;
+  Relaxed<T> r;
+  r.drho = p06 + (lo_sum + hi_sum);
+  r.rux = t[1] - t[2] + lo_x + hi_x;
+  r.ruy = t[3] - t[4] + lo_y + hi_y;
+  r.ruz = t[5] - t[6] + lo_sum - hi_sum;
+  if (fluid) { r.rux += bx; r.ruy += by; r.ruz += bz; }
+  const T sdiag = twoby3 * r.drho - p06;
   T sxx = sdiag + p12, syy = sdiag + p34, szz = sdiag + p56;
   T sxy = lo_xy + hi_xy, sxz = lo_x - hi_x, syz = lo_y - hi_y;
   if (stokes) {
     sxx = comega * sxx; sxy = comega * sxy; sxz = comega * sxz;
     syy = comega * syy; syz = comega * syz; szz = comega * szz;
   } else {
-    const T obyr = omega / (rho0 + drho);
-    sxx = comega * sxx + obyr * rux * rux;
-    sxy = comega * sxy + obyr * rux * ruy;
-    sxz = comega * sxz + obyr * rux * ruz;
-    syy = comega * syy + obyr * ruy * ruy;
-    syz = comega * syz + obyr * ruy * ruz;
-    szz = comega * szz + obyr * ruz * ruz;
+    const T obyr = omega / (rho0 + r.drho);
+    sxx = comega * sxx + obyr * r.rux * r.rux;
+    sxy = comega * sxy + obyr * r.rux * r.ruy;
+    sxz = comega * sxz + obyr * r.rux * r.ruz;
+    syy = comega * syy + obyr * r.ruy * r.ruy;
+    syz = comega * syz + obyr * r.ruy * r.ruz;
+    szz = comega * szz + obyr * r.ruz * r.ruz;
   }
-  rebuild<T, EXACT>(t, drho, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
+  r.sxx = sxx; r.syy = syy; r.szz = szz; r.sxy = sxy; r.sxz = sxz; r.syz = syz;
+  return r;
+}
+
+// Collision of one node: reference src/lbkernel.c:805-865.
+template <typename T, bool EXACT>
+__device__ __forceinline__ void collide(T (&t)[15], T omega, T comega, T rho0, int stokes,
+                                        bool fluid, T bx, T by, T bz) {
+  const Relaxed<T> r = relax<T>(t, omega, comega, rho0, stokes, fluid, bx, by, bz);
+  rebuild<T, EXACT>(t, r.drho, r.rux, r.ruy, r.ruz, r.sxx, r.syy, r.szz, r.sxy, r.sxz, r.syz);
 }
 
 // Add the moving-wall term to every population that arrived over a

@@ -307,7 +307,15 @@ slbc_lattice *slb_device(LBSys lb) {
     st->uw_sent = st->uw_gen;
   }
   if (st->a_sent != st->a_gen) {
-    slb_check(slbc_put_pops(st->dev, slb_host_a(lb)), "population upload");
+    int rc = slbc_put_pops(st->dev, slb_host_a(lb));
+    if (rc == 2 && lb->precision == SLB_BF16) {
+      /* the host array stays the state: upload it again in FP32 */
+      printf("Populations with unpaired deviations: lb->precision changed from SLB_BF16 to SLB_FP32\n");
+      lb->precision = SLB_FP32;
+      st->host_a_valid = 1;
+      return slb_device(lb);
+    }
+    slb_check(rc, "population upload");
     st->a_sent = st->a_gen;
   }
   sync_params(lb);
@@ -343,6 +351,16 @@ void lbpull(LBSys lb) {
 void slb_need_populations(LBSys lb, const char *what) {
   if (lb->precision != SLB_BF16) return;
   printf("%s needs stored populations: lb->precision changed from SLB_BF16 to SLB_FP32\n", what);
+  lb->precision = SLB_FP32;
+}
+
+/* BF16 storage pairs the deviations of q and opp(q), which a collision makes
+ * equal; solid nodes left unrelaxed (skip_solid) keep unpaired streamed
+ * populations, so such a lattice steps in FP32. */
+void slb_need_relaxed_solids(LBSys lb) {
+  if (lb->precision != SLB_BF16 || !lb->skip_solid) return;
+  printf("Relaxation only on fluid nodes (skip_solid) needs stored populations: "
+         "lb->precision changed from SLB_BF16 to SLB_FP32\n");
   lb->precision = SLB_FP32;
 }
 
@@ -411,7 +429,7 @@ void wrpars(LBSys lb) {
   for (x = 0; x < lb->nnodes; x++)
     if (lb->obj[x] == NULL) { fxs += lb->bx[x]; fys += lb->by[x]; fzs += lb->bz[x]; nfluid++; }
   nu = (lb->tau - 0.5) / 3.0; eta = lb->rho0 * nu;
-  msize = (lb->precision == SLB_BF16 ? 15.0 * 2 + 32.0 : 15.0 * (lb->precision == SLB_FP32 ? 4 : 8)) * lb->nnodes + 2.0 * lb->nnodes;
+  msize = (lb->precision == SLB_BF16 ? 2 * 16.0 + 2 * 16.0 : 15.0 * (lb->precision == SLB_FP32 ? 4 : 8)) * lb->nnodes + 2.0 * lb->nnodes;
   printf("---------------------------------------------------\n");
   printf(" Operating parameters\n");
   printf("---------------------------------------------------\n");

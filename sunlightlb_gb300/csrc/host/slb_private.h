@@ -55,5 +55,6 @@ long slb_node(LBSys lb, int i, int j, int k);
 void slb_trace(LBSys lb, const char *what);
 void slb_pull_rho(LBSys lb);
 void slb_need_populations(LBSys lb, const char *what);
+void slb_need_relaxed_solids(LBSys lb);
 
 #endif

@@ -59,7 +59,9 @@ void propagate(LBSys lb) {
 
 /* reference src/lbkernel.c:769-877 */
 void collide(LBSys lb) {
-  slbc_lattice *d = slb_device(lb);
+  slbc_lattice *d;
+  slb_need_relaxed_solids(lb);
+  d = slb_device(lb);
   if (lb->status != POST_PROPAGATE) out_of_position(lb, "Collision");
   slb_check(slbc_collide(d), "collision");
   slb_device_changed(lb);
@@ -73,6 +75,7 @@ void collide(LBSys lb) {
  * that bounce-back (reference src/lbkernel.c:41-51). */
 static void fused_step(LBSys lb, int with_force) {
   slbc_lattice *d;
+  slb_need_relaxed_solids(lb);
   if (lb->changed_objects) syncobjs(lb);
   d = slb_device(lb);
   if (with_force) {
@@ -104,6 +107,7 @@ void lbsteps(LBSys lb, int n) {
   slbc_lattice *d;
   if (n <= 0) return;
   if (lb->status != POST_COLLIDE) { lbstep(lb); n--; if (n <= 0) return; }
+  slb_need_relaxed_solids(lb);
   if (lb->changed_objects) syncobjs(lb);
   d = slb_device(lb);
   slb_check(slbc_step(d, n, 1), "update steps");

@@ -66,3 +66,56 @@ def test_bf16_separate_phases_move_to_fp32(gpu, orc):
         L.lbsteps(lb, 10)
     assert g.precision == 1
     assert rel(g.pops(), o.pops()) < 2e-5
+
+
+def test_bf16_skip_solid_moves_to_fp32(gpu, orc):
+    """Solid nodes left unrelaxed keep streamed populations whose deviations
+    are not paired (q and opp(q) differ), so BF16 storage cannot hold them:
+    the lattice steps in FP32 and follows the oracle to FP32 accuracy."""
+    g = two_spheres(gpu, tau=1.0, skip=1, steps=60, precision=2)
+    o = two_spheres(orc, tau=1.0, skip=1, steps=60)
+    assert g.precision == 1
+    assert rel(g.pops(), o.pops()) < 2e-5
+    assert rel(objects_ft(g)[:, :3], objects_ft(o)[:, :3]) < 2e-5
+
+
+def _uploaded(gpu, orc, perturb):
+    """The oracle's state after 40 steps at tau 0.8 (non-zero stress), with
+    perturb applied, uploaded into a BF16 lattice and into a second oracle
+    lattice; both then take 30 more steps."""
+    src = two_spheres(orc, tau=0.8, steps=40, measure=False)
+    state = src.pops()
+    perturb(state)
+    out = []
+    for L, prec in ((gpu, 2), (orc, 0)):
+        lb = two_spheres(L, tau=0.8, steps=0, measure=False, precision=prec)
+        lb.pops()
+        lb.array("a")[:] = state
+        L.lbpush(lb)
+        L.lbsteps(lb, 30)
+        L.measure(lb)
+        out.append(lb)
+    return out
+
+
+def test_bf16_upload_of_collided_state_stays_bf16(gpu, orc):
+    """A post-collision state has paired deviations: it stays in BF16
+    storage; after 30 more steps populations, mean flow and drag are within
+    2e-3 (the BF16 rounding of the stress part)."""
+    g, o = _uploaded(gpu, orc, lambda a: None)
+    assert g.precision == 2
+    assert rel(g.pops(), o.pops()) < 2e-3
+    assert abs(g.vmeanx - o.vmeanx) <= 2e-3 * abs(o.vmeanx)
+    assert rel(objects_ft(g)[:, :3], objects_ft(o)[:, :3]) < 2e-3
+
+
+def test_bf16_upload_of_unpaired_state_moves_to_fp32(gpu, orc):
+    """One population changed on one fluid node: its deviations are no
+    longer paired, the upload moves the lattice to FP32 and the run follows
+    the oracle to FP32 accuracy."""
+    def bump(a):
+        a[5, 1] += 1e-3
+    g, o = _uploaded(gpu, orc, bump)
+    assert g.precision == 1
+    assert rel(g.pops(), o.pops()) < 2e-5
+    assert abs(g.vmeanx - o.vmeanx) <= 2e-5 * abs(o.vmeanx)
