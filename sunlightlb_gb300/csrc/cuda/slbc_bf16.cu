@@ -71,9 +71,6 @@ __device__ __forceinline__ float eq_pop(int q, float4 m) {
   }
 }
 
-// BF16 bits in the low 16 bits of u -> FP32 (exact)
-__device__ __forceinline__ float bf_bits(uint32_t u) { return __uint_as_float(u << 16); }
-
 // stored deviation of pair p in a packed vector
 __device__ __forceinline__ float pair_dev(const uint4 &v, int p) {
   const uint32_t w = p < 2 ? v.x : (p < 4 ? v.y : (p < 6 ? v.z : v.w));
@@ -108,6 +105,11 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
                "l"(gmem)
                : "memory");
 }
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
@@ -119,12 +121,15 @@ constexpr int kPairSlots = 4;  // planes i-1, i, i+1 in use, i+2 arriving
 // one-node halo, sits in shared memory: the three a node gathers from and
 // the next one, copied in by cp.async while the current plane is updated.
 // Every value a node gathers comes from shared memory; global memory sees
-// one 16-byte load of each state vector per node (plus the halo) and one
-// store of each.  Nodes are independent, so there is one barrier per plane.
+// one load of each state vector per node (plus the halo) and one store of
+// each.  Nodes are independent, so there is one barrier per plane.  The
+// deviations sit word-major in the ring (word w = pairs 2w, 2w+1 of every
+// node in a row), so a warp gathering one pair from 32 neighbours reads
+// 32 consecutive words, free of bank conflicts.
 template <bool MOVING, bool BFU>
 __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepArgs<float> s, int planes) {
   __shared__ float4 ringM[kPairSlots][kPlane];
-  __shared__ uint4 ringP[kPairSlots][kPlane];
+  __shared__ uint32_t ringW[kPairSlots][4][kPlane];
   const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
   const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
   const int np = min(planes, a.esi - i0);
@@ -143,8 +148,11 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepA
 #pragma unroll
     for (int e = 0; e < kPlaneLoads; e++) {
       if (off[e] < 0) continue;
-      cp_async16(&ringM[slot][tid + kTileThreads * e], a.Min + base + off[e]);
-      cp_async16(&ringP[slot][tid + kTileThreads * e], a.Pin + base + off[e]);
+      const int c = tid + kTileThreads * e;
+      cp_async16(&ringM[slot][c], a.Min + base + off[e]);
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(a.Pin + base + off[e]);
+#pragma unroll
+      for (int h = 0; h < 4; h++) cp_async4(&ringW[slot][h][c], w + h);
     }
     cp_async_commit();
   };
@@ -153,21 +161,24 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepA
   fetch(i0 + 1, 2);
   const int j = j0 + tj, k = k0 + tk;
   const bool mine = j < a.esj && k < a.esk;
-  const int own = j * a.esk + k;
+  const int own = mine ? j * a.esk + k : 0;
   const int c0 = (tj + 1) * kHaloK + tk + 1;
+  uint16_t fl_next = __ldg(a.flags + (long long)i0 * plane_nodes + own);  // flag word, one plane ahead
   for (int ii = 0; ii < np; ii++) {
     const int i = i0 + ii;
+    const uint16_t fl = fl_next;
+    if (ii + 1 < np) fl_next = __ldg(a.flags + (long long)(i + 1) * plane_nodes + own);
     cp_async_wait_all();
     __syncthreads();  // plane i+1 has arrived; slot of plane i-2 is free
     if (ii + 1 < np) fetch(i + 2, (ii + 3) % kPairSlots);
     if (!mine) continue;
-    const float4 *RM[3] = {ringM[ii % kPairSlots], ringM[(ii + 1) % kPairSlots], ringM[(ii + 2) % kPairSlots]};
-    const uint4 *RP[3] = {ringP[ii % kPairSlots], ringP[(ii + 1) % kPairSlots], ringP[(ii + 2) % kPairSlots]};
+    const int s0 = ii % kPairSlots, s1 = (ii + 1) % kPairSlots, s2 = (ii + 2) % kPairSlots;
+    const float4 *RM[3] = {ringM[s0], ringM[s1], ringM[s2]};
+    const uint32_t(*RW[3])[kPlane] = {ringW[s0], ringW[s1], ringW[s2]};
     const int x = i * plane_nodes + own;
-    const uint16_t fl = __ldg(a.flags + x);
     const bool solid = (fl & FLAG_SOLID) != 0;
     const float4 mx = RM[1][c0];
-    const uint4 px = RP[1][c0];
+    const uint4 px = make_uint4(RW[1][0][c0], RW[1][1][c0], RW[1][2][c0], RW[1][3][c0]);
     // A bounce-back link (bit q) returns the node's own post-collision
     // opp(q): eq_opp(q)(m) is eq_q of m with the momentum negated (exact:
     // only signs change) and the deviation is that of the same pair.
@@ -180,7 +191,8 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepA
       const bool bnd = (fl >> q) & 1;
       const int c = c0 - CY(q) * kHaloK - CZ(q);
       const float4 my = RM[1 - CX(q)][c];
-      const float dy = bf_bits(reinterpret_cast<const unsigned short *>(RP[1 - CX(q)] + c)[pair_of(q)]);
+      const uint32_t wy = RW[1 - CX(q)][pair_of(q) >> 1][c];
+      const float dy = (pair_of(q) & 1) ? __uint_as_float(wy & 0xffff0000u) : __uint_as_float(wy << 16);
       const float4 m = bnd ? mneg : my;
       const float d = bnd ? pair_dev(px, pair_of(q)) : dy;
       t[q] = eq_pop(q, m) + d * a.inv;
