@@ -515,6 +515,26 @@ int ensure_graph(Lattice &L) {
 }  // namespace
 
 namespace slbc {
+
+// 1/rho of the FP64 density snapshot, for the FP32 tracer update
+__global__ void k_mp_rinv(const double *rho64, float *rinv, long long n) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) rinv[x] = (float)(1.0 / rho64[x]);
+}
+
+cudaError_t ensure_mp_rinv(Lattice &L) {
+  if (L.mp_rinv32 && L.mp_rinv_gen == L.mp_rho_gen) return cudaSuccess;
+  if (!L.mp_rho64) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+  if (!L.mp_rinv32) e = cudaMalloc(&L.mp_rinv32, (size_t)L.nnodes * sizeof(float));
+  if (e != cudaSuccess) return e;
+  k_mp_rinv<<<(int)((L.nnodes + 255) / 256), 256, 0, L.stream>>>(L.mp_rho64, L.mp_rinv32, L.nnodes);
+  g_launches += 1;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) L.mp_rinv_gen = L.mp_rho_gen;
+  return e;
+}
+
 void count_launch(int n) { g_launches += n; }
 void set_error(const std::string &msg) { g_err = msg; }
 int reduction_blocks(const Lattice &L) {
@@ -581,7 +601,7 @@ void slbc_destroy(slbc_lattice *h) {
   void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
                   L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
                   L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1],
-                  L.ads_links};
+                  L.ads_links, L.mp_rinv32};
   for (void *b : bufs) if (b) cudaFree(b);
   if (L.host_out) cudaFreeHost(L.host_out);
   if (L.graph) cudaGraphExecDestroy(L.graph);
@@ -1058,6 +1078,7 @@ int slbc_mp_rhoinit(slbc_lattice *h) {
   Lattice &L = h->L;
   if (!L.mp_rho64) CK(cudaMalloc(&L.mp_rho64, (size_t)L.nnodes * sizeof(double)));
   CK(DISPATCH3(L, launch_mp_rhoinit, L));
+  L.mp_rho_gen++;
   return 0;
 }
 

@@ -94,6 +94,10 @@ struct Lattice {
   // moment propagation: density snapshot (FP64, and FP32 for FP32 tracers)
   double *mp_rho64 = nullptr;
   float *mp_rho32 = nullptr;
+  // 1/rho in FP32 for the FP32 tracer update, rebuilt when the snapshot
+  // changes (mp_rho_gen counts snapshots)
+  float *mp_rinv32 = nullptr;
+  unsigned long long mp_rho_gen = 1, mp_rinv_gen = 0;
   // BF16 paired-deviation storage: post-collision moments (drho, ru), two
   // float4 buffers, and the deviation scale; the paired deviations are two
   // copies of one 16-byte vector per node in pop.  mom_cur selects the
@@ -204,6 +208,10 @@ cudaError_t launch_setvel_bf16(Lattice &L, const double *stage, long long x0, lo
                                int skip_solid);
 cudaError_t launch_collide_bf16(Lattice &L);
 cudaError_t launch_mp_rhoinit_bf16(Lattice &L);
+
+// 1/rho of the density snapshot for FP32 tracers, rebuilt when stale
+// (slbc_core.cu)
+cudaError_t ensure_mp_rinv(Lattice &L);
 
 // Launch bookkeeping and error text (defined in slbc_core.cu)
 void count_launch(int n = 1);

@@ -303,6 +303,24 @@ cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, i
   m.alpha = alpha; m.adprob = adprob; m.rho0 = L.par.rho0;
   m.alpha_f = (float)alpha; m.adprob_f = (float)adprob; m.rho0_f = (float)L.par.rho0;
   m.partial = adprob != 1.0;
+  // FP32 tracers: the division-free kernel in link order, while 32-bit
+  // population indices reach (15 * npad < 2^32)
+  if (!tp_f64 && 15ULL * (unsigned long long)L.npad < (1ULL << 32)) {
+    const cudaError_t e = ensure_mp_rinv(L);
+    if (e != cudaSuccess) return e;
+    const PopArgs<T_> pa = pop_args(L);
+    const float *ri = L.mp_rinv32;
+    switch (L.layout * 2 + (moving ? 1 : 0)) {
+      case SLBC_LAYOUT_N * 2: k_mp_step_f32<T_, SLBC_LAYOUT_N, false><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+      case SLBC_LAYOUT_N * 2 + 1: k_mp_step_f32<T_, SLBC_LAYOUT_N, true><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+      case SLBC_LAYOUT_C0 * 2: k_mp_step_f32<T_, SLBC_LAYOUT_C0, false><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+      case SLBC_LAYOUT_C0 * 2 + 1: k_mp_step_f32<T_, SLBC_LAYOUT_C0, true><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+      case SLBC_LAYOUT_C1 * 2: k_mp_step_f32<T_, SLBC_LAYOUT_C1, false><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+      default: k_mp_step_f32<T_, SLBC_LAYOUT_C1, true><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
+    }
+    count_launch();
+    return cudaGetLastError();
+  }
   // the wrap-node buckets need more than the default 48 KB of dynamic
   // shared memory for FP64 tracers
   static unsigned long long attr_set[2] = {0, 0};  // per device, bit = device index

@@ -305,6 +305,149 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(TP) == 8 ? 2 : 3) k_mp_st
   }
 }
 
+// FP32 tracer update: the terms of k_mp_step with TP = float, added in link
+// order (the reference's summation order matters for FP64 bit parity only).
+// The density snapshot enters as 1/rho (rinv, FP32), so a source node costs
+// no division: fac = p/rho and piece = p/72 * (rho0/rho - alpha) are products.
+// Each link term is the case-A/B/C expression times a factor that the flag
+// word, the adsorbing-link mask and the adsorption probability P decide:
+//   fluid x:  1, or over a link from an adsorbing solid (1 - P), 0 when P = 1;
+//   solid x (adsorbing): P over boundary links (1 when P = 1), 0 otherwise;
+// and on fluid boundary nodes with moving walls the wall term is added first.
+// Population indices are 32-bit (15 * npad < 2^32) and the layout is a
+// template argument, so a link's load costs a neighbour index, a select and
+// one address computation.
+template <typename T, int LAYOUT, bool MOVING>
+__global__ void __launch_bounds__(kTileThreads, 3)
+k_mp_step_f32(PopArgs<T> p, MpArgs m, const float *rinv, int planes) {
+  __shared__ MpSource<float> ring[3][kPlane];
+  const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
+  const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
+  const int np = min(planes, p.esi - i0);
+  const int plane_nodes = p.esj * p.esk;
+  const float alpha = m.alpha_f, rho0 = m.rho0_f, Pa = m.adprob_f;
+  const float cB = m.partial ? Pa : 1.0f;         // link into an adsorbing solid
+  const float cC = m.partial ? 1.0f - Pa : 0.0f;  // link from an adsorbing solid
+  const unsigned npad = (unsigned)p.npad;
+  int off[kPlaneLoads];
+#pragma unroll
+  for (int e = 0; e < kPlaneLoads; e++) {
+    const int c = tid + kTileThreads * e;
+    off[e] = c < kPlane ? wrap_index(j0 - 1 + c / kHaloK, p.esj) * p.esk + wrap_index(k0 - 1 + c % kHaloK, p.esk)
+                        : -1;
+  }
+  const float *pin = (const float *)m.p_in;
+  auto source_of = [&](float pt, float ri) {
+    MpSource<float> r;
+    r.fac = pt * ri;
+    r.piece = pt * (1.0f / 72.0f) * (rho0 * ri - alpha);
+    return r;
+  };
+  // plane q sits in ring slot (q - i0 + 1) % 3
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int base = wrap_index(i0 - 1 + h, p.esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = source_of(pin[base + off[e]], rinv[base + off[e]]);
+  }
+  // register prefetch one plane ahead: p and 1/rho of the halo tile of
+  // plane i+1, and the flag word, adsorption byte, adsorbing links and p of
+  // this thread's node of plane i
+  float pre_p[kPlaneLoads], pre_r[kPlaneLoads];
+  const int j = j0 + tj, k = k0 + tk;
+  const bool mine = j < p.esj && k < p.esk;
+  const int own = mine ? j * p.esk + k : 0;
+  auto prefetch_ring = [&](int plane) {
+    const int base = wrap_index(plane, p.esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) { pre_p[e] = pin[base + off[e]]; pre_r[e] = rinv[base + off[e]]; }
+  };
+  uint16_t n_fl = 0, n_al = 0;
+  unsigned char n_ads = 0;
+  float n_p = 0.0f;
+  auto prefetch_node = [&](int plane) {
+    const int x = plane * plane_nodes + own;
+    n_fl = p.flags[x];
+    n_ads = m.ads ? m.ads[x] : 0;
+    n_al = m.ads ? m.ads_links[x] : 0;
+    n_p = pin[x];
+  };
+  prefetch_ring(i0 + 1);
+  prefetch_node(i0);
+  float *pout = (float *)m.p_out;
+  const T *P = p.pop;
+  const int c0 = (tj + 1) * kHaloK + tk + 1;
+  for (int ii = 0; ii < np; ii++) {
+    const int i = i0 + ii;
+    const int sm = ii % 3, s0 = (ii + 1) % 3, sp = (ii + 2) % 3;  // planes i-1, i, i+1
+    __syncthreads();  // slot sp held plane i-2, last read in the previous iteration
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[sp][tid + kTileThreads * e] = source_of(pre_p[e], pre_r[e]);
+    __syncthreads();
+    const uint16_t fl = n_fl, al = n_al;
+    const bool ads_x = n_ads != 0;
+    const float pt_x = n_p;
+    if (ii + 1 < np) {
+      prefetch_ring(i + 2);
+      prefetch_node(i + 1);
+    }
+    if (!mine) continue;
+    const MpSource<float> *R[3] = {ring[sm], ring[s0], ring[sp]};
+    const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+    const int x = nb.at(0, 0, 0);
+    const bool solid = (fl & FLAG_SOLID) != 0;
+    if (solid && !ads_x) { pout[x] = 0.0f; continue; }
+    const MpSource<float> ex = R[1][c0];
+    const unsigned bmask = fl & FLAG_LINKS;
+    // factor masks: zero (solid x: links that are not boundary links, and
+    // the rest link q = 0) and the adsorption factor cval
+    const unsigned zmask = solid ? (~bmask & 0x7FFFu) : 0u;
+    const unsigned amask = solid ? bmask : (unsigned)al;
+    const float cval = solid ? cB : cC;
+    float sum = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 15; q++) {
+      float t;
+      if (q == 0) {
+        t = ex.fac * (float)P[x] + 16.0f * ex.piece + alpha * pt_x;
+      } else {
+        const bool bnd = (bmask >> q) & 1u;
+        const bool self_c = bnd && !solid;  // solid y returns what x sent along opp(q)
+        const int y = nb.at(-CX(q), -CY(q), -CZ(q));
+        unsigned idx;
+        if (LAYOUT == SLBC_LAYOUT_N) {
+          idx = self_c ? OPP(q) * npad + (unsigned)x : q * npad + (unsigned)y;
+        } else if (LAYOUT == SLBC_LAYOUT_C0) {
+          idx = self_c ? q * npad + (unsigned)x : OPP(q) * npad + (unsigned)y;
+        } else {  // C1: pushed into x unless y -> x is a boundary link
+          idx = (bnd && solid) ? OPP(q) * npad + (unsigned)y : q * npad + (unsigned)x;
+        }
+        const float av = (float)P[idx];
+        const MpSource<float> e = R[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
+        const float fac = self_c ? ex.fac : e.fac;
+        const float pw = self_c ? ex.piece : e.piece;
+        t = fac * av + (q <= 6 ? 8.0f : 1.0f) * pw;
+        if (MOVING && self_c) {
+          float u[3];
+          const int o = m.objidx[y];
+          int yi = i - CX(q), yj = j - CY(q), yk = k - CZ(q);
+          yi = yi < 0 ? p.esi - 1 : (yi >= p.esi ? 0 : yi);
+          yj = yj < 0 ? p.esj - 1 : (yj >= p.esj ? 0 : yj);
+          yk = yk < 0 ? p.esk - 1 : (yk >= p.esk ? 0 : yk);
+          mp_wall_u<float>(m.objstate + 9 * o, yi, yj, yk, rho0, u);
+          t += mp_wall_term<float>(q, ex.fac, u);
+        }
+      }
+      const float f = ((zmask >> q) & 1u) ? 0.0f : (((amask >> q) & 1u) ? cval : 1.0f);
+      sum += f * t;
+    }
+    pout[x] = solid ? pt_x + sum : sum;
+  }
+}
+
 // Density snapshot (reference src/mpmisc.c:64-79), kept in FP64 and, when
 // FP32 tracers exist, in FP32.
 template <typename T>

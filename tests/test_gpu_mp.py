@@ -148,3 +148,43 @@ def test_source_plane_breakthrough_and_balance(gpu, orc, mp_precision):
     assert abs(ig - io) <= tol * io
     assert abs(ho - io) <= 1e-12 * io          # oracle: exact balance
     assert abs(hg - ig) <= (1e-5 if mp_precision else 1e-12) * ig
+
+
+@pytest.mark.parametrize("cfg", [dict(moving=1), dict(ads=1), dict(ads=1, adprob=0.37),
+                                 dict(moving=1, ads=1, adprob=0.37)])
+def test_tracer_fp32_cases_close_to_fp64(gpu, orc, cfg):
+    """FP32 tracer update (terms in link order, 1/rho snapshot) with moving
+    walls and full or partial adsorption, flow steps between tracer steps
+    (both AA layouts), against the FP64 oracle: within 2e-5 of the largest
+    value after 60 updates."""
+    pg = tracer_run(gpu, precision=1, mp_precision=1, steps=60, **cfg)[1].field().copy()
+    po = tracer_run(orc, steps=60, **cfg)[1].field().copy()
+    assert np.abs(pg - po).max() <= 2e-5 * np.abs(po).max()
+
+
+def test_tracer_fp32_on_uploaded_flow(gpu, orc):
+    """FP32 tracer updates on a flow just uploaded (the reference's layout),
+    partial adsorption, against the FP64 oracle within 2e-5."""
+    out = []
+    for L, prec, mpp in ((gpu, 1, 1), (orc, 0, None)):
+        lb, mp = tracer_run(L, precision=prec, mp_precision=mpp, steps=0, interleave=False, ads=1, adprob=0.37)
+        lb.pops()
+        L.lbpush(lb)
+        for _ in range(30):
+            L.mpstep(mp)
+        L.mppull(mp)
+        out.append(mp.field().copy())
+    assert np.abs(out[0] - out[1]).max() <= 2e-5 * np.abs(out[1]).max()
+
+
+def test_tracer_fp32_mass_balance_frozen_flow(gpu):
+    """FP32 tracer, flow frozen: fluid + adsorbed tracer conserved to 1e-5
+    over 200 updates."""
+    for P in (1.0, 0.01):
+        lb, mp = tracer_run(gpu, ads=1, adprob=P, steps=0, interleave=False, precision=1, mp_precision=1)
+        gpu.mpall(mp, 1.0)
+        m0 = gpu.mptotal(mp, "fluid") + gpu.mptotal(mp, "adsorbed")
+        for _ in range(200):
+            gpu.mpstep(mp)
+        m1 = gpu.mptotal(mp, "fluid") + gpu.mptotal(mp, "adsorbed")
+        assert abs(m1 - m0) <= 1e-5 * m0, (P, m0, m1)
