@@ -451,7 +451,11 @@ def run_reference(args):
 TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED = 0.35, 6.0, 12.0, 4
 TRACER_ALPHA, TRACER_ADPROB = 0.5, 0.01
 # bytes per tracer update: 15 FP32 populations + p in, rho, p out
-TRACER_BYTES = {1: 60 + 3 * 4, 0: 60 + 3 * 8}
+# bytes per tracer update on the frozen flow: FP32 tracers apply 15 FP32
+# stencil coefficients per node and read and write p (the coefficients are
+# built once from the flow); FP64 tracers read 15 FP32 populations, p and
+# rho (FP64) and write p
+TRACER_BYTES = {1: 60 + 2 * 4, 0: 60 + 3 * 8}
 
 
 def time_tracer(torch, L, lb, mp, steps):
@@ -544,7 +548,9 @@ def run_tracer(args):
             "MLUPS_with_planes_and_samples": round(nodes * nsteps / wall / 1e6, 1),
             "kernel": {"MLUPS": round(nodes / (kms * 1e-3) / 1e6, 1), "ms_per_step": round(kms, 4),
                        "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
-                       "bytes_per_update": TRACER_BYTES[prec]},
+                       "bytes_per_update": TRACER_BYTES[prec],
+                       "update": "stencil coefficients of the frozen flow" if prec == 1 else
+                                 "terms from the populations, the reference's summation order"},
             "balance": {"fluid": fl, "adsorbed": ad, "all": al, "injected": inj,
                         "rel_error": (al - inj) / inj if inj else None},
             "breakthrough": curve,

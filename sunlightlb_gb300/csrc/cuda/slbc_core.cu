@@ -522,6 +522,71 @@ __global__ void k_mp_rinv(const double *rho64, float *rinv, long long n) {
   if (x < n) rinv[x] = (float)(1.0 / rho64[x]);
 }
 
+// One FP32 tracer update from stencil coefficients (k_mp_coef):
+// p'(x) = C_0(x) p(x) + sum_q C_q(x) p(x - c_q).  Tiles of 32 (k) x 8 (j)
+// nodes march along i with p of three planes (and halo) in shared memory,
+// the next plane prefetched into registers; the 15 coefficient loads per
+// node are the stream from memory.
+__global__ void __launch_bounds__(kTileThreads, 4)
+k_mp_apply(const float *coef, const float *pin, float *pout, int esi, int esj, int esk, unsigned npad, int planes) {
+  __shared__ float ring[3][kPlane];
+  const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
+  const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
+  const int np = min(planes, esi - i0);
+  const int plane_nodes = esj * esk;
+  int off[kPlaneLoads];
+#pragma unroll
+  for (int e = 0; e < kPlaneLoads; e++) {
+    const int c = tid + kTileThreads * e;
+    off[e] = c < kPlane ? wrap_index(j0 - 1 + c / kHaloK, esj) * esk + wrap_index(k0 - 1 + c % kHaloK, esk) : -1;
+  }
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int base = wrap_index(i0 - 1 + h, esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = pin[base + off[e]];
+  }
+  float pre[kPlaneLoads];
+  auto prefetch = [&](int plane) {
+    const int base = wrap_index(plane, esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) pre[e] = pin[base + off[e]];
+  };
+  prefetch(i0 + 1);
+  const int j = j0 + tj, k = k0 + tk;
+  const bool mine = j < esj && k < esk;
+  const int own = mine ? j * esk + k : 0;
+  const int c0 = (tj + 1) * kHaloK + tk + 1;
+  for (int ii = 0; ii < np; ii++) {
+    const int i = i0 + ii;
+    const int sm = ii % 3, s0 = (ii + 1) % 3, sp = (ii + 2) % 3;  // planes i-1, i, i+1
+    __syncthreads();  // slot sp held plane i-2, last read in the previous iteration
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) ring[sp][tid + kTileThreads * e] = pre[e];
+    __syncthreads();
+    if (ii + 1 < np) prefetch(i + 2);
+    if (!mine) continue;
+    const float *R[3] = {ring[sm], ring[s0], ring[sp]};
+    const unsigned x = (unsigned)(i * plane_nodes + own);
+    float cq[15];
+#pragma unroll
+    for (int q = 0; q < 15; q++) cq[q] = __ldcs(coef + q * npad + x);
+    float sum = cq[0] * R[1][c0];
+#pragma unroll
+    for (int q = 1; q < 15; q++) sum += cq[q] * R[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
+    pout[x] = sum;
+  }
+}
+
+cudaError_t launch_mp_apply(Lattice &L, const float *pin, float *pout, dim3 grid, dim3 block, int planes) {
+  k_mp_apply<<<grid, block, 0, L.stream>>>(L.mp_coef, pin, pout, L.esi, L.esj, L.esk, (unsigned)L.npad, planes);
+  g_launches += 1;
+  return cudaGetLastError();
+}
+
 cudaError_t ensure_mp_rinv(Lattice &L) {
   if (L.mp_rinv32 && L.mp_rinv_gen == L.mp_rho_gen) return cudaSuccess;
   if (!L.mp_rho64) return cudaErrorInvalidValue;
@@ -601,7 +666,7 @@ void slbc_destroy(slbc_lattice *h) {
   void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
                   L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
                   L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1],
-                  L.ads_links, L.mp_rinv32};
+                  L.ads_links, L.mp_rinv32, L.mp_coef};
   for (void *b : bufs) if (b) cudaFree(b);
   if (L.host_out) cudaFreeHost(L.host_out);
   if (L.graph) cudaGraphExecDestroy(L.graph);
@@ -796,6 +861,7 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
 
 int slbc_put_pops(slbc_lattice *h, const double *a) {
   Lattice &L = h->L;
+  L.state_version++;
   if (ensure_staging(L, L.nnodes, 15)) return 1;
   if (L.precision == 2) {  // count of unpaired nodes
     if (ensure_partials(L, 1)) return 1;
@@ -858,6 +924,7 @@ void slbc_host_free(void *p) {
 
 int slbc_step(slbc_lattice *h, int n, int use_graph) {
   Lattice &L = h->L;
+  L.state_version++;
   if (to_aa(L)) return 1;
   if (L.tune_state == 0 && autotune(L)) return 1;
   int done = 0;
@@ -878,6 +945,7 @@ int slbc_step(slbc_lattice *h, int n, int use_graph) {
 
 int slbc_force_step(slbc_lattice *h) {
   Lattice &L = h->L;
+  L.state_version++;
   if (to_aa(L)) return 1;
   CK(DISPATCH3(L, launch_force, L));
   return one_step(L);
@@ -885,6 +953,7 @@ int slbc_force_step(slbc_lattice *h) {
 
 int slbc_bbl(slbc_lattice *h, int with_force) {
   Lattice &L = h->L;
+  L.state_version++;
   if (no_bf16(L, "slbc_bbl")) return 1;
   if (to_natural(L)) return 1;
   CK(DISPATCH(L, launch_bbl, L, with_force));
@@ -893,6 +962,7 @@ int slbc_bbl(slbc_lattice *h, int with_force) {
 
 int slbc_propagate(slbc_lattice *h) {
   Lattice &L = h->L;
+  L.state_version++;
   if (no_bf16(L, "slbc_propagate")) return 1;
   if (to_natural(L)) return 1;
   if (ensure_scratch(L)) return 1;
@@ -904,6 +974,7 @@ int slbc_propagate(slbc_lattice *h) {
 
 int slbc_collide(slbc_lattice *h) {
   Lattice &L = h->L;
+  L.state_version++;
   if (L.precision == 2 && L.par.skip_solid) return fail_msg(kPairSkipSolid);
   if (to_natural(L)) return 1;
   CK(DISPATCH3(L, launch_collide, L));
@@ -984,6 +1055,7 @@ int slbc_distribf(slbc_lattice *h, const double *pos, double *ft) {
 int slbc_set_velocity(slbc_lattice *h, const double *rho, const double *ux, const double *uy,
                       const double *uz, int skip_solid) {
   Lattice &L = h->L;
+  L.state_version++;
   if (ensure_staging(L, L.nnodes, 4)) return 1;
   const long long chunk = L.staging_nodes / 4;
   std::vector<double> buf((size_t)(4 * std::min(chunk, L.nnodes)));
@@ -1011,6 +1083,7 @@ int slbc_get_velocity_dev(slbc_lattice *h, double fac, float *u) {
 
 int slbc_set_velocity_dev(slbc_lattice *h, const float *u, int skip_solid) {
   Lattice &L = h->L;
+  L.state_version++;
   if (!u) return fail_msg("slbc_set_velocity_dev: null input");
   if (ensure_staging(L, L.nnodes, 4)) return 1;
   const long long chunk = L.staging_nodes / 4;
@@ -1328,6 +1401,7 @@ int slbc_batch_step(slbc_batch *b, int nsteps) {
   if (nsteps <= 0) return 0;
   BatchState &B = b->B;
   for (Lattice *L : B.lats) {
+    L->state_version++;
     if (L->precision != B.precision) return fail_msg("slbc_batch_step: a lattice changed precision");
     if (to_aa(*L)) return 1;
     CK(cudaStreamSynchronize(L->stream));  // the batch stream follows every lattice's work

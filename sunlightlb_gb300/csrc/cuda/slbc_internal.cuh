@@ -98,6 +98,15 @@ struct Lattice {
   // changes (mp_rho_gen counts snapshots)
   float *mp_rinv32 = nullptr;
   unsigned long long mp_rho_gen = 1, mp_rinv_gen = 0;
+  // counts changes of the populations (steps, uploads, phases, warm starts)
+  unsigned long long state_version = 0;
+  // FP32 tracer on a frozen flow: per-node stencil coefficients
+  // (mp_coef[q*npad + x], q = 0 the node itself), valid for mp_coef_key;
+  // mp_last_key is the state seen by the previous FP32 tracer update
+  float *mp_coef = nullptr;
+  unsigned long long mp_coef_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long mp_last_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  bool mp_coef_valid = false;
   // BF16 paired-deviation storage: post-collision moments (drho, ru), two
   // float4 buffers, and the deviation scale; the paired deviations are two
   // copies of one 16-byte vector per node in pop.  mom_cur selects the
@@ -212,6 +221,8 @@ cudaError_t launch_mp_rhoinit_bf16(Lattice &L);
 // 1/rho of the density snapshot for FP32 tracers, rebuilt when stale
 // (slbc_core.cu)
 cudaError_t ensure_mp_rinv(Lattice &L);
+// one FP32 tracer update from the lattice's stencil coefficients
+cudaError_t launch_mp_apply(Lattice &L, const float *pin, float *pout, dim3 grid, dim3 block, int planes);
 
 // Launch bookkeeping and error text (defined in slbc_core.cu)
 void count_launch(int n = 1);

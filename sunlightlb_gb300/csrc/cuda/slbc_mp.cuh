@@ -448,6 +448,81 @@ k_mp_step_f32(PopArgs<T> p, MpArgs m, const float *rinv, int planes) {
   }
 }
 
+// Stencil coefficients of the FP32 tracer update on a frozen flow.  Every
+// term of k_mp_step_f32 is p of one node times a factor that depends only on
+// the flow, the density snapshot, alpha, P and the geometry, so one update is
+//   p'(x) = C_0(x) p(x) + sum_{q=1..14} C_q(x) p(x - c_q):
+// case A (and B) terms from y = x - c_q go to C_q; case C terms (x's own
+// populations returned by a solid neighbour, with the moving-wall term) and
+// the q = 0 term go to C_0; an adsorbing solid keeps its own p (C_0 += 1); a
+// non-adsorbing solid gets all zeros.  coef[q * npad + x], one thread per
+// node; the layout is that of the flow when the coefficients were built.
+template <typename T, int LAYOUT, bool MOVING>
+__global__ void __launch_bounds__(256) k_mp_coef(PopArgs<T> p, MpArgs m, const float *rinv, float *coef) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)p.esi * p.esj * p.esk) return;
+  const int x = (int)e;
+  int i, j, k;
+  decode(x, p.esj, p.esk, i, j, k);
+  const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+  const unsigned npad = (unsigned)p.npad;
+  const uint16_t fl = p.flags[x];
+  const bool solid = (fl & FLAG_SOLID) != 0;
+  const bool ads_x = m.ads ? m.ads[x] != 0 : false;
+  float c[15];
+#pragma unroll
+  for (int q = 0; q < 15; q++) c[q] = 0.0f;
+  if (!solid || ads_x) {
+    const float alpha = m.alpha_f, rho0 = m.rho0_f, Pa = m.adprob_f;
+    const float cB = m.partial ? Pa : 1.0f, cC = m.partial ? 1.0f - Pa : 0.0f;
+    const T *P = p.pop;
+    const float rx = rinv[x];
+    const float gx = (1.0f / 72.0f) * (rho0 * rx - alpha);  // piece of x per unit p
+    const unsigned bmask = fl & FLAG_LINKS;
+    const unsigned zmask = solid ? (~bmask & 0x7FFFu) : 0u;
+    const unsigned amask = solid ? bmask : (unsigned)(m.ads ? m.ads_links[x] : 0);
+    const float cval = solid ? cB : cC;
+    if (!solid) c[0] = rx * (float)P[x] + 16.0f * gx + alpha;
+#pragma unroll
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (bmask >> q) & 1u;
+      const bool self_c = bnd && !solid;
+      const int y = nb.at(-CX(q), -CY(q), -CZ(q));
+      unsigned idx;
+      if (LAYOUT == SLBC_LAYOUT_N) {
+        idx = self_c ? OPP(q) * npad + (unsigned)x : q * npad + (unsigned)y;
+      } else if (LAYOUT == SLBC_LAYOUT_C0) {
+        idx = self_c ? q * npad + (unsigned)x : OPP(q) * npad + (unsigned)y;
+      } else {
+        idx = (bnd && solid) ? OPP(q) * npad + (unsigned)y : q * npad + (unsigned)x;
+      }
+      const float av = (float)P[idx];
+      const float W = q <= 6 ? 8.0f : 1.0f;
+      const float f = ((zmask >> q) & 1u) ? 0.0f : (((amask >> q) & 1u) ? cval : 1.0f);
+      if (self_c) {
+        float kq = rx * av + W * gx;
+        if (MOVING) {
+          float u[3];
+          const int o = m.objidx[y];
+          int yi = i - CX(q), yj = j - CY(q), yk = k - CZ(q);
+          yi = yi < 0 ? p.esi - 1 : (yi >= p.esi ? 0 : yi);
+          yj = yj < 0 ? p.esj - 1 : (yj >= p.esj ? 0 : yj);
+          yk = yk < 0 ? p.esk - 1 : (yk >= p.esk ? 0 : yk);
+          mp_wall_u<float>(m.objstate + 9 * o, yi, yj, yk, rho0, u);
+          kq += rx * mp_wall_term<float>(q, 1.0f, u);
+        }
+        c[0] += f * kq;
+      } else {
+        const float ry = rinv[y];
+        c[q] = f * (ry * av + W * (1.0f / 72.0f) * (rho0 * ry - alpha));
+      }
+    }
+    if (solid) c[0] += 1.0f;
+  }
+#pragma unroll
+  for (int q = 0; q < 15; q++) coef[q * npad + (unsigned)x] = c[q];
+}
+
 // Density snapshot (reference src/mpmisc.c:64-79), kept in FP64 and, when
 // FP32 tracers exist, in FP32.
 template <typename T>
