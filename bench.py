@@ -452,10 +452,10 @@ TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED = 0.35, 6.0, 12.0, 4
 TRACER_ALPHA, TRACER_ADPROB = 0.5, 0.01
 # bytes per tracer update: 15 FP32 populations + p in, rho, p out
 # bytes per tracer update on the frozen flow: FP32 tracers apply 15 FP32
-# stencil coefficients per node and read and write p (the coefficients are
-# built once from the flow); FP64 tracers read 15 FP32 populations, p and
-# rho (FP64) and write p
-TRACER_BYTES = {1: 60 + 2 * 4, 0: 60 + 3 * 8}
+# stencil coefficients per node and read and write p as two FP32 words
+# (high and low part; the coefficients are built once from the flow); FP64
+# tracers read 15 FP32 populations, p and rho (FP64) and write p
+TRACER_BYTES = {1: 60 + 4 * 4, 0: 60 + 3 * 8}
 
 
 def time_tracer(torch, L, lb, mp, steps):

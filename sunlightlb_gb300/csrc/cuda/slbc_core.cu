@@ -30,6 +30,11 @@ struct slbc_tracer {
   double *acc = nullptr;  // tracer added by fills since creation or the last reset
   double *objstate = nullptr;
   int objstate_cap = 0;
+  // FP32 tracers: the low part of p (p = hi + lo, |lo| <= half an FP32 ulp
+  // of hi) kept by the stencil update on a frozen flow, swapped with p and
+  // p2; lo_live says lo holds the low part (else it is taken as zero)
+  float *lo = nullptr, *lo2 = nullptr;
+  int lo_live = 0;
 };
 
 namespace {
@@ -219,7 +224,7 @@ __device__ __forceinline__ long long plane_node(long long e, int axis, int pos, 
 // layer can keep count of the tracer the fills have added.
 template <typename TP>
 __global__ void __launch_bounds__(kReduceThreads)
-k_mp_fill(TP *p, const uint16_t *flags, int esi, int esj, int esk, int kind, double g0, double g1,
+k_mp_fill(TP *p, float *lo, const uint16_t *flags, int esi, int esj, int esk, int kind, double g0, double g1,
           double g2, double g3, double g4, double g5, double value, long long count, double *partials) {
   double v[1] = {0.0};
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < count;
@@ -246,8 +251,9 @@ k_mp_fill(TP *p, const uint16_t *flags, int esi, int esj, int esk, int kind, dou
     }
     if (in) {
       const TP nv = (TP)value;
-      v[0] += (double)nv - (double)p[x];
+      v[0] += (double)nv - (double)p[x] - (lo ? (double)lo[x] : 0.0);
       p[x] = nv;
+      if (lo) lo[x] = 0.0f;
     }
   }
   block_sum<1>(v);
@@ -527,9 +533,22 @@ __global__ void k_mp_rinv(const double *rho64, float *rinv, long long n) {
 // nodes march along i with p of three planes (and halo) in shared memory,
 // the next plane prefetched into registers; the 15 coefficient loads per
 // node are the stream from memory.
+//
+// p is held as hi + lo (float-float) and the sum is formed with error-free
+// products and sums, so the update adds no rounding of its own beyond about
+// 2^-44 of p.  A plain FP32 sum stalls once the field is close to steady:
+// the remaining change of each node is below half an ulp, rounds away with
+// the same sign at every update, and tracer mass drains at a steady rate.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 __global__ void __launch_bounds__(kTileThreads, 4)
-k_mp_apply(const float *coef, const float *pin, float *pout, int esi, int esj, int esk, unsigned npad, int planes) {
-  __shared__ float ring[3][kPlane];
+k_mp_apply(const float *coef, const float *pin, const float *lin, float *pout, float *lout, int esi, int esj,
+           int esk, unsigned npad, int planes) {
+  __shared__ float2 ring[3][kPlane];
   const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
   const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
   const int np = min(planes, esi - i0);
@@ -545,14 +564,14 @@ k_mp_apply(const float *coef, const float *pin, float *pout, int esi, int esj, i
     const int base = wrap_index(i0 - 1 + h, esi) * plane_nodes;
 #pragma unroll
     for (int e = 0; e < kPlaneLoads; e++)
-      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = pin[base + off[e]];
+      if (off[e] >= 0) ring[h][tid + kTileThreads * e] = make_float2(pin[base + off[e]], lin[base + off[e]]);
   }
-  float pre[kPlaneLoads];
+  float2 pre[kPlaneLoads];
   auto prefetch = [&](int plane) {
     const int base = wrap_index(plane, esi) * plane_nodes;
 #pragma unroll
     for (int e = 0; e < kPlaneLoads; e++)
-      if (off[e] >= 0) pre[e] = pin[base + off[e]];
+      if (off[e] >= 0) pre[e] = make_float2(pin[base + off[e]], lin[base + off[e]]);
   };
   prefetch(i0 + 1);
   const int j = j0 + tj, k = k0 + tk;
@@ -569,20 +588,59 @@ k_mp_apply(const float *coef, const float *pin, float *pout, int esi, int esj, i
     __syncthreads();
     if (ii + 1 < np) prefetch(i + 2);
     if (!mine) continue;
-    const float *R[3] = {ring[sm], ring[s0], ring[sp]};
+    const float2 *R[3] = {ring[sm], ring[s0], ring[sp]};
     const unsigned x = (unsigned)(i * plane_nodes + own);
     float cq[15];
 #pragma unroll
     for (int q = 0; q < 15; q++) cq[q] = __ldcs(coef + q * npad + x);
-    float sum = cq[0] * R[1][c0];
+    float sh = 0.0f, sl = 0.0f;
 #pragma unroll
-    for (int q = 1; q < 15; q++) sum += cq[q] * R[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
-    pout[x] = sum;
+    for (int q = 0; q < 15; q++) {
+      const float2 v = q == 0 ? R[1][c0] : R[1 - CX(q)][c0 - CY(q) * kHaloK - CZ(q)];
+      const float ph = __fmul_rn(cq[q], v.x);
+      const float pe = __fmaf_rn(cq[q], v.x, -ph);  // exact error of the product
+      float s, e;
+      two_sum(sh, ph, s, e);
+      sh = s;
+      sl = __fadd_rn(sl, __fadd_rn(e, __fmaf_rn(cq[q], v.y, pe)));
+    }
+    const float hi = __fadd_rn(sh, sl);
+    pout[x] = hi;
+    lout[x] = __fsub_rn(sl, __fsub_rn(hi, sh));
   }
 }
 
-cudaError_t launch_mp_apply(Lattice &L, const float *pin, float *pout, dim3 grid, dim3 block, int planes) {
-  k_mp_apply<<<grid, block, 0, L.stream>>>(L.mp_coef, pin, pout, L.esi, L.esj, L.esk, (unsigned)L.npad, planes);
+// Tracer mass on a frozen flow: what a fluid node y sends to all receivers
+// (its column of the stencil: C_0(y) and C_q(y + c_q), q = 1..14) adds up to
+// rho(y)/rho(y) = 1 in exact arithmetic.  In FP32 the column misses 1 by the
+// rounding of 1/rho and of the terms, with the same sign at every update;
+// this pass adds the FP64 residual 1 - sum to C_0(y), so that the stencil
+// conserves mass to the rounding of C_0 alone.
+__global__ void k_mp_coef_norm(float *coef, const uint16_t *flags, int esi, int esj, int esk, unsigned npad) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)esi * esj * esk) return;
+  const int x = (int)e;
+  if (flags[x] & FLAG_SOLID) return;
+  int i, j, k;
+  decode(x, esj, esk, i, j, k);
+  const Nbr nb = make_nbr(i, j, k, esi, esj, esk);
+  double sum = coef[x];
+#pragma unroll
+  for (int q = 1; q < 15; q++) sum += (double)coef[q * npad + (unsigned)nb.at(CX(q), CY(q), CZ(q))];
+  coef[x] = (float)((double)coef[x] + (1.0 - sum));
+}
+
+cudaError_t launch_mp_coef_norm(Lattice &L) {
+  k_mp_coef_norm<<<(int)((L.nnodes + 255) / 256), 256, 0, L.stream>>>(L.mp_coef, L.flags, L.esi, L.esj, L.esk,
+                                                                      (unsigned)L.npad);
+  g_launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mp_apply(Lattice &L, const float *pin, const float *lin, float *pout, float *lout, dim3 grid,
+                            dim3 block, int planes) {
+  k_mp_apply<<<grid, block, 0, L.stream>>>(L.mp_coef, pin, lin, pout, lout, L.esi, L.esj, L.esk, (unsigned)L.npad,
+                                           planes);
   g_launches += 1;
   return cudaGetLastError();
 }
@@ -1110,6 +1168,8 @@ int slbc_mp_create(slbc_lattice *h, slbc_tracer **out, int use_f64) {
   if (e == cudaSuccess) e = cudaMalloc(&t->p2, (size_t)L.nnodes * es);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->p, 0, (size_t)L.nnodes * es, L.stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->p2, 0, (size_t)L.nnodes * es, L.stream);
+  if (e == cudaSuccess && !use_f64) e = cudaMalloc(&t->lo, (size_t)L.nnodes * sizeof(float));
+  if (e == cudaSuccess && !use_f64) e = cudaMalloc(&t->lo2, (size_t)L.nnodes * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&t->acc, sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(t->acc, 0, sizeof(double), L.stream);
   if (e == cudaSuccess && !L.mp_rho64) {
@@ -1144,6 +1204,8 @@ void slbc_mp_destroy(slbc_tracer *t) {
   if (t->p2) cudaFree(t->p2);
   if (t->acc) cudaFree(t->acc);
   if (t->objstate) cudaFree(t->objstate);
+  if (t->lo) cudaFree(t->lo);
+  if (t->lo2) cudaFree(t->lo2);
   delete t;
 }
 
@@ -1165,6 +1227,7 @@ int slbc_mp_get_rho(slbc_lattice *h, double *rho) {
 
 int slbc_mp_put(slbc_tracer *t, const double *p) {
   Lattice &L = t->h->L;
+  t->lo_live = 0;  // the uploaded values are the whole of p
   if (t->f64) {
     CK(cudaMemcpyAsync(t->p, p, (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice, L.stream));
   } else {
@@ -1213,8 +1276,10 @@ int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
       CK(cudaMemcpyAsync(t->objstate, objstate, 9 * (size_t)nobj * sizeof(double), cudaMemcpyHostToDevice, L.stream));
   }
   for (int s = 0; s < n; s++) {
-    CK(DISPATCH(L, launch_mp_step, L, t->p, t->p2, t->f64, alpha, adprob, moving, t->objstate));
+    CK(DISPATCH(L, launch_mp_step, L, t->p, t->p2, t->f64, alpha, adprob, moving, t->objstate, t->lo, t->lo2,
+                &t->lo_live));
     std::swap(t->p, t->p2);
+    std::swap(t->lo, t->lo2);
   }
   return 0;
 }
@@ -1276,9 +1341,9 @@ int slbc_mp_fill(slbc_tracer *t, int kind, const double *geo, double value) {
   const int nb = (int)std::max<long long>(1, std::min<long long>(blocks_for(count, kReduceThreads), 152 * 4));
   if (ensure_partials(L, nb + 8)) return 1;
   if (t->f64)
-    k_mp_fill<double><<<nb, kReduceThreads, 0, L.stream>>>((double *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
+    k_mp_fill<double><<<nb, kReduceThreads, 0, L.stream>>>((double *)t->p, nullptr, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
   else
-    k_mp_fill<float><<<nb, kReduceThreads, 0, L.stream>>>((float *)t->p, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
+    k_mp_fill<float><<<nb, kReduceThreads, 0, L.stream>>>((float *)t->p, t->lo_live ? t->lo : nullptr, L.flags, L.esi, L.esj, L.esk, kind, g[0], g[1], g[2], g[3], g[4], g[5], value, count, L.partials);
   count_launch();
   CK(cudaGetLastError());
   k_sum_into<<<1, 256, 0, L.stream>>>(L.partials, nb, t->acc);
@@ -1323,6 +1388,9 @@ int slbc_mp_plane(slbc_tracer *t, int axis, int pos, double out[2]) {
 static int mp_misc(slbc_tracer *t, const slbc_tracer *src, int op, double fac) {
   Lattice &L = t->h->L;
   if (op == 2 && src->f64 != t->f64) return fail_msg("slbc_mp_add: tracers differ in precision");
+  // other operations on p act on its high part alone; the low part is dropped
+  // (at most half an FP32 ulp per node, once)
+  t->lo_live = 0;
   if (t->f64)
     k_mp_misc<double><<<blocks_for(L.nnodes, 256), 256, 0, L.stream>>>((double *)t->p, src ? (const double *)src->p : nullptr, L.flags, L.ads, L.nnodes, op, fac);
   else

@@ -200,7 +200,8 @@ struct BatchState {
   cudaError_t launch_mp_rhoinit_##SUFFIX(Lattice &L);                           \
   cudaError_t launch_mp_step_##SUFFIX(Lattice &L, const void *p_in, void *p_out, \
                                       int tp_f64, double alpha, double adprob,  \
-                                      int moving, const double *objstate);
+                                      int moving, const double *objstate,       \
+                                      float *lo_in, float *lo_out, int *lo_live);
 
 SLBC_DECLARE_LAUNCHERS(f64)
 SLBC_DECLARE_LAUNCHERS(f32)
@@ -221,8 +222,11 @@ cudaError_t launch_mp_rhoinit_bf16(Lattice &L);
 // 1/rho of the density snapshot for FP32 tracers, rebuilt when stale
 // (slbc_core.cu)
 cudaError_t ensure_mp_rinv(Lattice &L);
+// column sums of the tracer stencil set to 1 (mass conservation)
+cudaError_t launch_mp_coef_norm(Lattice &L);
 // one FP32 tracer update from the lattice's stencil coefficients
-cudaError_t launch_mp_apply(Lattice &L, const float *pin, float *pout, dim3 grid, dim3 block, int planes);
+cudaError_t launch_mp_apply(Lattice &L, const float *pin, const float *lin, float *pout, float *lout, dim3 grid,
+                            dim3 block, int planes);
 
 // Launch bookkeeping and error text (defined in slbc_core.cu)
 void count_launch(int n = 1);

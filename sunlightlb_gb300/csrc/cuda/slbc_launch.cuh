@@ -288,7 +288,7 @@ cudaError_t SLBC_FN(launch_mp_rhoinit)(Lattice &L) {
 
 cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, int tp_f64,
                                     double alpha, double adprob, int moving,
-                                    const double *objstate) {
+                                    const double *objstate, float *lo_in, float *lo_out, int *lo_live) {
   // planes per block: the largest of 1..8 that still gives about four
   // blocks per SM
   const long long tiles = (long long)((L.esk + kTileK - 1) / kTileK) * ((L.esj + kTileJ - 1) / kTileJ);
@@ -337,14 +337,23 @@ cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, i
             default: k_mp_coef<T_, SLBC_LAYOUT_C1, false><<<nb, 256, 0, L.stream>>>(pa, m, ri, L.mp_coef); break;
           }
           count_launch();
-          const cudaError_t ce = cudaGetLastError();
+          cudaError_t ce = cudaGetLastError();
+          if (ce == cudaSuccess) ce = launch_mp_coef_norm(L);
           if (ce != cudaSuccess) return ce;
           memcpy(L.mp_coef_key, key, sizeof key);
           L.mp_coef_valid = true;
           ready = true;
         }
       }
-      if (ready) return launch_mp_apply(L, (const float *)p_in, (float *)p_out, grid, block, planes);
+      if (ready && lo_in && lo_out) {
+        // the low part of p is zero where the direct update or an upload left p
+        if (!*lo_live) {
+          const cudaError_t me = cudaMemsetAsync(lo_in, 0, (size_t)L.nnodes * sizeof(float), L.stream);
+          if (me != cudaSuccess) return me;
+        }
+        *lo_live = 1;
+        return launch_mp_apply(L, (const float *)p_in, lo_in, (float *)p_out, lo_out, grid, block, planes);
+      }
     }
     switch (L.layout * 2 + (moving ? 1 : 0)) {
       case SLBC_LAYOUT_N * 2: k_mp_step_f32<T_, SLBC_LAYOUT_N, false><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
@@ -354,6 +363,7 @@ cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, i
       case SLBC_LAYOUT_C1 * 2: k_mp_step_f32<T_, SLBC_LAYOUT_C1, false><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
       default: k_mp_step_f32<T_, SLBC_LAYOUT_C1, true><<<grid, block, 0, L.stream>>>(pa, m, ri, planes); break;
     }
+    if (lo_live) *lo_live = 0;  // p alone holds the tracer
     count_launch();
     return cudaGetLastError();
   }
@@ -376,6 +386,7 @@ cudaError_t SLBC_FN(launch_mp_step)(Lattice &L, const void *p_in, void *p_out, i
     k_mp_step<T_, double><<<grid, block, mp_bucket_bytes<double>(), L.stream>>>(pop_args(L), L.layout, m, planes);
   else
     k_mp_step<T_, float><<<grid, block, mp_bucket_bytes<float>(), L.stream>>>(pop_args(L), L.layout, m, planes);
+  if (lo_live) *lo_live = 0;  // p alone holds the tracer
   count_launch();
   return cudaGetLastError();
 }

@@ -178,8 +178,9 @@ def test_tracer_fp32_on_uploaded_flow(gpu, orc):
 
 
 def test_tracer_fp32_mass_balance_frozen_flow(gpu):
-    """FP32 tracer, flow frozen: fluid + adsorbed tracer conserved to 1e-5
-    over 200 updates."""
+    """FP32 tracer, flow frozen (stencil update, columns normalised to 1,
+    compensated accumulation on adsorbing solids): fluid + adsorbed tracer
+    conserved to 2e-6 over 200 updates."""
     for P in (1.0, 0.01):
         lb, mp = tracer_run(gpu, ads=1, adprob=P, steps=0, interleave=False, precision=1, mp_precision=1)
         gpu.mpall(mp, 1.0)
@@ -187,4 +188,4 @@ def test_tracer_fp32_mass_balance_frozen_flow(gpu):
         for _ in range(200):
             gpu.mpstep(mp)
         m1 = gpu.mptotal(mp, "fluid") + gpu.mptotal(mp, "adsorbed")
-        assert abs(m1 - m0) <= 1e-5 * m0, (P, m0, m1)
+        assert abs(m1 - m0) <= 2e-6 * m0, (P, m0, m1)
