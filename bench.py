@@ -368,7 +368,8 @@ def run_e2e(L, precision, spheres, solid, args):
         L.measure(lb)
         _ = (lb.vmeanx, lb.step)
         d2h += 5 * 8 * 3 + 6 * 8  # three mean-flow sums and the object force/torque
-    pops = lb.pops()
+    L.lbpull(lb)  # populations into the host buffer lb->a (FP64, reference order)
+    pops = lb.array("a")
     d2h += pops.nbytes
     dt = time.perf_counter() - t0
     steps = intervals * CHECK

@@ -222,16 +222,33 @@ static void upload_geometry(LBSys lb) {
   count = (int *)xcalloc(nobj + 1, sizeof(int));
   start = (int *)xcalloc(nobj + 1, sizeof(int));
   tmp_node = (long *)xcalloc(n, sizeof(long));
-  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
-    x = slb_node(lb, i, j, k);
-    if (objidx[x] < 0) continue;
-    for (q = 1; q < 15; q++) {
-      int ii = (i + LINKS[q][0] + lb->esi) % lb->esi;
-      int jj = (j + LINKS[q][1] + lb->esj) % lb->esj;
-      int kk = (k + LINKS[q][2] + lb->esk) % lb->esk;
-      if (lb->obj[slb_node(lb, ii, jj, kk)] == NULL) break;
+  {
+    /* away from the faces a neighbour is x + off[q]; on the faces the
+     * coordinates wrap (every side >= 1, links move by at most 1) */
+    const int ei = lb->esi, ej = lb->esj, ek = lb->esk;
+    long off[15];
+    for (q = 0; q < 15; q++) off[q] = ((long)LINKS[q][0] * ej + LINKS[q][1]) * ek + LINKS[q][2];
+    for (i = 0; i < ei; i++) for (j = 0; j < ej; j++) {
+      const int inner_ij = i > 0 && i < ei - 1 && j > 0 && j < ej - 1;
+      const long row = slb_node(lb, i, j, 0);
+      for (k = 0; k < ek; k++) {
+        x = row + k;
+        if (objidx[x] < 0) continue;
+        if (inner_ij && k > 0 && k < ek - 1) {
+          for (q = 1; q < 15; q++)
+            if (objidx[x + off[q]] < 0) break;
+        } else {
+          for (q = 1; q < 15; q++) {
+            int ii = i + LINKS[q][0], jj = j + LINKS[q][1], kk = k + LINKS[q][2];
+            ii = ii < 0 ? ii + ei : (ii >= ei ? ii - ei : ii);
+            jj = jj < 0 ? jj + ej : (jj >= ej ? jj - ej : jj);
+            kk = kk < 0 ? kk + ek : (kk >= ek ? kk - ek : kk);
+            if (objidx[slb_node(lb, ii, jj, kk)] < 0) break;
+          }
+        }
+        if (q < 15) { tmp_node[nb++] = x; count[objidx[x]]++; }
+      }
     }
-    if (q < 15) { tmp_node[nb++] = x; count[objidx[x]]++; }
   }
   for (o = 1; o <= nobj; o++) start[o] = start[o - 1] + count[o - 1];
   free(st->bnd_node); free(st->bnd_obj);

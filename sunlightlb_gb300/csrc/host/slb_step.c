@@ -278,7 +278,11 @@ void distribf(LBSys lb) {
 void measure(LBSys lb) {
   int fused = lb->status == POST_COLLIDE;
   if (!fused) out_of_position(lb, "Measurements");
-  zeroforce(lb);
+  /* zeroforce on the device only: the force steps below change the node
+   * forces at once, so the host arrays are refreshed by lbpull on demand */
+  slb_check(slbc_zero_force(slb_device(lb)), "force reset");
+  slb_forces_changed(lb);
+  slb_trace(lb, "zeroforce");
   lb->vmeanx = lb->vmeany = lb->vmeanz = 0.0;
   accvmean(lb, 0.25);
   if (fused) fused_step(lb, 1); else { bblforce(lb); propagate(lb); collide(lb); }
