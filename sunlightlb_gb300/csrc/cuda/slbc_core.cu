@@ -1495,7 +1495,7 @@ int slbc_batch_step(slbc_batch *b, int nsteps) {
       cudaGraphDestroy(g);
       if (ie != cudaSuccess) return fail("slbc_batch_step: cudaGraphInstantiate", ie);
       int nclass = 0;
-      for (int c = 0; c < 4; c++) nclass += B.class_tiles[c] > 0;
+      for (int c = 0; c < 4; c++) nclass += (B.class_tiles[c][0] > 0) + (B.class_tiles[c][1] > 0);
       count_launch(-G * nclass);  // the captured launches run only in the replays
       for (; done + G <= nsteps; done += G) {
         const cudaError_t le = cudaGraphLaunch(ge, B.stream);

@@ -171,7 +171,9 @@ struct BatchState {
   int *work_off = nullptr, *work = nullptr;  // persistent: lattices of each block (CSR)
   int2 *tiles = nullptr;            // tiles: (lattice, first cell), grouped by class
   long long tiles_cap = 0;
-  int class_tiles[4] = {0, 0, 0, 0};
+  // tiles per (class, starting parity): class = 2 * moving + uniform force,
+  // group g holds the domains whose first step has parity g (odd0 = g)
+  int class_tiles[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
 };

@@ -298,13 +298,14 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchDom<T> *d
 
 // Packed cell index of a batch: every domain is cut into tiles of
 // kBatchTile consecutive cells, tile t = (domain, first cell).  One launch
-// updates every tile of one (moving walls, uniform force) class by one step;
-// a domain's parity follows its first-step parity odd0 and the step number.
+// updates the tiles of one (moving walls, uniform force, parity) group by
+// one step: the host groups each class's tiles by the parity of their
+// domain's first step, so one launch has one parity (ODD) and carries the
+// code of that parity only (64 registers, four blocks per SM).
 constexpr int kBatchTile = 256;
 
-template <typename T, bool EXACT, bool MOVING, bool BFU>
-__global__ void __launch_bounds__(kBatchTile) k_batch_tiles(const BatchDom<T> *doms, const int2 *tiles,
-                                                            int step) {
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+__global__ void __launch_bounds__(kBatchTile, 4) k_batch_tiles(const BatchDom<T> *doms, const int2 *tiles) {
   __shared__ BatchDom<T> dom;
   const int2 tile = tiles[blockIdx.x];
   if (threadIdx.x == 0) dom = doms[tile.x];
@@ -314,8 +315,7 @@ __global__ void __launch_bounds__(kBatchTile) k_batch_tiles(const BatchDom<T> *d
   const int e = tile.y + threadIdx.x;
   if (e >= a.p.esi * esj * esk) return;
   const int r = e / esk;
-  if (((step + dom.odd0) & 1) == 1) step_node<T, true, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
-  else step_node<T, false, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
+  step_node<T, ODD, EXACT, MOVING, BFU>(a, r / esj, r % esj, e - r * esk);
 }
 
 // Explicitly rounded add / multiply: never contracted into FMA, so the

@@ -138,12 +138,14 @@ cudaError_t SLBC_FN(prepare_tiles)(BatchState &B) {
     h[d].odd0 = B.lats[d]->layout == SLBC_LAYOUT_C0 ? 1 : 0;
   }
   for (int c = 0; c < 4; c++) {
-    const size_t first = tiles.size();
-    for (int d = 0; d < n; d++) {
-      if ((h[d].a.moving ? 2 : 0) + (h[d].a.bf_uniform ? 1 : 0) != c) continue;
-      for (long long e = 0; e < B.lats[d]->nnodes; e += kBatchTile) tiles.push_back(make_int2(d, (int)e));
+    for (int g = 0; g < 2; g++) {
+      const size_t first = tiles.size();
+      for (int d = 0; d < n; d++) {
+        if ((h[d].a.moving ? 2 : 0) + (h[d].a.bf_uniform ? 1 : 0) != c || h[d].odd0 != g) continue;
+        for (long long e = 0; e < B.lats[d]->nnodes; e += kBatchTile) tiles.push_back(make_int2(d, (int)e));
+      }
+      B.class_tiles[c][g] = (int)(tiles.size() - first);
     }
-    B.class_tiles[c] = (int)(tiles.size() - first);
   }
   cudaError_t e = cudaMemcpy(B.doms, h.data(), n * sizeof(BatchDom<T_>), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return e;
@@ -163,18 +165,26 @@ cudaError_t SLBC_FN(launch_tiles)(BatchState &B, int step) {
   const BatchDom<T_> *D = (const BatchDom<T_> *)B.doms;
   const int2 *t = B.tiles;
   for (int c = 0; c < 4; c++) {
-    const int nt = B.class_tiles[c];
-    if (nt == 0) continue;
-    switch (c) {
-      case 0: k_batch_tiles<T_, SLBC_EXACT, false, false><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
-      case 1: k_batch_tiles<T_, SLBC_EXACT, false, true><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
-      case 2: k_batch_tiles<T_, SLBC_EXACT, true, false><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
-      default: k_batch_tiles<T_, SLBC_EXACT, true, true><<<nt, kBatchTile, 0, B.stream>>>(D, t, step); break;
+    for (int g = 0; g < 2; g++) {
+      const int nt = B.class_tiles[c][g];
+      if (nt == 0) continue;
+      // domains of group g take an odd step when (step + g) is odd
+      const bool odd = ((step + g) & 1) == 1;
+      switch (c * 2 + (odd ? 1 : 0)) {
+        case 0: k_batch_tiles<T_, false, SLBC_EXACT, false, false><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 1: k_batch_tiles<T_, true, SLBC_EXACT, false, false><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 2: k_batch_tiles<T_, false, SLBC_EXACT, false, true><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 3: k_batch_tiles<T_, true, SLBC_EXACT, false, true><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 4: k_batch_tiles<T_, false, SLBC_EXACT, true, false><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 5: k_batch_tiles<T_, true, SLBC_EXACT, true, false><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        case 6: k_batch_tiles<T_, false, SLBC_EXACT, true, true><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+        default: k_batch_tiles<T_, true, SLBC_EXACT, true, true><<<nt, kBatchTile, 0, B.stream>>>(D, t); break;
+      }
+      count_launch();
+      t += nt;
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
     }
-    count_launch();
-    t += nt;
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
