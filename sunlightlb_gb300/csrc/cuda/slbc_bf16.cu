@@ -100,36 +100,43 @@ __device__ __forceinline__ float bf_post(const PairArgs &a, int q, long long x) 
   return eq_pop(q, a.Min[x]) + pair_dev(a.Pin[x], pair_of(q)) * a.inv;
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-               "l"(gmem)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-               "l"(gmem)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-constexpr int kPairSlots = 4;  // planes i-1, i, i+1 in use, i+2 arriving
+// The 15 post-collision populations of a node from its state (the same
+// operations as eq_pop, so that every kernel reconstructs the same values).
+__device__ __forceinline__ void decode_state(float4 m, uint4 v, float inv, float (&a)[15]) {
+  const float rhobyb = m.x * (1.0f / 72.0f);
+  const float erhobyb = 8.0f * rhobyb;
+  const float d0 = __uint_as_float(v.x << 16) * inv, d1 = __uint_as_float(v.x & 0xffff0000u) * inv;
+  const float d2 = __uint_as_float(v.y << 16) * inv, d3 = __uint_as_float(v.y & 0xffff0000u) * inv;
+  const float d4 = __uint_as_float(v.z << 16) * inv, d5 = __uint_as_float(v.z & 0xffff0000u) * inv;
+  const float d6 = __uint_as_float(v.w << 16) * inv, d7 = __uint_as_float(v.w & 0xffff0000u) * inv;
+  a[0] = 2.0f * erhobyb + d0;
+  a[1] = (erhobyb + (8.0f / 24.0f) * m.y) + d1;
+  a[2] = (erhobyb - (8.0f / 24.0f) * m.y) + d1;
+  a[3] = (erhobyb + (8.0f / 24.0f) * m.z) + d2;
+  a[4] = (erhobyb - (8.0f / 24.0f) * m.z) + d2;
+  a[5] = (erhobyb + (8.0f / 24.0f) * m.w) + d3;
+  a[6] = (erhobyb - (8.0f / 24.0f) * m.w) + d3;
+#pragma unroll
+  for (int q = 7; q < 15; q++) a[q] = eq_pop(q, m) + (q == 7 || q == 14 ? d4 : q == 8 || q == 13 ? d5
+                                                           : q == 9 || q == 12 ? d6 : d7);
+}
+
+constexpr int kPairSlots = 3;  // decoded planes i-1, i, i+1
+constexpr int kPairSmem = kPairSlots * 15 * kPlane * (int)sizeof(float);
 
 // The fused update of k_step (same pull rule) on paired-deviation storage.
 // A block of 32 (k) x 8 (j) threads marches along i over `planes` planes.
-// The state (moments and deviations) of four consecutive planes, with a
-// one-node halo, sits in shared memory: the three a node gathers from and
-// the next one, copied in by cp.async while the current plane is updated.
-// Every value a node gathers comes from shared memory; global memory sees
-// one load of each state vector per node (plus the halo) and one store of
-// each.  Nodes are independent, so there is one barrier per plane.  The
-// deviations sit word-major in the ring (word w = pairs 2w, 2w+1 of every
-// node in a row), so a warp gathering one pair from 32 neighbours reads
-// 32 consecutive words, free of bank conflicts.
+// The populations of three consecutive planes, with a one-node halo, sit
+// decoded (FP32, 15 per node, direction-major) in shared memory; the state
+// of the plane after them is loaded into registers one plane ahead and
+// decoded into the ring when its slot frees up.  A node gathers each of its
+// 15 populations with one 4-byte shared load whose address the bounce-back
+// bit selects (upstream node y = x - c_q, direction q; or x itself,
+// direction opp(q)), and writes its new state with two 16-byte stores.
 template <bool MOVING, bool BFU>
-__global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepArgs<float> s, int planes) {
-  __shared__ float4 ringM[kPairSlots][kPlane];
-  __shared__ uint32_t ringW[kPairSlots][4][kPlane];
+__global__ void __launch_bounds__(kTileThreads, 3) k_step_pair(PairArgs a, StepArgs<float> s, int planes) {
+  extern __shared__ __align__(16) float dec[];  // [slot][q][kPlane]
   const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * kTileK + tk;
   const int k0 = blockIdx.x * kTileK, j0 = blockIdx.y * kTileJ, i0 = blockIdx.z * planes;
   const int np = min(planes, a.esi - i0);
@@ -142,23 +149,31 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepA
     off[e] = c < kPlane ? wrap_index(j0 - 1 + c / kHaloK, a.esj) * a.esk + wrap_index(k0 - 1 + c % kHaloK, a.esk)
                         : -1;
   }
-  // plane p goes to ring slot (p - i0 + 1) % kPairSlots
-  auto fetch = [&](int plane, int slot) {
+  float4 pm[kPlaneLoads];
+  uint4 pp[kPlaneLoads];
+  auto prefetch = [&](int plane) {
     const long long base = (long long)wrap_index(plane, a.esi) * plane_nodes;
+#pragma unroll
+    for (int e = 0; e < kPlaneLoads; e++)
+      if (off[e] >= 0) { pm[e] = __ldcs(a.Min + base + off[e]); pp[e] = __ldcs(a.Pin + base + off[e]); }
+  };
+  auto decode_into = [&](int slot) {
 #pragma unroll
     for (int e = 0; e < kPlaneLoads; e++) {
       if (off[e] < 0) continue;
+      float v[15];
+      decode_state(pm[e], pp[e], a.inv, v);
       const int c = tid + kTileThreads * e;
-      cp_async16(&ringM[slot][c], a.Min + base + off[e]);
-      const uint32_t *w = reinterpret_cast<const uint32_t *>(a.Pin + base + off[e]);
 #pragma unroll
-      for (int h = 0; h < 4; h++) cp_async4(&ringW[slot][h][c], w + h);
+      for (int q = 0; q < 15; q++) dec[(slot * 15 + q) * kPlane + c] = v[q];
     }
-    cp_async_commit();
   };
-  fetch(i0 - 1, 0);
-  fetch(i0, 1);
-  fetch(i0 + 1, 2);
+  // plane p sits in ring slot (p - i0 + 1) % 3
+  prefetch(i0 - 1);
+  decode_into(0);
+  prefetch(i0);
+  decode_into(1);
+  prefetch(i0 + 1);
   const int j = j0 + tj, k = k0 + tk;
   const bool mine = j < a.esj && k < a.esk;
   const int own = mine ? j * a.esk + k : 0;
@@ -168,34 +183,25 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_step_pair(PairArgs a, StepA
     const int i = i0 + ii;
     const uint16_t fl = fl_next;
     if (ii + 1 < np) fl_next = __ldg(a.flags + (long long)(i + 1) * plane_nodes + own);
-    cp_async_wait_all();
-    __syncthreads();  // plane i+1 has arrived; slot of plane i-2 is free
-    if (ii + 1 < np) fetch(i + 2, (ii + 3) % kPairSlots);
+    __syncthreads();  // the slot of plane i-2 was last read in the previous iteration
+    decode_into((ii + 2) % kPairSlots);
+    __syncthreads();
+    if (ii + 1 < np) prefetch(i + 2);
     if (!mine) continue;
-    const int s0 = ii % kPairSlots, s1 = (ii + 1) % kPairSlots, s2 = (ii + 2) % kPairSlots;
-    const float4 *RM[3] = {ringM[s0], ringM[s1], ringM[s2]};
-    const uint32_t(*RW[3])[kPlane] = {ringW[s0], ringW[s1], ringW[s2]};
+    const float *D[3] = {dec + (ii % kPairSlots) * 15 * kPlane, dec + ((ii + 1) % kPairSlots) * 15 * kPlane,
+                         dec + ((ii + 2) % kPairSlots) * 15 * kPlane};
     const int x = i * plane_nodes + own;
     const bool solid = (fl & FLAG_SOLID) != 0;
-    const float4 mx = RM[1][c0];
-    const uint4 px = make_uint4(RW[1][0][c0], RW[1][1][c0], RW[1][2][c0], RW[1][3][c0]);
-    // A bounce-back link (bit q) returns the node's own post-collision
-    // opp(q): eq_opp(q)(m) is eq_q of m with the momentum negated (exact:
-    // only signs change) and the deviation is that of the same pair.
-    // Otherwise the population was produced by y = x - c_q.
-    const float4 mneg = make_float4(mx.x, -mx.y, -mx.z, -mx.w);
     float t[15];
-    t[0] = eq_pop(0, mx) + pair_dev(px, 0) * a.inv;
+    t[0] = D[1][c0];
 #pragma unroll
     for (int q = 1; q < 15; q++) {
+      // over a bounce-back link the node's own post-collision opp(q) comes
+      // back; otherwise the population q of y = x - c_q arrives
       const bool bnd = (fl >> q) & 1;
-      const int c = c0 - CY(q) * kHaloK - CZ(q);
-      const float4 my = RM[1 - CX(q)][c];
-      const uint32_t wy = RW[1 - CX(q)][pair_of(q) >> 1][c];
-      const float dy = (pair_of(q) & 1) ? __uint_as_float(wy & 0xffff0000u) : __uint_as_float(wy << 16);
-      const float4 m = bnd ? mneg : my;
-      const float d = bnd ? pair_dev(px, pair_of(q)) : dy;
-      t[q] = eq_pop(q, m) + d * a.inv;
+      const float *src = bnd ? D[1] + OPP(q) * kPlane + c0
+                             : D[1 - CX(q)] + q * kPlane + (c0 - CY(q) * kHaloK - CZ(q));
+      t[q] = *src;
     }
     if (MOVING && (fl & FLAG_LINKS)) {
       const Nbr nb = make_nbr(i, j, k, a.esi, a.esj, a.esk);
@@ -431,12 +437,27 @@ cudaError_t launch_pair_step(Lattice &L, int planes) {
   const dim3 b(kTileK, kTileJ);
   const PairArgs a = pair_args(L);
   const StepArgs<float> s = step_args_f(L);
+  // the decoded ring needs more than the default 48 KB of dynamic shared
+  // memory: opt in once per device
+  static unsigned long long attr_set = 0;  // bit = device index
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (!(attr_set >> (dev & 63) & 1ull)) {
+    const void *fns[4] = {(const void *)k_step_pair<true, true>, (const void *)k_step_pair<true, false>,
+                          (const void *)k_step_pair<false, true>, (const void *)k_step_pair<false, false>};
+    for (const void *f : fns) {
+      e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kPairSmem);
+      if (e != cudaSuccess) return e;
+    }
+    attr_set |= 1ull << (dev & 63);
+  }
   if (s.moving) {
-    if (s.bf_uniform) k_step_pair<true, true><<<g, b, 0, L.stream>>>(a, s, planes);
-    else k_step_pair<true, false><<<g, b, 0, L.stream>>>(a, s, planes);
+    if (s.bf_uniform) k_step_pair<true, true><<<g, b, kPairSmem, L.stream>>>(a, s, planes);
+    else k_step_pair<true, false><<<g, b, kPairSmem, L.stream>>>(a, s, planes);
   } else {
-    if (s.bf_uniform) k_step_pair<false, true><<<g, b, 0, L.stream>>>(a, s, planes);
-    else k_step_pair<false, false><<<g, b, 0, L.stream>>>(a, s, planes);
+    if (s.bf_uniform) k_step_pair<false, true><<<g, b, kPairSmem, L.stream>>>(a, s, planes);
+    else k_step_pair<false, false><<<g, b, kPairSmem, L.stream>>>(a, s, planes);
   }
   count_launch();
   return cudaGetLastError();
