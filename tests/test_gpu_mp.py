@@ -189,3 +189,18 @@ def test_tracer_fp32_mass_balance_frozen_flow(gpu):
             gpu.mpstep(mp)
         m1 = gpu.mptotal(mp, "fluid") + gpu.mptotal(mp, "adsorbed")
         assert abs(m1 - m0) <= 2e-6 * m0, (P, m0, m1)
+
+
+def test_tracer_fp32_stencil_tracks_fp64(gpu, orc):
+    """Frozen flow, 200 FP32 updates (the stencil path from the second
+    update on: FP32 coefficients, field kept as high + low parts) against
+    the FP64 oracle: within 1e-6 of the largest value, with partial
+    adsorption."""
+    out = []
+    for L, prec, mpp in ((gpu, 1, 1), (orc, 0, None)):
+        lb, mp = tracer_run(L, precision=prec, mp_precision=mpp, steps=0, interleave=False, ads=1, adprob=0.37)
+        for _ in range(200):
+            L.mpstep(mp)
+        L.mppull(mp)
+        out.append(mp.field().copy())
+    assert np.abs(out[0] - out[1]).max() <= 1e-6 * np.abs(out[1]).max()
