@@ -195,8 +195,10 @@ def tuning(L, lb):
     import ctypes
     cfg = (ctypes.c_int * 4)()
     state = L.lbtuning(lb, ctypes.addressof(cfg))
-    return {"state": {1: "tuned", -1: "default", 0: "none"}.get(state, state),
-            "even": {"rows_per_thread": cfg[0], "threads_k": cfg[1]},
+    st = {1: "tuned", -1: "default", 0: "none"}.get(state, state)
+    if lb.precision == 2:  # one update kernel: planes per block (32 x 8 threads)
+        return {"state": st, "planes_per_block": cfg[0]}
+    return {"state": st, "even": {"rows_per_thread": cfg[0], "threads_k": cfg[1]},
             "odd": {"rows_per_thread": cfg[2], "threads_k": cfg[3]}}
 
 

@@ -420,13 +420,13 @@ int autotune_time(Lattice &L) {
   static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
   const bool bf = L.precision == 2;
   // BF16: powers of two, and the plane counts that fill one or two waves of
-  // four blocks per SM evenly
+  // three blocks per SM evenly
   int cand_bf[7][2] = {{1, 32}, {2, 32}, {4, 32}, {8, 32}, {16, 32}, {0, 32}, {0, 32}};
   int nbf = 5;
   {
     const long long tiles = (long long)((L.esk + kTileK - 1) / kTileK) * ((L.esj + kTileJ - 1) / kTileJ);
     for (int w = 1; w <= 2; w++) {
-      const long long chunks = std::max<long long>(1, (w * 152LL * 4 + tiles - 1) / tiles);
+      const long long chunks = std::max<long long>(1, (w * 152LL * 3 + tiles - 1) / tiles);
       const int planes = (int)std::min<long long>(64, (L.esi + chunks - 1) / chunks);
       bool dup = false;
       for (int c = 0; c < nbf; c++) dup = dup || cand_bf[c][0] == planes;
