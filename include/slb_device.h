@@ -76,6 +76,13 @@ int slbc_synchronize(slbc_lattice *h);
  * src/lbobjs.c:526-560, 660-663. */
 int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj,
                       const long *bnd_node, const int *bnd_obj, long nbnd);
+/* The same with the boundary list built on the GPU from the flag words
+ * (solid nodes with a fluid neighbour, grouped by object, node order kept
+ * within an object); the list is returned in *bnd_node / *bnd_obj (malloc'ed,
+ * the caller frees them) with its length in *nbnd.  Replaces the device side
+ * of makemask/syncobjs like slbc_set_geometry. */
+int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj,
+                           long **bnd_node, int **bnd_obj, long *nbnd);
 /* Adsorption bits (0x4000 of the reference mask) of every node, 1 byte per
  * node (reference src/mpads.c:28-44). */
 int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads);

@@ -91,6 +91,56 @@ __global__ void k_flags(const int *objidx, uint16_t *flags, int esi, int esj, in
   flags[x] = f;
 }
 
+// Solid boundary nodes (a solid node with at least one boundary link, i.e. a
+// fluid neighbour), compacted in node order.  Block b covers the nodes
+// [b * kBndChunk, (b + 1) * kBndChunk): k_bnd_count counts them, the host
+// turns the counts into offsets, and k_bnd_write writes each block's nodes
+// in order (warp ballots and a running block offset).
+constexpr int kBndChunk = 4096;
+
+__device__ __forceinline__ bool boundary_solid(uint16_t f) { return (f & FLAG_SOLID) && (f & FLAG_LINKS); }
+
+__global__ void __launch_bounds__(256) k_bnd_count(const uint16_t *flags, long long n, int *counts) {
+  __shared__ int total;
+  if (threadIdx.x == 0) total = 0;
+  __syncthreads();
+  const long long lo = (long long)blockIdx.x * kBndChunk;
+  const long long hi = lo + kBndChunk < n ? lo + kBndChunk : n;
+  int c = 0;
+  for (long long x = lo + threadIdx.x; x < hi; x += blockDim.x) c += boundary_solid(flags[x]);
+  atomicAdd(&total, c);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(256) k_bnd_write(const uint16_t *flags, long long n, const int *offsets,
+                                                   int *out) {
+  __shared__ int warp_sum[8];
+  __shared__ int base;
+  if (threadIdx.x == 0) base = offsets[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long lo = (long long)blockIdx.x * kBndChunk;
+  const long long hi = lo + kBndChunk < n ? lo + kBndChunk : n;
+  for (long long r = lo; r < hi; r += 256) {
+    const long long x = r + threadIdx.x;
+    const bool p = x < hi && boundary_solid(flags[x]);
+    const unsigned m = __ballot_sync(0xffffffffu, p);
+    if (lane == 0) warp_sum[w] = __popc(m);
+    __syncthreads();
+    int off = base;
+    for (int v = 0; v < w; v++) off += warp_sum[v];
+    if (p) out[off + __popc(m & ((1u << lane) - 1u))] = (int)x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int v = 0; v < 8; v++) t += warp_sum[v];
+      base += t;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_scale(double *v, long long n, double fac) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e < n) v[e] *= fac;
@@ -776,21 +826,23 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
   return 0;
 }
 
-int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *bnd_node,
-                      const int *bnd_obj, long nbnd) {
-  Lattice &L = h->L;
+// object map and flag words
+static int geometry_flags(Lattice &L, slbc_lattice *h, const int *objidx) {
   L.ads_version++;  // the boundary links change
   const long long n = L.nnodes;
   for (long long x = 0; x < n; x++) h->solid_host[x] = objidx[x] >= 0;
   CK(cudaMemcpyAsync(L.objidx, objidx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, L.stream));
-  {
-    const int bx = L.esk >= 128 ? 128 : 32;
-    dim3 grid((L.esk + bx - 1) / bx, L.esj, L.esi);
-    k_flags<<<grid, bx, 0, L.stream>>>(L.objidx, L.flags, L.esi, L.esj, L.esk);
-    count_launch();
-    CK(cudaGetLastError());
-  }
-  // boundary list
+  const int bx = L.esk >= 128 ? 128 : 32;
+  dim3 grid((L.esk + bx - 1) / bx, L.esj, L.esi);
+  k_flags<<<grid, bx, 0, L.stream>>>(L.objidx, L.flags, L.esi, L.esj, L.esk);
+  count_launch();
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// boundary list (sorted by object, node order within an object), node
+// forces and the distribf pieces
+static int geometry_boundary(Lattice &L, int nobj, const long *bnd_node, const int *bnd_obj, long nbnd) {
   void *old[] = {L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj, L.piece_lo, L.piece_hi,
                  L.piece_sum, L.obj_pos, L.obj_ft};
   CK(cudaStreamSynchronize(L.stream));
@@ -841,6 +893,64 @@ int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *
     }
   }
   L.generation++;
+  return 0;
+}
+
+int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *bnd_node,
+                      const int *bnd_obj, long nbnd) {
+  Lattice &L = h->L;
+  if (geometry_flags(L, h, objidx)) return 1;
+  return geometry_boundary(L, nobj, bnd_node, bnd_obj, nbnd);
+}
+
+int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj, long **bnd_node_out,
+                           int **bnd_obj_out, long *nbnd_out) {
+  Lattice &L = h->L;
+  *bnd_node_out = nullptr; *bnd_obj_out = nullptr; *nbnd_out = 0;
+  if (geometry_flags(L, h, objidx)) return 1;
+  // boundary nodes in node order, found on the GPU from the flag words
+  const int nb = (int)((L.nnodes + kBndChunk - 1) / kBndChunk);
+  int *counts = nullptr, *list = nullptr;
+  CK(cudaMalloc(&counts, (size_t)nb * sizeof(int)));
+  k_bnd_count<<<nb, 256, 0, L.stream>>>(L.flags, L.nnodes, counts);
+  count_launch();
+  std::vector<int> off((size_t)nb);
+  cudaError_t e = cudaMemcpyAsync(off.data(), counts, (size_t)nb * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  long total = 0;
+  for (int b = 0; b < nb && e == cudaSuccess; b++) {
+    const int c = off[b];
+    off[b] = (int)total;
+    total += c;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts, off.data(), (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, L.stream);
+  if (e == cudaSuccess && total > 0) e = cudaMalloc(&list, (size_t)total * sizeof(int));
+  std::vector<int> nodes((size_t)total);
+  if (e == cudaSuccess && total > 0) {
+    k_bnd_write<<<nb, 256, 0, L.stream>>>(L.flags, L.nnodes, counts, list);
+    count_launch();
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nodes.data(), list, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  }
+  cudaFree(counts);
+  if (list) cudaFree(list);
+  if (e != cudaSuccess) return fail("slbc_set_geometry_auto", e);
+  // grouped by object, node order kept (a counting sort over the list)
+  long *bn = (long *)malloc((size_t)(total > 0 ? total : 1) * sizeof(long));
+  int *bo = (int *)malloc((size_t)(total > 0 ? total : 1) * sizeof(int));
+  if (!bn || !bo) { free(bn); free(bo); return fail_msg("slbc_set_geometry_auto: no host memory"); }
+  std::vector<long> start((size_t)nobj + 1, 0);
+  for (long t = 0; t < total; t++) start[(size_t)objidx[nodes[t]] + 1]++;
+  for (int o = 0; o < nobj; o++) start[(size_t)o + 1] += start[o];
+  for (long t = 0; t < total; t++) {
+    const int o = objidx[nodes[t]];
+    const long slot = start[o]++;
+    bn[slot] = nodes[t];
+    bo[slot] = o;
+  }
+  if (geometry_boundary(L, nobj, bn, bo, total)) { free(bn); free(bo); return 1; }
+  *bnd_node_out = bn; *bnd_obj_out = bo; *nbnd_out = total;
   return 0;
 }
 

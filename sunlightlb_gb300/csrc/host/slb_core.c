@@ -178,11 +178,9 @@ static int objmap_get(objmap_t *m, LBObj p, int *next, LBObj **objs, int *cap) {
 static void upload_geometry(LBSys lb) {
   slb_priv *st = slb_state(lb);
   long n = lb->nnodes, x, nb = 0;
-  int i, j, k, q, o, nobj = 0, cap = 16;
+  int nobj = 0, cap = 16;
   int *objidx = (int *)xcalloc(n, sizeof(int));
   LBObj *objs = (LBObj *)xcalloc(cap, sizeof(LBObj));
-  int *count, *start;
-  long *tmp_node;
   objmap_t m;
   /* dense index of every object the map references, in first-seen order */
   m.cap = 64;
@@ -218,54 +216,16 @@ static void upload_geometry(LBSys lb) {
     objidx[x] = objmap_get(&m, p, &nobj, &objs, &cap);
   }
   free(m.key); free(m.val);
-  /* solid nodes with a fluid neighbour, grouped by object, node order kept */
-  count = (int *)xcalloc(nobj + 1, sizeof(int));
-  start = (int *)xcalloc(nobj + 1, sizeof(int));
-  tmp_node = (long *)xcalloc(n, sizeof(long));
-  {
-    /* away from the faces a neighbour is x + off[q]; on the faces the
-     * coordinates wrap (every side >= 1, links move by at most 1) */
-    const int ei = lb->esi, ej = lb->esj, ek = lb->esk;
-    long off[15];
-    for (q = 0; q < 15; q++) off[q] = ((long)LINKS[q][0] * ej + LINKS[q][1]) * ek + LINKS[q][2];
-    for (i = 0; i < ei; i++) for (j = 0; j < ej; j++) {
-      const int inner_ij = i > 0 && i < ei - 1 && j > 0 && j < ej - 1;
-      const long row = slb_node(lb, i, j, 0);
-      for (k = 0; k < ek; k++) {
-        x = row + k;
-        if (objidx[x] < 0) continue;
-        if (inner_ij && k > 0 && k < ek - 1) {
-          for (q = 1; q < 15; q++)
-            if (objidx[x + off[q]] < 0) break;
-        } else {
-          for (q = 1; q < 15; q++) {
-            int ii = i + LINKS[q][0], jj = j + LINKS[q][1], kk = k + LINKS[q][2];
-            ii = ii < 0 ? ii + ei : (ii >= ei ? ii - ei : ii);
-            jj = jj < 0 ? jj + ej : (jj >= ej ? jj - ej : jj);
-            kk = kk < 0 ? kk + ek : (kk >= ek ? kk - ek : kk);
-            if (objidx[slb_node(lb, ii, jj, kk)] < 0) break;
-          }
-        }
-        if (q < 15) { tmp_node[nb++] = x; count[objidx[x]]++; }
-      }
-    }
-  }
-  for (o = 1; o <= nobj; o++) start[o] = start[o - 1] + count[o - 1];
+  /* flag words on the GPU, and from them the solid nodes with a fluid
+   * neighbour, grouped by object, node order kept */
   free(st->bnd_node); free(st->bnd_obj);
-  st->bnd_node = (long *)xcalloc(nb, sizeof(long));
-  st->bnd_obj = (int *)xcalloc(nb, sizeof(int));
-  for (x = 0; x < nb; x++) {
-    int ob = objidx[tmp_node[x]];
-    long slot = start[ob]++;
-    st->bnd_node[slot] = tmp_node[x];
-    st->bnd_obj[slot] = ob;
-  }
+  st->bnd_node = NULL; st->bnd_obj = NULL;
+  slb_check(slbc_set_geometry_auto(st->dev, objidx, nobj, &st->bnd_node, &st->bnd_obj, &nb), "geometry upload");
   st->nbnd = nb;
   free(st->objs);
   st->objs = objs;
   st->nobj = nobj;
-  slb_check(slbc_set_geometry(st->dev, objidx, nobj, st->bnd_node, st->bnd_obj, nb), "geometry upload");
-  free(objidx); free(count); free(start); free(tmp_node);
+  free(objidx);
   st->geom_sent = st->geom_gen;
   /* solidity changed: body-force uniformity must be re-checked */
   st->bf_sent = 0;
