@@ -351,6 +351,162 @@ k_conv_fwd(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUten
   if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
 }
 
+// Convolution of the narrower layers (32, 64 or 128 output channels) with input
+// reuse.  An output tile is 16 (x) x 8 (y) x 2 (z) voxels.  For each
+// 32-channel chunk and each x-shift dx, one 5-D TMA box brings the input
+// block x0+dx .. x0+dx+15, y0-1 .. y0+8, z0-1 .. z0+2 (rows of 64 B,
+// x fastest) into shared memory, with the weights of the nine taps of that
+// dx.  The A operand of tap (dy, dz) for output slice s is then the 128
+// consecutive rows starting at row ((s + dz) * 10 + dy) * 16, a multiple of
+// 16 rows (1024 B, whole 64-byte swizzle atoms), so each input voxel crosses
+// from L2 three times per chunk instead of 27.  Slices s = 0, 1 accumulate
+// in TMEM columns [s * cout, (s + 1) * cout).
+constexpr int kHzSlices = 2;
+constexpr int kHzRows = (kHzSlices + 2) * 10 * 16;  // rows of one input block
+constexpr int kHzTileA = kHzRows * 64;              // 40 KB
+__host__ __device__ constexpr int hz_stages(int cout) { return cout <= 32 ? 3 : 2; }  // 32: 3, 64 / 128: 2
+__host__ __device__ constexpr int hz_smem(int cout) { return hz_stages(cout) * (kHzTileA + 9 * cout * 64) + 1024; }
+static_assert(hz_smem(32) <= 227 * 1024 && hz_smem(64) <= 227 * 1024 && hz_smem(128) <= 227 * 1024,
+              "stage budget");
+
+template <int NST>
+__global__ void __launch_bounds__(128, 1)
+k_conv_halo(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tw, ConvArgs a, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *tA = smem_raw + pad;
+  const uint32_t tile_b = (uint32_t)a.cout * 64u;  // one tap's weights
+  uint8_t *tB = tA + NST * kHzTileA;
+  __shared__ uint64_t full[NST], empty[NST], done;
+  __shared__ uint32_t tmem_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = blockIdx.y;
+  const int tiles_x = a.W / 16, tiles_y = a.H / 8;
+  const int m = blockIdx.x;
+  const int x0 = (m % tiles_x) * 16, y0 = ((m / tiles_x) % tiles_y) * 8, z0 = (m / (tiles_x * tiles_y)) * kHzSlices;
+  const int nck = a.cin / 32;
+  const int nk = 3 * nck;  // stages: (chunk, dx)
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, (uint32_t)a.tmem_cols);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < NST; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  int issued = 0;
+  if (threadIdx.x == 0) {
+    int s = 0, round = 0, ck = 0, dx = 0;
+    for (int kt = 0; kt < nk; kt++) {
+      if (round > 0 && !tc::mbar_wait(&empty[s], (uint32_t)(round - 1) & 1u, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      tc::mbar_expect_tx(&full[s], (uint32_t)kHzTileA + 9u * tile_b);
+      // padded coordinates: interior voxel v is v + 1, so x0 + dx is x0 + dx - 1 inside
+      tc::tma_load_5d(tA + s * kHzTileA, &tx, &full[s], a.in_coff + ck * 32, x0 + dx, y0, z0, n);
+      uint8_t *bs = tB + s * 9 * tile_b;
+      for (int dz = 0; dz < 3; dz++)
+        for (int dy = 0; dy < 3; dy++) {
+          const int tap = dz * 9 + dy * 3 + dx;
+          tc::tma_load_2d(bs + (dz * 3 + dy) * tile_b, &tw, &full[s], 0, (tap * nck + ck) * a.cout);
+        }
+      issued = kt + 1;
+      if (++dx == 3) { dx = 0; ++ck; }
+      if (++s == NST) { s = 0; ++round; }
+    }
+  } else if (threadIdx.x == 32) {
+    const uint32_t idesc = tc::idesc_bf16(128, a.cout);
+    int s = 0, round = 0;
+    for (int kt = 0; kt < nk; kt++) {
+      if (!tc::mbar_wait(&full[s], (uint32_t)round & 1u, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const uint64_t a0 = tc::smem_desc(tA + s * kHzTileA, tc::kSwizzle64, 64);
+      const uint64_t b0 = tc::smem_desc(tB + s * 9 * tile_b, tc::kSwizzle64, 64);
+      for (int dz = 0; dz < 3; dz++)
+        for (int dy = 0; dy < 3; dy++) {
+          const uint64_t bd = b0 + (uint64_t)((dz * 3 + dy) * (tile_b >> 4));
+#pragma unroll
+          for (int sl = 0; sl < kHzSlices; sl++) {
+            // rows ((sl + dz) * 10 + dy) * 16 of 64 B; the start field counts 16-byte units
+            const uint64_t ad = a0 + (uint64_t)(((sl + dz) * 10 + dy) * 16 * 4);
+            const uint32_t d = tmem + (uint32_t)(sl * a.cout);
+            const uint32_t acc = (kt != 0 || dz != 0 || dy != 0) ? 1u : 0u;
+            tc::mma_bf16(d, ad, bd, idesc, acc);
+            tc::mma_bf16(d, ad + 2, bd + 2, idesc, 1);
+          }
+        }
+      tc::mma_commit(&empty[s]);
+      if (++s == NST) { s = 0; ++round; }
+    }
+    tc::mma_commit(&done);
+  }
+  __syncwarp();
+  const bool okd = __all_sync(0xffffffffu, tc::mbar_wait(&done, 0, kWaitLimit));
+  tc::fence_after_sync();
+  if (okd) {
+    const int r = warp * 32 + lane;
+    const int vx = x0 + r % 16, vy = y0 + r / 16;
+#pragma unroll 1
+    for (int sl = 0; sl < kHzSlices; sl++) {
+      const int vz = z0 + sl;
+      const long long vox = (((long long)n * (a.D + 2) + vz + 1) * (a.H + 2) + vy + 1) * (a.W + 2) + vx + 1;
+      __nv_bfloat16 *dst = a.out ? a.out + vox * a.out_ctot + a.out_coff : nullptr;
+      const __nv_bfloat16 *msk = a.mask ? a.mask + vox * a.out_ctot + a.out_coff : nullptr;
+#pragma unroll 1
+      for (int c = 0; c < a.cout; c += 8) {
+        float v[8];
+        tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(sl * a.cout + c), v);
+        if (a.bias) {
+#pragma unroll
+          for (int i = 0; i < 8; i++) v[i] += a.bias[c + i];
+        }
+        if (a.relu) {
+#pragma unroll
+          for (int i = 0; i < 8; i++) v[i] = fmaxf(v[i], 0.0f);
+        }
+        if (msk) {
+          const uint4 mv = *(const uint4 *)(msk + c);
+          const __nv_bfloat16 *mb = (const __nv_bfloat16 *)&mv;
+#pragma unroll
+          for (int i = 0; i < 8; i++) v[i] = __bfloat162float(mb[i]) > 0.0f ? v[i] : 0.0f;
+        }
+        if (a.out_f32) {
+          float4 *fd = (float4 *)(a.out_f32 + vox * a.out_ctot + a.out_coff + c);
+          fd[0] = make_float4(v[0], v[1], v[2], v[3]);
+          fd[1] = make_float4(v[4], v[5], v[6], v[7]);
+        } else {
+          uint4 o;
+          __nv_bfloat162 *ob = (__nv_bfloat162 *)&o;
+#pragma unroll
+          for (int i = 0; i < 4; i++) ob[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+          *(uint4 *)(dst + c) = o;
+        }
+      }
+    }
+  }
+  if (!ok || !okd) atomicExch(err, 1);
+  if (threadIdx.x == 0) {
+    for (int kt = issued > NST ? issued - NST : 0; kt < issued; kt++)
+      if (!tc::mbar_wait(&full[kt % NST], (kt / NST) & 1, kWaitLimit)) atomicExch(err, 2);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.tmem_cols);
+}
+
 // Periodic halo of channels [coff, coff + nch) (nch a multiple of 8): every
 // halo voxel gets its wrapped interior voxel.  The halo voxels of a sample
 // are enumerated face by face: the planes z = 0 and z = D + 1 whole, then
@@ -686,6 +842,28 @@ static int conv3d(const void *in, int B, int D, int H, int W, int in_ctot, int i
   a.mask = (const __nv_bfloat16 *)mask;
   a.out = out_f32 ? nullptr : (__nv_bfloat16 *)out;
   a.out_f32 = out_f32;
+  if ((cout == 32 || cout == 64 || cout == 128) && W % 16 == 0 && H % 8 == 0 && D % kHzSlices == 0) {
+    // narrow layer: input-reuse tiles of 16 x 8 x 2 voxels
+    CUtensorMap th;
+    if (!make_map_act(&th, in, B, D, H, W, in_ctot, 16, 10, kHzSlices + 2))
+      return slbc::set_error("slbc_tc_conv3d: tensor map encoding failed"), 1;
+    a.tmem_cols = kHzSlices * cout;  // 64, 128 or 256 columns
+    static unsigned long long attr_hz[2] = {0, 0};
+    const int nst = hz_stages(cout), smem = hz_smem(cout);
+    const void *fn = nst == 3 ? (const void *)k_conv_halo<3> : (const void *)k_conv_halo<2>;
+    // one opt-in per instantiation, at the largest size it launches with
+    cudaError_t eh = smem_opt_in(fn, nst == 3 ? hz_smem(32) : hz_smem(128), attr_hz[nst == 3 ? 0 : 1]);
+    if (eh != cudaSuccess) return slbc::set_error(std::string("slbc_tc_conv3d: ") + cudaGetErrorString(eh)), 1;
+    const dim3 grid((unsigned)((W / 16) * (H / 8) * (D / kHzSlices)), (unsigned)B);
+    if (nst == 3)
+      k_conv_halo<3><<<grid, 128, smem, (cudaStream_t)stream>>>(th, tw, a, err);
+    else
+      k_conv_halo<2><<<grid, 128, smem, (cudaStream_t)stream>>>(th, tw, a, err);
+    slbc::count_launch();
+    eh = cudaGetLastError();
+    if (eh != cudaSuccess) return slbc::set_error(std::string("slbc_tc_conv3d: ") + cudaGetErrorString(eh)), 1;
+    return 0;
+  }
   static unsigned long long attr_done[3] = {0, 0, 0};
   const int nst = conv_stages(cout), smem = conv_smem(nst, cout);
   const void *fn = nst == 8 ? (const void *)k_conv_fwd<8> : (nst == 6 ? (const void *)k_conv_fwd<6> : (const void *)k_conv_fwd<4>);

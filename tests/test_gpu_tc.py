@@ -81,6 +81,13 @@ CONV_CASES = [  # B, D, H, W, cin, cout, in_ctot, in_coff, out_ctot, out_coff, r
     (1, 8, 32, 32, 96, 128, 96, 0, 128, 0, 1, 1),
     (1, 4, 4, 64, 32, 256, 32, 0, 256, 0, 0, 0),
     (1, 2, 2, 128, 32, 16, 40, 8, 24, 8, 0, 0),
+    # narrower layers (32, 64 or 128 output channels, W % 16, H % 8, D % 2 == 0):
+    # input-reuse tiles of 16 x 8 x 2 voxels
+    (2, 8, 16, 16, 32, 32, 32, 0, 32, 0, 1, 0),
+    (1, 4, 8, 32, 96, 32, 96, 0, 40, 8, 0, 1),
+    (1, 6, 16, 32, 64, 64, 96, 32, 72, 8, 1, 0),
+    (2, 2, 8, 16, 160, 64, 160, 0, 64, 0, 0, 1),
+    (1, 4, 8, 16, 64, 128, 64, 0, 136, 8, 1, 0),
 ]
 
 
