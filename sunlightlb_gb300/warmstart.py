@@ -481,6 +481,41 @@ def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-
     return traj
 
 
+def conv_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
+    """Forward-convolution time of every layer shape of the network on
+    `batch` grids of side^3 (CUDA events over `reps` launches on random
+    BF16 data): [(level, cin, cout, ms, TFLOP/s)]."""
+    import torch
+    k = Kernels(lib.dll)
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    w0, w1, w2, w3 = widths
+    shapes = [(0, IN_CH, w0), (0, w0, w0), (0, w1 + w0, w0), (0, w0, w0), (0, w0, OUT_CH),
+              (1, w0, w1), (1, w1, w1), (1, w2 + w1, w1), (1, w1, w1),
+              (2, w1, w2), (2, w2, w2), (2, w3 + w2, w2), (2, w2, w2),
+              (3, w2, w3), (3, w3, w3)]
+    out = []
+    for lv, cin, cout in shapes:
+        d = side >> lv
+        x = torch.randn((batch, d + 2, d + 2, d + 2, cin), device=dev).to(torch.bfloat16)
+        y = torch.zeros((batch, d + 2, d + 2, d + 2, cout), device=dev, dtype=torch.bfloat16)
+        w = (torch.randn(27 * cin * cout, device=dev) * 0.01).to(torch.bfloat16)
+        b = torch.zeros(cout, device=dev)
+        args = (x.data_ptr(), batch, d, d, d, cin, 0, cin, w.data_ptr(), b.data_ptr(), cout, y.data_ptr(), cout, 0,
+                1, None, stream)
+        for _ in range(3):
+            k.tc_conv3d(*args)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            k.tc_conv3d(*args)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out.append((lv, cin, cout, ms, 2.0 * 27 * cin * cout * batch * d ** 3 / (ms * 1e-3) / 1e12))
+    return out
+
+
 def first_within(traj, k_ref, rel):
     """(steps, wall) of the first check within rel of k_ref, else None."""
     for steps, k, wall in traj:
