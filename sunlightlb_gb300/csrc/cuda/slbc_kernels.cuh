@@ -88,6 +88,18 @@ __device__ __forceinline__ R link_term(int q, R ux, R uy, R uz) {
   }
 }
 
+// Correctly rounded a / b for a constant b with rb = RN(1/b), by Markstein's
+// theorem (binary64, round to nearest, no underflow or overflow): q = RN(a rb)
+// is within one ulp of a / b, the remainder r = a - b q is exact (one fused
+// multiply-add), and RN(q + r rb) = RN(a / b).  Three FP64 operations instead
+// of a full division; a = +-0 returns a (keeps the sign of zero).
+__device__ __forceinline__ double div_const(double a, double b, double rb) {
+  const double q = __dmul_rn(a, rb);
+  const double r = __fma_rn(-q, b, a);
+  const double q1 = __fma_rn(r, rb, q);
+  return a == 0.0 ? a : q1;
+}
+
 // Rebuild the 15 populations from density deviation, momentum and stress:
 // reference src/lbkernel.c:838-865, same evaluation order.
 template <typename T, bool EXACT>
@@ -96,9 +108,9 @@ __device__ __forceinline__ void rebuild(T (&t)[15], T drho, T rux, T ruy, T ruz,
   const T dbybc2 = T(1.0 / 24.0), dd2bybc4 = T(1.0 / 8.0);
   const T fdd2bybc4 = T(4.0) * dd2bybc4, edbybc2 = T(8.0) * dbybc2;
   T rhobyb, trsby3;
-  if (EXACT) {
-    rhobyb = drho / T(72.0);
-    trsby3 = (sxx + syy + szz) / T(3.0);
+  if (EXACT) {  // the reference's divisions, correctly rounded
+    rhobyb = div_const(drho, 72.0, 1.0 / 72.0);
+    trsby3 = div_const(sxx + syy + szz, 3.0, 1.0 / 3.0);
   } else {
     rhobyb = drho * T(1.0 / 72.0);
     trsby3 = (sxx + syy + szz) * T(1.0 / 3.0);
