@@ -119,3 +119,19 @@ def test_bf16_upload_of_unpaired_state_moves_to_fp32(gpu, orc):
     assert g.precision == 1
     assert rel(g.pops(), o.pops()) < 2e-5
     assert abs(g.vmeanx - o.vmeanx) <= 2e-5 * abs(o.vmeanx)
+
+
+@pytest.mark.parametrize("tau", [1.0, 0.8])
+def test_bf16_thin_lattice_couette(gpu, orc, tau):
+    """A 1 x 1 x 22 lattice (planar Couette flow between moving walls):
+    every plane ring and halo of the paired-deviation step wraps onto the
+    same few nodes.  Populations and wall stresses follow the FP64 oracle to
+    2e-5 at tau = 1 (zero stress part) and 2e-3 at tau = 0.8."""
+    from scenarios import couette
+    g, gw1, gw2, _ = couette(gpu, tau=tau, steps=3000, precision=2)
+    o, ow1, ow2, _ = couette(orc, tau=tau, steps=3000)
+    tol = 2e-5 if tau == 1.0 else 2e-3
+    assert g.precision == 2
+    assert rel(g.pops(), o.pops()) < tol
+    assert abs(gw1.frcx - ow1.frcx) <= tol * abs(ow1.frcx)
+    assert abs(gw2.frcx - ow2.frcx) <= tol * abs(ow2.frcx)
