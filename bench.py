@@ -426,8 +426,9 @@ def cpu_baseline(spheres, solid, budget_s=10.0, threads=1):
 
 def run_reference(args):
     """The reference's CPU implementation of the path (the oracle port of its
-    C code; the reference itself is not built on the GPU machine) on every host
-    core: one lattice per thread, aggregate MLUPS per step."""
+    C code: a build of the reference needs its sources, which this machine
+    may not hold) on every host core: one lattice per thread, aggregate MLUPS
+    per step."""
     from sunlightlb_gb300 import workloads as W
     world, rank, _ = dist_env()
     if rank != 0:
