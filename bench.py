@@ -753,6 +753,7 @@ def run_batch(args):
 # ---- learned warm start ------------------------------------------------------
 
 WARM_SEED, WARM_FORCE = 3, 1e-6
+WARM_CHECKS = (100, 50)  # permeability check intervals of the time-to-accuracy comparison
 
 
 def run_warmstart(args):
@@ -802,26 +803,42 @@ def run_warmstart(args):
         solid = WS.packing(ev_side, phi, sd)
         traj = WS.permeability_run(L, solid, force)
         k_conv = traj[-1][1]
-        plain = WS.first_within(traj, k_conv, 1e-4)
         sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         u = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1)
         torch.cuda.synchronize()
         t_inf = time.perf_counter() - t0
-        trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u)
-        hitw = WS.first_within(trajw, k_conv, 1e-4)
-        rows.append({"phi": round(phi, 4), "k": k_conv, "plain_steps_to_1e-4": plain[0] if plain else None,
-                     "plain_wall_s": round(plain[1], 4) if plain else None,
-                     "plain_converged_steps": traj[-1][0],
-                     "warm_steps_to_1e-4": hitw[0] if hitw else None,
-                     "warm_wall_s": round(hitw[1] + t_inf, 4) if hitw else None,
-                     "inference_s": round(t_inf, 4),
-                     "warm_k_error_first_check": abs(trajw[0][1] - k_conv) / abs(k_conv),
-                     "plain_k_error_first_check": abs(traj[0][1] - k_conv) / abs(k_conv)})
-    ok = [r for r in rows if r["plain_wall_s"] and r["warm_wall_s"]]
-    speed = [r["plain_wall_s"] / r["warm_wall_s"] for r in ok]
-    steps_ratio = [r["plain_steps_to_1e-4"] / r["warm_steps_to_1e-4"] for r in ok]
+        row = {"phi": round(phi, 4), "k": k_conv, "plain_converged_steps": traj[-1][0], "inference_s": round(t_inf, 4)}
+        # time to k within 1e-4, the permeability measured every `check` steps
+        # in both arms (the plain arm from rest, the warm arm from the
+        # prediction, inference included)
+        for check in WARM_CHECKS:
+            tp = traj if check == 100 else WS.permeability_run(L, solid, force, k_ref=k_conv, check=check)
+            plain = WS.first_within(tp, k_conv, 1e-4)
+            trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, check=check)
+            hitw = WS.first_within(trajw, k_conv, 1e-4)
+            row[f"check{check}"] = {"plain_steps": plain[0] if plain else None,
+                                    "plain_wall_s": round(plain[1], 4) if plain else None,
+                                    "warm_steps": hitw[0] if hitw else None,
+                                    "warm_wall_s": round(hitw[1] + t_inf, 4) if hitw else None}
+            if check == 100:
+                row["warm_k_error_first_check"] = abs(trajw[0][1] - k_conv) / abs(k_conv)
+                row["plain_k_error_first_check"] = abs(traj[0][1] - k_conv) / abs(k_conv)
+        rows.append(row)
+
+    def summary(check):
+        ok = [r[f"check{check}"] for r in rows if r[f"check{check}"]["plain_wall_s"] and r[f"check{check}"]["warm_wall_s"]]
+        speed = [r["plain_wall_s"] / r["warm_wall_s"] for r in ok]
+        steps_ratio = [r["plain_steps"] / r["warm_steps"] for r in ok]
+        return {"check_every": check, "samples": len(ok),
+                "wall_speedup_mean": float(np.mean(speed)) if speed else None,
+                "wall_speedup_median": float(np.median(speed)) if speed else None,
+                "steps_ratio_mean": float(np.mean(steps_ratio)) if steps_ratio else None,
+                "warm_faster_fraction": float(np.mean([s > 1 for s in speed])) if speed else None,
+                "plain_wall_total_s": round(float(sum(r["plain_wall_s"] for r in ok)), 3),
+                "warm_wall_total_s": round(float(sum(r["warm_wall_s"] for r in ok)), 3)}
+
     line = {
         "workload": f"learned warm start: U-Net trained on {args.train} converged {side}^3 packings, "
                     f"evaluated on {args.eval} held-out {ev_side}^3 packings",
@@ -838,10 +855,8 @@ def run_warmstart(args):
         "train_s": round(t_train, 1), "train_ms_per_iteration": round(1e3 * t_train / iters, 2),
         "loss": hist, "tc_status": tc_status,
         "eval": rows,
-        "summary": {"samples": len(ok), "wall_speedup_mean": float(np.mean(speed)) if speed else None,
-                    "wall_speedup_median": float(np.median(speed)) if speed else None,
-                    "steps_ratio_mean": float(np.mean(steps_ratio)) if steps_ratio else None,
-                    "warm_faster_fraction": float(np.mean([s > 1 for s in speed])) if speed else None},
+        "summary": summary(WARM_CHECKS[-1]),
+        "summary_by_check": [summary(c) for c in WARM_CHECKS],
     }
     print(json.dumps(line), flush=True)
     if args.save_weights:

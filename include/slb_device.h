@@ -304,6 +304,16 @@ int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, floa
                  int t, void *stream);
 int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
                 void *grad, int gctot, double *loss, void *stream);
+/* Gradient-norm clipping against a running norm, without a host round
+ * trip: slbc_nn_sqsum adds the sum of squares of one gradient tensor to
+ * state[0] (call it for every tensor), slbc_nn_clip turns the total into
+ * state[2] = min(1, factor * running / norm) and updates the running norm
+ * state[1] (0 before the first call) by decay, slbc_nn_scale multiplies a
+ * tensor by state[2].  A non-finite norm zeroes the gradients.  state is
+ * three device doubles, zero at the start. */
+int slbc_nn_sqsum(const float *g, long long n, double *state, void *stream);
+int slbc_nn_clip(double *state, float factor, float decay, void *stream);
+int slbc_nn_scale(float *g, long long n, const double *state, void *stream);
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
                    void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,

@@ -225,6 +225,48 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, long long n
   }
 }
 
+// Gradient-norm clipping against a running norm, all on the device (no
+// host round trip per iteration).  state[0]: sum of squares of every
+// gradient tensor (k_sqsum adds to it, k_clip_scale resets it); state[1]:
+// running norm (0 before the first call); state[2]: the scale to apply.
+__global__ void k_sqsum(const float *g, long long n, double *state) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    s += (double)g[i] * g[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(state, sh[0]);
+}
+
+// scale = min(1, factor * running / norm); running <- decay * running +
+// (1 - decay) * norm * scale.  A non-finite norm gives scale 0 (the
+// gradients are zeroed) and leaves the running norm as it was.
+__global__ void k_clip_scale(double *state, float factor, float decay) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double nrm = sqrt(state[0]);
+  state[0] = 0.0;
+  const double run = state[1] > 0.0 ? state[1] : nrm;
+  if (!isfinite(nrm)) {
+    state[2] = 0.0;
+    return;
+  }
+  const double sc = nrm > (double)factor * run ? (double)factor * run / nrm : 1.0;
+  state[1] = (double)decay * run + (1.0 - (double)decay) * nrm * sc;
+  state[2] = sc;
+}
+
+__global__ void k_scale(float *g, long long n, const double *state) {
+  const float sc = (float)state[2];
+  if (sc == 1.0f) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    g[i] = sc == 0.0f ? 0.0f : g[i] * sc;
+}
+
 // loss = mean over voxels and the 3 components of (pred - label)^2, pred in
 // FP32 channels 0..2 of a padded buffer (ctot_p channels), label
 // [n][D][H][W][3] FP32; grad (BF16, gctot channels, padded) = d loss /
@@ -266,9 +308,41 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, const f
 // periodic distance from a fluid node to the nearest solid node, searched
 // over a cube of half-width R (d = R when none is that close; 0 on solid
 // nodes); other channels zero (interior; the halo is filled afterwards)
-constexpr int kDistR = 5;
+constexpr int kDistR = 5, kDistCap = kDistR * kDistR;
 
-__global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W, bf16 *out, int ctot, int features) {
+// The squared distance min over the cube of dx^2 + dy^2 + dz^2 (solid
+// nodes, capped at R^2) separates into three one-axis passes (a minimum
+// of sums is the nested minimum), each over 2R + 1 neighbours instead of
+// (2R + 1)^3.  Values stay integers, so the result equals the cube search.
+// Pass 1 (along x, stride 1): nearest solid node on the row.
+__global__ void k_dist_x(const unsigned char *solid, long long total, int W, unsigned char *a) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(e % W);
+    const unsigned char *row = solid + (e - x);
+    int best = kDistCap;
+#pragma unroll
+    for (int dx = -kDistR; dx <= kDistR; dx++)
+      if (dx * dx < best && row[((x + dx) % W + W) % W]) best = dx * dx;
+    a[e] = (unsigned char)best;
+  }
+}
+
+// Passes 2 and 3 (along y, stride W, extent H; along z, stride W H,
+// extent D): b = min over |d| <= R of d^2 + a at the node d steps away.
+__global__ void k_dist_min(const unsigned char *a, long long total, int n, long long stride, unsigned char *b) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int p = (int)((e / stride) % n);
+    const unsigned char *col = a + (e - (long long)p * stride);
+    int best = kDistCap;
+#pragma unroll
+    for (int d = -kDistR; d <= kDistR; d++) best = min(best, d * d + (int)col[(long long)(((p + d) % n + n) % n) * stride]);
+    b[e] = (unsigned char)best;
+  }
+}
+
+// dist2: the squared distances of the passes above (null without features)
+__global__ void k_encode(const unsigned char *solid, const unsigned char *dist2, int B, int D, int H, int W, bf16 *out,
+                         int ctot) {
   const long long total = (long long)B * D * H * W;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -280,21 +354,8 @@ __global__ void k_encode(const unsigned char *solid, int B, int D, int H, int W,
     for (int c = 0; c < ctot; c += 8) *(uint4 *)(p + c) = make_uint4(0, 0, 0, 0);
     const bool s = solid[e] != 0;
     p[0] = __float2bfloat16(s ? 1.0f : 0.0f);
-    if (features && !s) {
-      const unsigned char *sn = solid + (long long)n * D * H * W;
-      int best = kDistR * kDistR;
-      for (int dz = -kDistR; dz <= kDistR; dz++) {
-        const int zz = ((z + dz) % D + D) % D;
-        for (int dy = -kDistR; dy <= kDistR; dy++) {
-          const int yy = ((y + dy) % H + H) % H;
-          const unsigned char *row = sn + ((long long)zz * H + yy) * W;
-          for (int dx = -kDistR; dx <= kDistR; dx++) {
-            const int d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 < best && row[((x + dx) % W + W) % W]) best = d2;
-          }
-        }
-      }
-      const float d = sqrtf((float)best) * (1.0f / kDistR);
+    if (dist2 && !s) {
+      const float d = sqrtf((float)dist2[e]) * (1.0f / kDistR);
       p[1] = __float2bfloat16(d);
       p[2] = __float2bfloat16(d * d);
     }
@@ -412,6 +473,24 @@ int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, floa
   return launched("slbc_nn_adam");
 }
 
+int slbc_nn_sqsum(const float *g, long long n, double *state, void *stream) {
+  if (n <= 0) return bad("slbc_nn_sqsum: empty tensor");
+  k_sqsum<<<std::min(grid_for(n), 152 * 4), 256, 0, (cudaStream_t)stream>>>(g, n, state);
+  return launched("slbc_nn_sqsum");
+}
+
+int slbc_nn_clip(double *state, float factor, float decay, void *stream) {
+  if (!(factor > 0.0f) || !(decay >= 0.0f && decay < 1.0f)) return bad("slbc_nn_clip: factor > 0, 0 <= decay < 1");
+  k_clip_scale<<<1, 32, 0, (cudaStream_t)stream>>>(state, factor, decay);
+  return launched("slbc_nn_clip");
+}
+
+int slbc_nn_scale(float *g, long long n, const double *state, void *stream) {
+  if (n <= 0) return bad("slbc_nn_scale: empty tensor");
+  k_scale<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(g, n, state);
+  return launched("slbc_nn_scale");
+}
+
 int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
                 void *grad, int gctot, double *loss, void *stream) {
   if (ctot_p < 3 || gctot % 8 || gctot < 8) return bad("slbc_nn_mse: bad channel counts");
@@ -423,9 +502,26 @@ int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
                    void *stream) {
   if (ctot % 8 || ctot < 8) return bad("slbc_nn_encode: bad channel count");
-  k_encode<<<grid_for((long long)B * D * H * W), 256, 0, (cudaStream_t)stream>>>(solid, B, D, H, W, (bf16 *)out, ctot,
-                                                                                features);
-  return launched("slbc_nn_encode");
+  const long long total = (long long)B * D * H * W;
+  const cudaStream_t st = (cudaStream_t)stream;
+  unsigned char *a = nullptr;
+  if (features) {
+    // two stream-ordered scratch masks of one byte per voxel
+    const cudaError_t e = cudaMallocAsync((void **)&a, 2 * total, st);
+    if (e != cudaSuccess) return bad((std::string("slbc_nn_encode scratch: ") + cudaGetErrorString(e)).c_str());
+    unsigned char *b = a + total;
+    k_dist_x<<<grid_for(total), 256, 0, st>>>(solid, total, W, a);
+    k_dist_min<<<grid_for(total), 256, 0, st>>>(a, total, H, W, b);
+    k_dist_min<<<grid_for(total), 256, 0, st>>>(b, total, D, (long long)W * H, a);
+    slbc::count_launch(3);
+  }
+  k_encode<<<grid_for(total), 256, 0, st>>>(solid, a, B, D, H, W, (bf16 *)out, ctot);
+  const int rc = launched("slbc_nn_encode");
+  if (a) {
+    const cudaError_t e = cudaFreeAsync(a, st);
+    if (e != cudaSuccess && rc == 0) return bad((std::string("slbc_nn_encode scratch: ") + cudaGetErrorString(e)).c_str());
+  }
+  return rc;
 }
 
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,

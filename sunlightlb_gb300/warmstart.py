@@ -56,6 +56,9 @@ class Kernels:
             "slbc_nn_wdgrad": [p, i, i, i, i, p, p],
             "slbc_nn_adam": [p, p, p, p, ll, f, f, f, f, i, p],
             "slbc_nn_mse": [p, i, p, p, i, i, i, i, p, i, p, p],
+            "slbc_nn_sqsum": [p, ll, p, p],
+            "slbc_nn_clip": [p, f, f, p],
+            "slbc_nn_scale": [p, ll, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, p, p],
             "slbc_tc_status": [],
@@ -123,6 +126,7 @@ class UNet:
         self.buf = {n: self._act(lv, c) for n, (lv, c) in self.buf_spec.items()}
         self.buf["OUT"] = torch.zeros(self._shape(0, OUT_CH), device=self.dev, dtype=torch.float32)
         self.grad = None
+        self.clip_state = None
         self.params = params if params is not None else self._init_params(seed)
         self.wf = {}
         self.wd = {}
@@ -347,6 +351,19 @@ class UNet:
                 self._dgrad(lay_a, ga, gpn)
         return self.loss_acc
 
+    def clip_grads(self, factor=3.0, decay=0.98):
+        """Scale all gradients down to at most `factor` times their running
+        norm (device-side: no host synchronisation)."""
+        if self.clip_state is None:
+            self.clip_state = self.torch.zeros(3, device=self.dev, dtype=self.torch.float64)
+        st = self.clip_state.data_ptr()
+        grads = [self.params[name]["g" + key] for name, *_ in self.layers for key in ("w", "b")]
+        for g in grads:
+            self.k.nn_sqsum(g.data_ptr(), g.numel(), st, self.stream)
+        self.k.nn_clip(st, factor, decay, self.stream)
+        for g in grads:
+            self.k.nn_scale(g.data_ptr(), g.numel(), st, self.stream)
+
     def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         self.t += 1
         for name, *_ in self.layers:
@@ -524,12 +541,15 @@ def first_within(traj, k_ref, rel):
     return None
 
 
-def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None):
+def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None, warmup=100, clip=3.0):
     """Adam on mini-batches of net.B samples drawn (seeded) from masks
     (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)),
     optional per-sample loss weights (device FP32 (N,)); with lr_min the
-    learning rate decays from lr to lr_min along a half cosine.  Returns the
-    loss every log_every iterations (and the last)."""
+    learning rate decays from lr to lr_min along a half cosine.  The rate
+    ramps up linearly over the first `warmup` iterations and the gradients
+    are clipped to `clip` times their running norm (0: off): without these,
+    some seeds of the 1e-3 rate fell into a plateau near loss 0.25 early on.
+    Returns the loss every log_every iterations (and the last)."""
     import torch
     rng = np.random.default_rng(seed)
     n = masks.shape[0]
@@ -542,7 +562,11 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None
         net.encode(mb)
         net.forward()
         loss = net.loss_and_backward(lab, sw)
+        if clip:
+            net.clip_grads(clip)
         rate = lr if lr_min is None else lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * (it - 1) / iters))
+        if it <= warmup:
+            rate *= it / warmup
         net.adam(rate)
         if (log_every and it % log_every == 0) or it == iters:
             hist.append((it, float(loss.item())))

@@ -83,6 +83,38 @@ def test_wall_distance_features(gpu):
     assert np.abs(got[..., 2] - np.where(s, 0.0, d * d)).max() <= 4e-3
 
 
+@pytest.mark.parametrize("B,D,H,W,frac", [(2, 4, 8, 16, 0.98), (1, 12, 3, 40, 0.995), (3, 16, 16, 16, 0.9)])
+def test_wall_distance_small_and_wrapped(gpu, B, D, H, W, frac):
+    """The separable distance passes on grids thinner than the search cube
+    (offsets wrap onto the same node more than once) and on batches: equal
+    to the cube search over periodic images."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    k = WS.Kernels(gpu.dll)
+    rng = np.random.default_rng(B * 1000 + D * 10 + W)
+    solid = (rng.random((B, D, H, W)) > frac).astype(np.uint8)
+    out = torch.zeros((B, D + 2, H + 2, W + 2, 32), device="cuda", dtype=torch.bfloat16)
+    k.nn_encode(torch.as_tensor(solid, device="cuda").data_ptr(), B, D, H, W, out.data_ptr(), 32, 1,
+                torch.cuda.current_stream().cuda_stream)
+    got = out[:, 1:-1, 1:-1, 1:-1, :].float().cpu().numpy()
+    for b in range(B):
+        s = solid[b].astype(bool)
+        best = np.full((D, H, W), 25.0)
+        for dz in range(-5, 6):
+            for dy in range(-5, 6):
+                for dx in range(-5, 6):
+                    d2 = dx * dx + dy * dy + dz * dz
+                    if d2 >= 25:
+                        continue
+                    hit = np.roll(s, shift=(-dz, -dy, -dx), axis=(0, 1, 2))
+                    best = np.where(hit & (d2 < best), d2, best)
+        d = np.where(s, 0.0, np.sqrt(best) / 5.0)
+        assert np.array_equal(got[b, ..., 0], s.astype(np.float32))
+        assert np.abs(got[b, ..., 1] - d).max() <= 4e-3
+        assert np.abs(got[b, ..., 2] - np.where(s, 0.0, d * d)).max() <= 4e-3
+        assert not got[b, ..., 3:].any()
+
+
 def test_training_lowers_the_loss(gpu):
     """A few Adam steps on one batch reduce its loss."""
     torch = pytest.importorskip("torch")
@@ -94,8 +126,46 @@ def test_training_lowers_the_loss(gpu):
     labels = (rng.random((B, D, H, W, 3)).astype(np.float32) * 0.5) * (1 - solid[..., None])
     m_dev = torch.as_tensor(solid, device="cuda")
     l_dev = torch.as_tensor(labels, device="cuda")
-    hist = WS.train(net, m_dev, l_dev, iters=60, lr=2e-3, seed=1, log_every=1)
+    hist = WS.train(net, m_dev, l_dev, iters=60, lr=2e-3, seed=1, log_every=1, warmup=10)
     assert net.status() == 0
     first = np.mean([l for _, l in hist[:5]])
     last = np.mean([l for _, l in hist[-5:]])
     assert last < 0.7 * first, (first, last)
+
+
+def test_gradient_clipping(gpu):
+    """Device-side clipping against the running gradient norm: the first
+    call sets the running norm, a 10x spike is scaled to 3x the running
+    norm, a non-finite gradient is zeroed without touching the running norm."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    net = WS.UNet(gpu, 32, 32, 64, batch=1, widths=(32, 32, 32, 32), seed=2)
+    net._alloc_grads()
+    grads = [net.params[name]["g" + key] for name, *_ in net.layers for key in ("w", "b")]
+    count = sum(g.numel() for g in grads)
+
+    def fill(v):
+        for g in grads:
+            g.fill_(v)
+
+    def norm():
+        return float(torch.sqrt(sum((g.double() ** 2).sum() for g in grads)))
+
+    v = 2.0 ** -10  # exact in FP32, so the norms below are exact
+    fill(v)
+    n1 = v * np.sqrt(count)
+    net.clip_grads(3.0, 0.98)
+    assert abs(norm() - n1) <= 1e-6 * n1
+    run = n1
+    assert abs(float(net.clip_state[1]) - run) <= 1e-6 * run  # decay passed as FP32
+    fill(10 * v)  # 10x spike
+    net.clip_grads(3.0, 0.98)
+    assert abs(norm() - 3.0 * n1) <= 1e-5 * n1
+    run = 0.98 * run + 0.02 * 3.0 * n1
+    assert abs(float(net.clip_state[1]) - run) <= 1e-6 * run  # decay passed as FP32
+    fill(v)
+    grads[3][0] = float("nan")
+    net.clip_grads(3.0, 0.98)
+    assert all(not g.any() for g in grads)
+    assert abs(float(net.clip_state[1]) - run) <= 1e-6 * run  # decay passed as FP32
+    assert float(net.clip_state[0]) == 0.0
