@@ -541,7 +541,35 @@ def first_within(traj, k_ref, rel):
     return None
 
 
-def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None, warmup=100, clip=3.0):
+def symmetry(mask, label, flip_x, flip_y, flip_z, swap_yz):
+    """One of the 16 symmetries of the periodic packed-bed problem with the
+    body force along x, applied to a mask (D, H, W) over (x, y, z) and its
+    steady flow (D, H, W, 3).  Reflecting y (or z) negates u_y (u_z);
+    swapping y and z swaps u_y and u_z; reflecting x reverses the force, so
+    by linearity of Stokes flow the flow of the reflected bed is the
+    reflected flow with u_x kept and u_y, u_z negated."""
+    import torch
+    dims, sign = [], [1.0, 1.0, 1.0]
+    if flip_x:
+        dims.append(0)
+        sign[1], sign[2] = -sign[1], -sign[2]
+    if flip_y:
+        dims.append(1)
+        sign[1] = -sign[1]
+    if flip_z:
+        dims.append(2)
+        sign[2] = -sign[2]
+    if dims:
+        mask, label = mask.flip(dims), label.flip(dims)
+    label = label * torch.tensor(sign, device=label.device, dtype=label.dtype)
+    if swap_yz:
+        mask = mask.transpose(1, 2)
+        label = label.transpose(1, 2)[..., [0, 2, 1]]
+    return mask.contiguous(), label.contiguous()
+
+
+def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None, warmup=100, clip=3.0,
+          augment=False):
     """Adam on mini-batches of net.B samples drawn (seeded) from masks
     (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)),
     optional per-sample loss weights (device FP32 (N,)); with lr_min the
@@ -549,6 +577,8 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None
     ramps up linearly over the first `warmup` iterations and the gradients
     are clipped to `clip` times their running norm (0: off): without these,
     some seeds of the 1e-3 rate fell into a plateau near loss 0.25 early on.
+    With augment, every drawn sample goes through a random one of the 16
+    symmetries of the problem (cubic grids only).
     Returns the loss every log_every iterations (and the last)."""
     import torch
     rng = np.random.default_rng(seed)
@@ -559,6 +589,9 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None
         mb = masks.index_select(0, idx).contiguous()
         lab = labels.index_select(0, idx).contiguous()
         sw = sample_w.index_select(0, idx).contiguous() if sample_w is not None else None
+        if augment and mb.shape[1] == mb.shape[2] == mb.shape[3]:
+            for b, bits in enumerate(rng.integers(0, 2, size=(net.B, 4))):
+                mb[b], lab[b] = symmetry(mb[b], lab[b], *bits)
         net.encode(mb)
         net.forward()
         loss = net.loss_and_backward(lab, sw)

@@ -169,3 +169,27 @@ def test_gradient_clipping(gpu):
     assert all(not g.any() for g in grads)
     assert abs(float(net.clip_state[1]) - run) <= 1e-6 * run  # decay passed as FP32
     assert float(net.clip_state[0]) == 0.0
+
+
+def test_symmetries_map_flows_to_flows(gpu):
+    """The training augmentation: each symmetry applied to a bed and its
+    converged flow gives the converged flow of the transformed bed
+    (FP64 lattices; a wrong sign or component swap shows as an error of
+    the size of u_y, u_z)."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    n = 24
+    solid = WS.packing(n, 0.25, 11)
+    cases = [(1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1), (1, 1, 0, 1), (1, 1, 1, 1)]
+    m0 = torch.as_tensor(solid.astype(np.uint8), device="cuda")
+    (f0,), _ = WS.converged_flows(gpu, [solid], tol=1e-11, maxsteps=40000, precision=0)
+    l0 = WS.to_labels(f0, (n, n, n))
+    moved = [WS.symmetry(m0, l0, *c) for c in cases]
+    fields, _ = WS.converged_flows(gpu, [m.cpu().numpy().astype(bool) for m, _ in moved], tol=1e-11, maxsteps=40000,
+                                   precision=0)
+    scale = float(l0.abs().max())
+    side = float(l0[..., 1:].abs().max())
+    assert side > 0.05 * scale  # the transverse components are not negligible
+    for c, (m, l), f in zip(cases, moved, fields):
+        got = WS.to_labels(f, (n, n, n))
+        assert float((got - l).abs().max()) <= 1e-6 * scale, c

@@ -198,3 +198,21 @@ def test_packings_are_seeded_and_stable():
         assert len(spheres) == n
         assert hashlib.sha256(np.packbits(solid).tobytes()).hexdigest()[:32] == digest
         assert solid.mean() >= args[1]
+
+
+def test_flow_symmetries_algebra():
+    """The augmentation's symmetries on a constant flow (1, 2, 3): signs and
+    component swap, and each generator undone by applying it again."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    m = torch.zeros((4, 4, 4), dtype=torch.uint8)
+    m[0, 1, 2] = 1
+    lab = torch.tensor([1.0, 2.0, 3.0]).expand(4, 4, 4, 3).contiguous()
+    want = {(1, 0, 0, 0): (1, -2, -3), (0, 1, 0, 0): (1, -2, 3), (0, 0, 1, 0): (1, 2, -3), (0, 0, 0, 1): (1, 3, 2)}
+    where = {(1, 0, 0, 0): (3, 1, 2), (0, 1, 0, 0): (0, 2, 2), (0, 0, 1, 0): (0, 1, 1), (0, 0, 0, 1): (0, 2, 1)}
+    for bits, u in want.items():
+        m2, l2 = WS.symmetry(m, lab, *bits)
+        assert torch.equal(l2[1, 2, 3], torch.tensor(u, dtype=torch.float32)), bits
+        assert m2[where[bits]] == 1 and int(m2.sum()) == 1, bits
+        m3, l3 = WS.symmetry(m2, l2, *bits)
+        assert torch.equal(m3, m) and torch.equal(l3, lab), bits
