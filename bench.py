@@ -825,6 +825,13 @@ def run_warmstart(args):
             if check == 100:
                 row["warm_k_error_first_check"] = abs(trajw[0][1] - k_conv) / abs(k_conv)
                 row["plain_k_error_first_check"] = abs(traj[0][1] - k_conv) / abs(k_conv)
+        # the same network with the predicted velocity set unshifted and
+        # shifted by half the force (the warm start sets u - F / rho0)
+        for shift in (0.0, 0.5):
+            us = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=shift)
+            hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=us, check=50), k_conv, 1e-4)
+            row[f"check50_force_shift_{shift:g}"] = {"warm_steps": hs[0] if hs else None,
+                                                    "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
         rows.append(row)
 
     def summary(check):
@@ -857,6 +864,12 @@ def run_warmstart(args):
         "eval": rows,
         "summary": summary(WARM_CHECKS[-1]),
         "summary_by_check": [summary(c) for c in WARM_CHECKS],
+        "force_shift_at_check50": {
+            f"{shift:g}": {"wall_speedup_mean": float(np.mean([r["check50"]["plain_wall_s"] / r[key]["warm_wall_s"]
+                                                               for r in rows if r[key]["warm_wall_s"]])),
+                           "steps_ratio_mean": float(np.mean([r["check50"]["plain_steps"] / r[key]["warm_steps"]
+                                                              for r in rows if r[key]["warm_steps"]]))}
+            for shift, key in ((0.0, "check50_force_shift_0"), (0.5, "check50_force_shift_0.5"))},
     }
     print(json.dumps(line), flush=True)
     if args.save_weights:

@@ -317,7 +317,7 @@ int slbc_nn_scale(float *g, long long n, const double *state, void *stream);
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
                    void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                   float *u, void *stream);
+                   float shift_x, float *u, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

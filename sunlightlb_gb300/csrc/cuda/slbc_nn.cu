@@ -364,9 +364,9 @@ __global__ void k_encode(const unsigned char *solid, const unsigned char *dist2,
 
 // prediction (FP32 channels 0..2 of a padded buffer) * scale on fluid
 // nodes into three FP32 arrays u[c * N + e] (0 on solid nodes), the layout
-// of lbsetveldev
+// of lbsetveldev; shift_x is subtracted from u_x on fluid nodes
 __global__ void k_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                         float *u) {
+                         float shift_x, float *u) {
   const long long total = (long long)D * H * W;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -375,7 +375,7 @@ __global__ void k_decode(const float *pred, int ctot_p, const unsigned char *sol
     const int z = (int)(r / H);
     const long long v = vox(0, z, y, x, D, H, W);
 #pragma unroll
-    for (int c = 0; c < 3; c++) u[c * total + e] = solid[e] ? 0.0f : scale * pred[v * ctot_p + c];
+    for (int c = 0; c < 3; c++) u[c * total + e] = solid[e] ? 0.0f : scale * pred[v * ctot_p + c] - (c == 0 ? shift_x : 0.0f);
   }
 }
 
@@ -525,9 +525,10 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
 }
 
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                   float *u, void *stream) {
+                   float shift_x, float *u, void *stream) {
   if (ctot_p < 3) return bad("slbc_nn_decode: bad channel count");
-  k_decode<<<grid_for((long long)D * H * W), 256, 0, (cudaStream_t)stream>>>(pred, ctot_p, solid, D, H, W, scale, u);
+  k_decode<<<grid_for((long long)D * H * W), 256, 0, (cudaStream_t)stream>>>(pred, ctot_p, solid, D, H, W, scale,
+                                                                                       shift_x, u);
   return launched("slbc_nn_decode");
 }
 

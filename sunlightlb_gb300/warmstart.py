@@ -60,7 +60,7 @@ class Kernels:
             "slbc_nn_clip": [p, f, f, p],
             "slbc_nn_scale": [p, ll, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
-            "slbc_nn_decode": [p, i, p, i, i, i, f, p, p],
+            "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, p],
             "slbc_tc_status": [],
         }
         self.dll = dll
@@ -446,16 +446,26 @@ def to_labels(field, shape):
 
 # ---- warm start -------------------------------------------------------------------
 
-def predict_velocity(net, solid_u8, force, eta):
+def predict_velocity(net, solid_u8, force, eta, rho0=72.0, force_shift=1.0):
     """Velocity field (3 x N device FP32, layout of lbsetveldev) predicted by
-    a batch-1 network for a solid mask (device uint8 (D, H, W))."""
+    a batch-1 network for a solid mask (device uint8 (D, H, W)), body force
+    `force` along x.  The labels are the converged fields lbvelocity reads
+    from post-collision states, while lbsetveldev takes the velocity of the
+    state before the collision that adds the force: a converged state is
+    rebuilt exactly from u - F / (2 rho) and its own density (10 steps to
+    k within 1e-4, against 120-850 without the shift).  With rho = rho0
+    everywhere (the network predicts no density) the whole force, u - F /
+    rho0, measured best: on 100 held-out 128^3 packings the mean steps
+    ratio to the plain start was 2.73x unshifted, 3.01x with F / 2 and
+    3.20x with F.  So u_x is set with force_shift * force / rho0 taken off
+    on fluid nodes."""
     import torch
     net.encode(solid_u8.view(1, *solid_u8.shape))
     out = net.forward()
     n = solid_u8.numel()
     u = torch.empty(3 * n, device="cuda", dtype=torch.float32)
-    net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta, u.data_ptr(),
-                    net.stream)
+    net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta,
+                    force_shift * force / rho0, u.data_ptr(), net.stream)
     return u
 
 
