@@ -754,6 +754,7 @@ def run_batch(args):
 
 WARM_SEED, WARM_FORCE = 3, 1e-6
 WARM_CHECKS = (100, 50)  # permeability check intervals of the time-to-accuracy comparison
+WARM_VARIANTS = ("velocity_only", "state_whole_force_shift")
 
 
 def run_warmstart(args):
@@ -778,7 +779,8 @@ def run_warmstart(args):
     t_pack = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    fields, lsteps = WS.converged_flows(L, solids, force=force, tol=args.label_tol, maxsteps=args.label_maxsteps)
+    fields, lsteps = WS.converged_flows(L, solids, force=force, tol=args.label_tol, maxsteps=args.label_maxsteps,
+                                        density=True)
     torch.cuda.synchronize()
     t_labels = time.perf_counter() - t0
     masks = torch.as_tensor(np.stack(solids).astype(np.uint8), device="cuda")
@@ -806,7 +808,7 @@ def run_warmstart(args):
         sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        u = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1)
+        u, drho = WS.predict_state(inf, sdev, force, WS.ETA_TAU1)
         torch.cuda.synchronize()
         t_inf = time.perf_counter() - t0
         row = {"phi": round(phi, 4), "k": k_conv, "plain_converged_steps": traj[-1][0], "inference_s": round(t_inf, 4)}
@@ -816,7 +818,7 @@ def run_warmstart(args):
         for check in WARM_CHECKS:
             tp = traj if check == 100 else WS.permeability_run(L, solid, force, k_ref=k_conv, check=check)
             plain = WS.first_within(tp, k_conv, 1e-4)
-            trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, check=check)
+            trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho, check=check)
             hitw = WS.first_within(trajw, k_conv, 1e-4)
             row[f"check{check}"] = {"plain_steps": plain[0] if plain else None,
                                     "plain_wall_s": round(plain[1], 4) if plain else None,
@@ -825,13 +827,18 @@ def run_warmstart(args):
             if check == 100:
                 row["warm_k_error_first_check"] = abs(trajw[0][1] - k_conv) / abs(k_conv)
                 row["plain_k_error_first_check"] = abs(traj[0][1] - k_conv) / abs(k_conv)
-        # the same network with the predicted velocity set unshifted and
-        # shifted by half the force (the warm start sets u - F / rho0)
-        for shift in (0.0, 0.5):
-            us = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=shift)
-            hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=us, check=50), k_conv, 1e-4)
-            row[f"check50_force_shift_{shift:g}"] = {"warm_steps": hs[0] if hs else None,
-                                                    "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
+        # the same network set without its density (rho = rho0, u - F / rho0,
+        # the best shift without a density) and with its density but the
+        # whole-force shift (the warm start sets u - F / (2 rho0) and rho)
+        for name in WARM_VARIANTS:
+            if name == "velocity_only":
+                vs, ds = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0), None
+            else:
+                vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0)
+            hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=vs, warm_drho=ds, check=50),
+                                 k_conv, 1e-4)
+            row[f"check50_{name}"] = {"warm_steps": hs[0] if hs else None,
+                                      "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
         rows.append(row)
 
     def summary(check):
@@ -855,6 +862,7 @@ def run_warmstart(args):
                    "widths": list(net.widths), "batch": args.batch, "iterations": iters,
                    "lr": f"{args.lr:g} -> {args.lr * 0.01:g} (half cosine)",
                    "input": "solid mask + periodic wall distance d/5 and (d/5)^2 (d capped at 5)",
+                   "output": "velocity and density deviation; set with u - F / (2 rho0) and rho0 + drho",
                    "labels": f"FP32 populations, converged to |d vmeanx|/vmeanx < {args.label_tol:g} per 200 steps",
                    "precision": "BF16 weights/activations, FP32 accumulation (tcgen05)"},
         "packing_s": round(t_pack, 1), "labels_s": round(t_labels, 1),
@@ -864,12 +872,12 @@ def run_warmstart(args):
         "eval": rows,
         "summary": summary(WARM_CHECKS[-1]),
         "summary_by_check": [summary(c) for c in WARM_CHECKS],
-        "force_shift_at_check50": {
-            f"{shift:g}": {"wall_speedup_mean": float(np.mean([r["check50"]["plain_wall_s"] / r[key]["warm_wall_s"]
-                                                               for r in rows if r[key]["warm_wall_s"]])),
-                           "steps_ratio_mean": float(np.mean([r["check50"]["plain_steps"] / r[key]["warm_steps"]
-                                                              for r in rows if r[key]["warm_steps"]]))}
-            for shift, key in ((0.0, "check50_force_shift_0"), (0.5, "check50_force_shift_0.5"))},
+        "variants_at_check50": {
+            name: {"wall_speedup_mean": float(np.mean([r["check50"]["plain_wall_s"] / r[f"check50_{name}"]["warm_wall_s"]
+                                                       for r in rows if r[f"check50_{name}"]["warm_wall_s"]])),
+                   "steps_ratio_mean": float(np.mean([r["check50"]["plain_steps"] / r[f"check50_{name}"]["warm_steps"]
+                                                      for r in rows if r[f"check50_{name}"]["warm_steps"]]))}
+            for name in WARM_VARIANTS},
     }
     print(json.dumps(line), flush=True)
     if args.save_weights:

@@ -224,6 +224,13 @@ int slbc_get_velocity_dev(slbc_lattice *h, double fac, float *u);
 /* Velocity warm start from three device FP32 arrays (as slbc_set_velocity
  * with rho = rho0; velocities already rescaled): layout N. */
 int slbc_set_velocity_dev(slbc_lattice *h, const float *u, int skip_solid);
+/* slbc_get_velocity_dev plus, when drho is not null, the density deviation
+ * rho - rho0 = sum_q a_q of every fluid node (0 on solid nodes) into one
+ * device FP32 array. */
+int slbc_get_state_dev(slbc_lattice *h, double fac, float *u, float *drho);
+/* slbc_set_velocity_dev with the density of every node rho0 + drho[x]
+ * (drho: device FP32 deviations, kept exact; null: rho = rho0). */
+int slbc_set_state_dev(slbc_lattice *h, const float *u, const float *drho, int skip_solid);
 
 /* Tensor-core kernels of the learned warm start (no counterpart in the
  * reference).  slbc_tc_gemm: D[M x N] (FP32, row-major, leading dimension
@@ -302,8 +309,8 @@ int slbc_nn_wfwd(const float *master, int cout, int cin, void *w, void *stream);
 int slbc_nn_wdgrad(const float *master, int cout, int cin, int ci0, int nci, void *w, void *stream);
 int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
                  int t, void *stream);
-int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
-                void *grad, int gctot, double *loss, void *stream);
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int nch, const float *sample_w, int B, int D, int H,
+                int W, void *grad, int gctot, double *loss, void *stream);
 /* Gradient-norm clipping against a running norm, without a host round
  * trip: slbc_nn_sqsum adds the sum of squares of one gradient tensor to
  * state[0] (call it for every tensor), slbc_nn_clip turns the total into
@@ -317,7 +324,7 @@ int slbc_nn_scale(float *g, long long n, const double *state, void *stream);
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,
                    void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                   float shift_x, float *u, void *stream);
+                   float shift_x, float *u, float drho_scale, float *drho, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

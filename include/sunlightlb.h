@@ -322,6 +322,12 @@ void lbsetveldev(LBSys, void *);
 /* Velocity field (the per-node accvmean term, half-force corrected when
  * lb->vel_corrected) into three FP32 device arrays laid out as above. */
 void lbvelocity(LBSys, void *);
+/* lbvelocity plus the density deviation rho - rho0 of every fluid node (0 on
+ * solid nodes) into one FP32 device array (appended, no counterpart). */
+void lbstate(LBSys, void *, void *);
+/* lbsetveldev with the density rho0 + drho[x] of every node from an FP32
+ * device array of deviations (NULL: rho0) (appended, no counterpart). */
+void lbsetstatedev(LBSys, void *, void *);
 /* Tracer totals over "fluid", "solid", "adsorbed" or "all" nodes (the sums
  * that mpcheck and adtotal print, reference src/mpmisc.c:121-136), or
  * "injected": the tracer that mpall, mpslab, mpwall, mpsph and mpcyl have

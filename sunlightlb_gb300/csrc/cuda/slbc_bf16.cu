@@ -333,9 +333,11 @@ __global__ void k_setvel_pair(PairArgs a, const double *stage, long long x0, lon
   const long long x = x0 + e;
   Relaxed<float> r{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (!(skip_solid && (a.flags[x] & FLAG_SOLID))) {  // else all populations zero
-    const float rho = has_rho ? (float)stage[4 * e] : (float)rho0;
+    // has_rho 1: stage[4e] is the density; 2: the deviation rho - rho0
+    const float rho = has_rho == 2 ? (float)rho0 + (float)stage[4 * e] : has_rho ? (float)stage[4 * e] : (float)rho0;
     const float vx = (float)stage[4 * e + 1], vy = (float)stage[4 * e + 2], vz = (float)stage[4 * e + 3];
-    r.drho = rho - (float)rho0; r.rux = rho * vx; r.ruy = rho * vy; r.ruz = rho * vz;
+    r.drho = has_rho == 2 ? (float)stage[4 * e] : rho - (float)rho0;
+    r.rux = rho * vx; r.ruy = rho * vy; r.ruz = rho * vz;
     if (!stokes) {
       r.sxx = vx * r.rux; r.sxy = vx * r.ruy; r.sxz = vx * r.ruz;
       r.syy = vy * r.ruy; r.syz = vy * r.ruz; r.szz = vz * r.ruz;

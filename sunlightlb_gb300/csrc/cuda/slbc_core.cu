@@ -199,12 +199,14 @@ __global__ void k_ads_links(const uint16_t *flags, const unsigned char *ads, uin
   links[x] = mask;
 }
 
-// Staging for k_setvel from three device FP32 velocity arrays (rho = rho0).
-__global__ void k_stage_velocity(const float *u, long long nnodes, long long x0, long long n, double *stage) {
+// Staging for k_setvel from three device FP32 velocity arrays and, if
+// given, the density deviations rho - rho0 (else rho = rho0).
+__global__ void k_stage_velocity(const float *u, const float *drho, long long nnodes, long long x0, long long n,
+                                 double *stage) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const long long x = x0 + e;
-  stage[4 * e] = 0.0;
+  stage[4 * e] = drho ? (double)drho[x] : 0.0;
   stage[4 * e + 1] = u[x];
   stage[4 * e + 2] = u[nnodes + x];
   stage[4 * e + 3] = u[2 * nnodes + x];
@@ -1241,29 +1243,35 @@ int slbc_set_velocity(slbc_lattice *h, const double *rho, const double *ux, cons
   return 0;
 }
 
-int slbc_get_velocity_dev(slbc_lattice *h, double fac, float *u) {
+int slbc_get_state_dev(slbc_lattice *h, double fac, float *u, float *drho) {
   Lattice &L = h->L;
-  if (no_bf16(L, "slbc_get_velocity_dev")) return 1;
-  if (!u) return fail_msg("slbc_get_velocity_dev: null output");
-  CK(DISPATCH(L, launch_velocity, L, fac, u));
+  if (no_bf16(L, "slbc_get_state_dev")) return 1;
+  if (!u) return fail_msg("slbc_get_state_dev: null output");
+  CK(DISPATCH(L, launch_velocity, L, fac, u, drho));
   return 0;
 }
 
-int slbc_set_velocity_dev(slbc_lattice *h, const float *u, int skip_solid) {
+int slbc_get_velocity_dev(slbc_lattice *h, double fac, float *u) { return slbc_get_state_dev(h, fac, u, nullptr); }
+
+int slbc_set_state_dev(slbc_lattice *h, const float *u, const float *drho, int skip_solid) {
   Lattice &L = h->L;
   L.state_version++;
-  if (!u) return fail_msg("slbc_set_velocity_dev: null input");
+  if (!u) return fail_msg("slbc_set_state_dev: null input");
   if (ensure_staging(L, L.nnodes, 4)) return 1;
   const long long chunk = L.staging_nodes / 4;
   for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {
     const long long n = std::min(chunk, L.nnodes - x0);
-    k_stage_velocity<<<blocks_for(n, 256), 256, 0, L.stream>>>(u, L.nnodes, x0, n, L.staging);
+    k_stage_velocity<<<blocks_for(n, 256), 256, 0, L.stream>>>(u, drho, L.nnodes, x0, n, L.staging);
     count_launch();
     CK(cudaGetLastError());
-    CK(DISPATCH3(L, launch_setvel, L, L.staging, x0, n, 0, skip_solid));
+    CK(DISPATCH3(L, launch_setvel, L, L.staging, x0, n, drho ? 2 : 0, skip_solid));
   }
   L.layout = SLBC_LAYOUT_N;
   return 0;
+}
+
+int slbc_set_velocity_dev(slbc_lattice *h, const float *u, int skip_solid) {
+  return slbc_set_state_dev(h, u, nullptr, skip_solid);
 }
 
 // ---- moment propagation ----------------------------------------------------

@@ -180,7 +180,7 @@ struct BatchState {
 
 #define SLBC_DECLARE_LAUNCHERS(SUFFIX)                                          \
   cudaError_t launch_batch_##SUFFIX(BatchState &B, int nsteps);                 \
-  cudaError_t launch_velocity_##SUFFIX(Lattice &L, double fac, float *u);        \
+  cudaError_t launch_velocity_##SUFFIX(Lattice &L, double fac, float *u, float *drho); \
   cudaError_t prepare_tiles_##SUFFIX(BatchState &B);                             \
   cudaError_t launch_tiles_##SUFFIX(BatchState &B, int step);                    \
   cudaError_t launch_step_##SUFFIX(Lattice &L, int odd);                        \

@@ -651,14 +651,16 @@ __global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long l
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const long long x = x0 + e;
-  const T r = has_rho ? (T)stage[4 * e] : (T)rho0;
+  // has_rho 1: stage[4e] is the density; 2: it is the deviation rho - rho0
+  // (kept exact in FP32, where rho0 + 1e-4 would lose most of it)
+  const T r = has_rho == 2 ? (T)rho0 + (T)stage[4 * e] : has_rho ? (T)stage[4 * e] : (T)rho0;
   const T vx = (T)stage[4 * e + 1], vy = (T)stage[4 * e + 2], vz = (T)stage[4 * e + 3];
   T t[15];
   if (skip_solid && (p.flags[x] & FLAG_SOLID)) {
 #pragma unroll
     for (int q = 0; q < 15; q++) t[q] = T(0);
   } else {
-    const T drho = r - (T)rho0, rux = r * vx, ruy = r * vy, ruz = r * vz;
+    const T drho = has_rho == 2 ? (T)stage[4 * e] : r - (T)rho0, rux = r * vx, ruy = r * vy, ruz = r * vz;
     T sxx = T(0), syy = T(0), szz = T(0), sxy = T(0), sxz = T(0), syz = T(0);
     if (!stokes) {
       sxx = vx * rux; sxy = vx * ruy; sxz = vx * ruz;
@@ -675,12 +677,12 @@ __global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long l
 // three FP32 arrays (the per-node form of the accvmean sum).
 template <typename T>
 __global__ void k_velocity(PopArgs<T> p, int layout, double rho0, double fac, int bf_uniform, double b0, double b1,
-                           double b2, const T *bf, float *u) {
+                           double b2, const T *bf, float *u, float *drho) {
   const long long n = (long long)p.esi * p.esj * p.esk;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     const int x = (int)e;
     const uint16_t fl = p.flags[x];
-    float ux = 0.f, uy = 0.f, uz = 0.f;
+    float ux = 0.f, uy = 0.f, uz = 0.f, dr = 0.f;
     if (!(fl & FLAG_SOLID)) {
       int i, j, k;
       decode(x, p.esj, p.esk, i, j, k);
@@ -700,10 +702,12 @@ __global__ void k_velocity(PopArgs<T> p, int layout, double rho0, double fac, in
       ux = (float)((mx + fac * bx) * inv);
       uy = (float)((my + fac * by) * inv);
       uz = (float)((mz + fac * bz) * inv);
+      dr = (float)r;
     }
     u[x] = ux;
     u[n + x] = uy;
     u[2 * n + x] = uz;
+    if (drho) drho[x] = dr;
   }
 }
 

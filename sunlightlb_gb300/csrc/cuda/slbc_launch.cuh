@@ -281,10 +281,10 @@ cudaError_t SLBC_FN(launch_setvel)(Lattice &L, const double *stage, long long x0
   return cudaGetLastError();
 }
 
-cudaError_t SLBC_FN(launch_velocity)(Lattice &L, double fac, float *u) {
+cudaError_t SLBC_FN(launch_velocity)(Lattice &L, double fac, float *u, float *drho) {
   const int blocks = (int)std::min<long long>((L.nnodes + 255) / 256, 152LL * 16);
   k_velocity<T_><<<blocks, 256, 0, L.stream>>>(pop_args(L), L.layout, L.par.rho0, fac, L.bf_uniform, L.bf_const[0],
-                                               L.bf_const[1], L.bf_const[2], (const T_ *)L.bf, u);
+                                               L.bf_const[1], L.bf_const[2], (const T_ *)L.bf, u, drho);
   count_launch();
   return cudaGetLastError();
 }

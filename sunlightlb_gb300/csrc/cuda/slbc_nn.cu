@@ -267,15 +267,15 @@ __global__ void k_scale(float *g, long long n, const double *state) {
     g[i] = sc == 0.0f ? 0.0f : g[i] * sc;
 }
 
-// loss = mean over voxels and the 3 components of (pred - label)^2, pred in
-// FP32 channels 0..2 of a padded buffer (ctot_p channels), label
-// [n][D][H][W][3] FP32; grad (BF16, gctot channels, padded) = d loss /
-// d pred in channels 0..2, 0 in the others.  loss[0] += the sum / count.
-__global__ void k_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H,
-                      int W, bf16 *grad, int gctot, double *loss) {
+// loss = mean over voxels and the nch components of (pred - label)^2, pred
+// in FP32 channels 0..nch-1 of a padded buffer (ctot_p channels), label
+// [n][D][H][W][nch] FP32; grad (BF16, gctot channels, padded) = d loss /
+// d pred in channels 0..nch-1, 0 in the others.  loss[0] += the sum / count.
+__global__ void k_mse(const float *pred, int ctot_p, const float *label, int nch, const float *sample_w, int B, int D,
+                      int H, int W, bf16 *grad, int gctot, double *loss) {
   __shared__ double sh[256];
   const long long total = (long long)B * D * H * W;
-  const double inv = 1.0 / (3.0 * (double)total);
+  const double inv = 1.0 / ((double)nch * (double)total);
   double acc = 0.0;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -287,9 +287,8 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, const f
     const float sw = sample_w ? sample_w[n] : 1.0f;
     bf16 *gp = grad + v * gctot;
     for (int c = 0; c < gctot; c += 8) *(uint4 *)(gp + c) = make_uint4(0, 0, 0, 0);
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float d = pred[v * ctot_p + c] - label[e * 3 + c];
+    for (int c = 0; c < nch; c++) {
+      const float d = pred[v * ctot_p + c] - label[e * nch + c];
       acc += (double)sw * d * d;
       gp[c] = __float2bfloat16((float)(2.0 * inv) * sw * d);
     }
@@ -364,9 +363,10 @@ __global__ void k_encode(const unsigned char *solid, const unsigned char *dist2,
 
 // prediction (FP32 channels 0..2 of a padded buffer) * scale on fluid
 // nodes into three FP32 arrays u[c * N + e] (0 on solid nodes), the layout
-// of lbsetveldev; shift_x is subtracted from u_x on fluid nodes
+// of lbsetveldev; shift_x is subtracted from u_x on fluid nodes.  With
+// drho, channel 3 * drho_scale into drho[e] (0 on solid nodes).
 __global__ void k_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                         float shift_x, float *u) {
+                         float shift_x, float *u, float drho_scale, float *drho) {
   const long long total = (long long)D * H * W;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -376,6 +376,7 @@ __global__ void k_decode(const float *pred, int ctot_p, const unsigned char *sol
     const long long v = vox(0, z, y, x, D, H, W);
 #pragma unroll
     for (int c = 0; c < 3; c++) u[c * total + e] = solid[e] ? 0.0f : scale * pred[v * ctot_p + c] - (c == 0 ? shift_x : 0.0f);
+    if (drho) drho[e] = solid[e] ? 0.0f : drho_scale * pred[v * ctot_p + 3];
   }
 }
 
@@ -491,11 +492,11 @@ int slbc_nn_scale(float *g, long long n, const double *state, void *stream) {
   return launched("slbc_nn_scale");
 }
 
-int slbc_nn_mse(const float *pred, int ctot_p, const float *label, const float *sample_w, int B, int D, int H, int W,
-                void *grad, int gctot, double *loss, void *stream) {
-  if (ctot_p < 3 || gctot % 8 || gctot < 8) return bad("slbc_nn_mse: bad channel counts");
+int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int nch, const float *sample_w, int B, int D, int H,
+                int W, void *grad, int gctot, double *loss, void *stream) {
+  if (nch < 1 || ctot_p < nch || gctot % 8 || gctot < 8 || gctot < nch) return bad("slbc_nn_mse: bad channel counts");
   k_mse<<<std::min(grid_for((long long)B * D * H * W), 152 * 4), 256, 0, (cudaStream_t)stream>>>(
-      pred, ctot_p, label, sample_w, B, D, H, W, (bf16 *)grad, gctot, loss);
+      pred, ctot_p, label, nch, sample_w, B, D, H, W, (bf16 *)grad, gctot, loss);
   return launched("slbc_nn_mse");
 }
 
@@ -525,10 +526,10 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
 }
 
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
-                   float shift_x, float *u, void *stream) {
-  if (ctot_p < 3) return bad("slbc_nn_decode: bad channel count");
+                   float shift_x, float *u, float drho_scale, float *drho, void *stream) {
+  if (ctot_p < (drho ? 4 : 3)) return bad("slbc_nn_decode: bad channel count");
   k_decode<<<grid_for((long long)D * H * W), 256, 0, (cudaStream_t)stream>>>(pred, ctot_p, solid, D, H, W, scale,
-                                                                                       shift_x, u);
+                                                                                       shift_x, u, drho_scale, drho);
   return launched("slbc_nn_decode");
 }
 

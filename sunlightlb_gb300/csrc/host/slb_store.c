@@ -206,12 +206,27 @@ void lbsetveldev(LBSys lb, void *u) {
 }
 
 /* appended: the velocity field into three device FP32 arrays, with the
- * half-force correction accvmean applies when lb->vel_corrected */
-void lbvelocity(LBSys lb, void *u) {
+ * half-force correction accvmean applies when lb->vel_corrected, and with
+ * lbstate the density deviation of every fluid node */
+void lbstate(LBSys lb, void *u, void *drho) {
   double fac = 0.0;
   if (lb->vel_corrected) fac = lb->status == POST_PROPAGATE ? 0.5 : -0.5;
   if (lb->changed_objects) syncobjs(lb);
-  slb_check(slbc_get_velocity_dev(slb_device(lb), fac, (float *)u), "velocity field");
+  slb_check(slbc_get_state_dev(slb_device(lb), fac, (float *)u, (float *)drho), "velocity field");
+}
+
+void lbvelocity(LBSys lb, void *u) { lbstate(lb, u, NULL); }
+
+/* appended: lbsetveldev with a device field of density deviations */
+void lbsetstatedev(LBSys lb, void *u, void *drho) {
+  if (lb->changed_objects) syncobjs(lb);
+  if (lb->rescale != 1.0) printf("lbsetstatedev: lb->rescale ignored (velocities used as given)\n");
+  slb_check(slbc_set_state_dev(slb_device(lb), (const float *)u, (const float *)drho, lb->skip_solid),
+            "state warm start");
+  slb_device_changed(lb);
+  lb->status = POST_PROPAGATE;
+  collide(lb);
+  lb->rescale = 1.0;
 }
 
 /* reference src/lbstore.c:305-404 */

@@ -33,7 +33,8 @@ from . import workloads as W
 
 ETA_TAU1 = 72.0 * (1.0 - 0.5) / 3.0   # rho0 (tau - 1/2) / 3 at tau = 1, rho0 = 72
 IN_CH = 32                             # input channels (channel 0 = solid mask)
-OUT_CH = 32                            # output channels (0..2 = velocity)
+OUT_CH = 32                            # output channels (0..2 = velocity, 3 = density when trained with it)
+DRHO_UNIT = 12.0                       # density labels: (rho - rho0) / (DRHO_UNIT * body force)
 
 
 class Kernels:
@@ -55,12 +56,12 @@ class Kernels:
             "slbc_nn_wfwd": [p, i, i, p, p],
             "slbc_nn_wdgrad": [p, i, i, i, i, p, p],
             "slbc_nn_adam": [p, p, p, p, ll, f, f, f, f, i, p],
-            "slbc_nn_mse": [p, i, p, p, i, i, i, i, p, i, p, p],
+            "slbc_nn_mse": [p, i, p, i, p, i, i, i, i, p, i, p, p],
             "slbc_nn_sqsum": [p, ll, p, p],
             "slbc_nn_clip": [p, f, f, p],
             "slbc_nn_scale": [p, ll, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
-            "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, p],
+            "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, f, p, p],
             "slbc_tc_status": [],
         }
         self.dll = dll
@@ -298,8 +299,9 @@ class UNet:
         k, G, X = self.k, self.grad, self.buf
         B, (w0, w1, w2, w3) = self.B, self.widths
         self.loss_acc.zero_()
-        k.nn_mse(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), sample_w.data_ptr() if sample_w is not None else None,
-                 B, self.D, self.H, self.W, G["gOUT"].data_ptr(), OUT_CH, self.loss_acc.data_ptr(), self.stream)
+        k.nn_mse(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), labels.shape[-1],
+                 sample_w.data_ptr() if sample_w is not None else None, B, self.D, self.H, self.W, G["gOUT"].data_ptr(),
+                 OUT_CH, self.loss_acc.data_ptr(), self.stream)
         self._halo("gOUT")
         # level 0 decoder
         self._wgrad("out", "gOUT", "D0")
@@ -390,12 +392,14 @@ def packing(side, phi, seed, r_range=(3.0, 8.0)):
     return W.rsa_packing(side, phi, r_range[0], r_range[1], seed, overlap=True)[1]
 
 
-def converged_flows(L, solids, force=1e-6, tol=1e-6, check=200, maxsteps=40000, chunk=256, precision=1):
+def converged_flows(L, solids, force=1e-6, tol=1e-6, check=200, maxsteps=40000, chunk=256, precision=1,
+                    density=False):
     """Steady Stokes flow of every packing (tau = 1, body force along x),
     advanced as batches of `chunk` lattices; a lattice leaves the batch once
     the relative change of its mean flow between checks is below tol.
     Returns (velocity fields as device FP32 tensors (3, N) in units of the
-    Darcy response q = u * eta / b, steps per lattice)."""
+    Darcy response q = u * eta / b, steps per lattice); with density a
+    fourth row holds the density deviation in units of DRHO_UNIT * b."""
     import torch
     fields, steps = [None] * len(solids), [0] * len(solids)
     for start in range(0, len(solids), chunk):
@@ -431,17 +435,24 @@ def converged_flows(L, solids, force=1e-6, tol=1e-6, check=200, maxsteps=40000, 
             active = still
         for i in idx:
             lb = lbs[i]
-            u = torch.empty(3 * lb.nnodes, device="cuda", dtype=torch.float32)
-            L.lbvelocity(lb, u.data_ptr())
+            u = torch.empty((4 if density else 3) * lb.nnodes, device="cuda", dtype=torch.float32)
+            if density:
+                L.lbstate(lb, u.data_ptr(), u[3 * lb.nnodes:].data_ptr())
+            else:
+                L.lbvelocity(lb, u.data_ptr())
             torch.cuda.synchronize()
-            fields[i] = u.view(3, lb.nnodes) * (ETA_TAU1 / force)
+            f = u.view(-1, lb.nnodes)
+            f[:3] *= ETA_TAU1 / force
+            if density:
+                f[3] *= 1.0 / (DRHO_UNIT * force)
+            fields[i] = f
             L.freelb(lb)
     return fields, steps
 
 
 def to_labels(field, shape):
-    """(3, N) -> (D, H, W, 3)."""
-    return field.view(3, *shape).permute(1, 2, 3, 0).contiguous()
+    """(C, N) -> (D, H, W, C)."""
+    return field.view(field.shape[0], *shape).permute(1, 2, 3, 0).contiguous()
 
 
 # ---- warm start -------------------------------------------------------------------
@@ -465,15 +476,33 @@ def predict_velocity(net, solid_u8, force, eta, rho0=72.0, force_shift=1.0):
     n = solid_u8.numel()
     u = torch.empty(3 * n, device="cuda", dtype=torch.float32)
     net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta,
-                    force_shift * force / rho0, u.data_ptr(), net.stream)
+                    force_shift * force / rho0, u.data_ptr(), 0.0, None, net.stream)
     return u
 
 
-def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-4, check=100, maxsteps=60000):
+def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5):
+    """Velocity (3 x N) and density deviation (N) device FP32 fields from a
+    network trained on labels with density (converged_flows(density=True)):
+    with its own density a converged state is rebuilt exactly from
+    u - F / (2 rho), so force_shift defaults to 1/2 here."""
+    import torch
+    net.encode(solid_u8.view(1, *solid_u8.shape))
+    out = net.forward()
+    n = solid_u8.numel()
+    u = torch.empty(3 * n, device="cuda", dtype=torch.float32)
+    drho = torch.empty(n, device="cuda", dtype=torch.float32)
+    net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta,
+                    force_shift * force / rho0, u.data_ptr(), DRHO_UNIT * force, drho.data_ptr(), net.stream)
+    return u, drho
+
+
+def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-4, check=100, maxsteps=60000,
+                     warm_drho=None):
     """Packed bed (device uint8 or numpy mask) until the relative change of
     the mean flow between checks is below tol (plain) or, given k_ref, until
     the permeability is within `rel` of k_ref; warm_u (device velocities,
-    lbsetveldev layout) warm-starts the lattice.  Returns the trajectory
+    lbsetveldev layout) warm-starts the lattice, with warm_drho (device
+    density deviations) through lbsetstatedev.  Returns the trajectory
     [(steps, k, wall seconds)] measured every `check` steps; the wall clock
     starts before the warm start."""
     import torch
@@ -489,7 +518,9 @@ def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-
     torch.cuda.synchronize()
     eta = lb.rho0 * (lb.tau - 0.5) / 3.0
     t0 = time.perf_counter()
-    if warm_u is not None:
+    if warm_u is not None and warm_drho is not None:
+        L.lbsetstatedev(lb, warm_u.data_ptr(), warm_drho.data_ptr())
+    elif warm_u is not None:
         L.lbsetveldev(lb, warm_u.data_ptr())
     steps, prev, traj = 0, None, []
     while steps < maxsteps:
@@ -569,12 +600,13 @@ def symmetry(mask, label, flip_x, flip_y, flip_z, swap_yz):
     if flip_z:
         dims.append(2)
         sign[2] = -sign[2]
+    extra = label.shape[-1] - 3  # a density channel is a scalar: unchanged
     if dims:
         mask, label = mask.flip(dims), label.flip(dims)
-    label = label * torch.tensor(sign, device=label.device, dtype=label.dtype)
+    label = label * torch.tensor(sign + [1.0] * extra, device=label.device, dtype=label.dtype)
     if swap_yz:
         mask = mask.transpose(1, 2)
-        label = label.transpose(1, 2)[..., [0, 2, 1]]
+        label = label.transpose(1, 2)[..., [0, 2, 1] + list(range(3, 3 + extra))]
     return mask.contiguous(), label.contiguous()
 
 

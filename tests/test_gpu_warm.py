@@ -227,3 +227,56 @@ def test_trained_network_beats_plain_start(gpu):
     plain_steps, warm_steps, plain_err, warm_err = (sum(c) for c in zip(*rows))
     assert warm_err < 0.5 * plain_err, rows
     assert warm_steps < 0.8 * plain_steps, rows
+
+
+def test_state_warm_start_rebuilds_converged_state(gpu):
+    """lbstate / lbsetstatedev: the velocity and density deviation of a
+    converged FP32 lattice, set back with u_x - F / (2 rho0) on fluid nodes,
+    give the converged permeability within 1e-4 after 10 steps; without a
+    density field lbsetstatedev equals lbsetveldev."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    n, force = 32, 1e-6
+    solid = WS.packing(n, 0.3, 21)
+    traj = WS.permeability_run(gpu, solid, force)
+    k = traj[-1][1]
+    def lattice():
+        lb = gpu.newlb(n, n, n, "null")
+        lb.precision = 1
+        lb.tau = 1.0
+        lb.stokes_flow = 1
+        WS.W.insert_solid(gpu, lb, solid)
+        gpu.syncobjs(lb)
+        gpu.addbf(lb, force, 0.0, 0.0)
+        gpu.lbsteps(lb, 2)
+        return lb
+
+    src = lattice()
+    gpu.lbsteps(src, traj[-1][0])
+    u = torch.empty(3 * n ** 3, device="cuda", dtype=torch.float32)
+    drho = torch.empty(n ** 3, device="cuda", dtype=torch.float32)
+    gpu.lbstate(src, u.data_ptr(), drho.data_ptr())
+    torch.cuda.synchronize()
+    gpu.freelb(src)
+    fluid = torch.as_tensor(~solid.reshape(-1), device="cuda")
+    assert float(drho[~fluid].abs().max()) == 0.0 and float(drho[fluid].abs().max()) > 0.0
+    us = u.clone()
+    us[:n ** 3][fluid] -= force / (2 * 72.0)
+    eta = 72.0 * 0.5 / 3.0
+
+    def k_after(set_state):
+        lb = lattice()
+        set_state(lb)
+        gpu.lbsteps(lb, 8)
+        gpu.measure(lb)
+        kk = lb.vmeanx * eta / force
+        gpu.lbpull(lb)
+        a = lb.array("a").copy()
+        gpu.freelb(lb)
+        return kk, a
+
+    k_state, _ = k_after(lambda lb: gpu.lbsetstatedev(lb, us.data_ptr(), drho.data_ptr()))
+    assert abs(k_state - k) <= 1e-4 * k, (k_state, k)
+    _, a_vel = k_after(lambda lb: gpu.lbsetveldev(lb, us.data_ptr()))
+    _, a_state0 = k_after(lambda lb: gpu.lbsetstatedev(lb, us.data_ptr(), None))
+    assert np.array_equal(a_vel, a_state0)
