@@ -216,3 +216,10 @@ def test_flow_symmetries_algebra():
         assert m2[where[bits]] == 1 and int(m2.sum()) == 1, bits
         m3, l3 = WS.symmetry(m2, l2, *bits)
         assert torch.equal(m3, m) and torch.equal(l3, lab), bits
+    # a density channel is a scalar: moved with the nodes, never negated or swapped
+    lab4 = torch.cat([lab, torch.full((4, 4, 4, 1), 5.0)], dim=-1)
+    lab4[0, 1, 2, 3] = 7.0
+    for bits in want:
+        m2, l2 = WS.symmetry(m, lab4, *bits)
+        assert torch.equal(l2[..., :3], WS.symmetry(m, lab, *bits)[1]), bits
+        assert float(l2[where[bits]][3]) == 7.0 and int((l2[..., 3] == 7.0).sum()) == 1, bits
