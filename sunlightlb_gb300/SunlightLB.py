@@ -27,4 +27,5 @@ POST_PROPAGATE = _binding.POST_PROPAGATE
 POST_COLLIDE = _binding.POST_COLLIDE
 SLB_FP64 = _binding.SLB_FP64
 SLB_FP32 = _binding.SLB_FP32
+SLB_BF16 = _binding.SLB_BF16
 PI = 3.14159265358979323846
