@@ -5,7 +5,8 @@ sunlightlb_gb300/warmstart.py runs on the tensor cores: the same layer
 list, periodic 3x3x3 convolutions (tap = 9 dz + 3 dy + dx for the neighbour
 offset (dx-1, dy-1, dz-1)), ReLU, 2x2x2 average pooling, nearest
 upsampling, channel concatenation (upsampled part first, skip part after),
-the mean-square loss over velocity channels 0..2, and the exact gradients
+the mean-square loss over the label channels (velocity 0..2, and the
+density deviation 3 when the labels carry it), and the exact gradients
 of all of it.  There is no counterpart in the reference (its lattice
 Boltzmann code has no learned part); the GPU gradients are checked against
 this.  Arrays are channels-last without halo: (B, D, H, W, C).
@@ -68,7 +69,8 @@ def relu(x):
 
 def forward_backward(params, inp, labels):
     """params: {layer: (w, b)} (float64), inp: (B, D, H, W, 32) input
-    encoding, labels: (B, D, H, W, 3).  Returns (loss, {layer: (dw, db)})."""
+    encoding, labels: (B, D, H, W, C), C = 3 or 4.  Returns (loss,
+    {layer: (dw, db)})."""
     P = params
     a = {}
     a["A0"] = relu(conv(inp, *P["e0a"]))
@@ -92,11 +94,12 @@ def forward_backward(params, inp, labels):
     e0 = relu(conv(c0, *P["d0a"]))
     d0 = relu(conv(e0, *P["d0b"]))
     out = conv(d0, *P["out"])
-    n = labels[..., 0].size * 3
-    diff = out[..., :3] - labels
+    nch = labels.shape[-1]
+    n = labels[..., 0].size * nch
+    diff = out[..., :nch] - labels
     loss = float((diff ** 2).sum() / n)
     g_out = np.zeros_like(out)
-    g_out[..., :3] = 2.0 * diff / n
+    g_out[..., :nch] = 2.0 * diff / n
     grads = {}
 
     def back(name, x, g, y=None):

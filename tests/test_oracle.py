@@ -11,6 +11,7 @@ examples must give the published numbers.
 import hashlib
 import json
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -121,3 +122,37 @@ def test_partial_adsorption_conserves_mass(orc):
         if P == 0.0:
             assert L.mptotal(mp, "adsorbed") == 0.0
         L.adnone(mp)
+
+
+def test_network_oracle_gradients_with_density_channel():
+    """The network oracle's exact gradients, with a fourth (density) label
+    channel, against central differences of its own loss (float64)."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import orc_unet
+    rng = np.random.default_rng(3)
+    w0 = w1 = w2 = w3 = 4
+    shapes = {"e0a": (4, w0), "e0b": (w0, w0), "e1a": (w0, w1), "e1b": (w1, w1), "e2a": (w1, w2),
+              "e2b": (w2, w2), "e3a": (w2, w3), "e3b": (w3, w3), "d2a": (w3 + w2, w2), "d2b": (w2, w2),
+              "d1a": (w2 + w1, w1), "d1b": (w1, w1), "d0a": (w1 + w0, w0), "d0b": (w0, w0), "out": (w0, 4)}
+    params = {k: (rng.normal(0, (2.0 / (27 * ci)) ** 0.5, (27, co, ci)), rng.normal(0, 0.1, co))
+              for k, (ci, co) in shapes.items()}
+    inp = (rng.random((1, 16, 16, 16, 4)) > 0.7).astype(np.float64)
+    labels = rng.normal(0, 1, (1, 16, 16, 16, 4))
+    loss, grads = orc_unet.forward_backward(params, inp, labels)
+    h = 1e-6
+    for name, idx in (("out", (13, 3, 2)), ("out", (0, 2, 1)), ("d0b", (5, 1, 2)), ("e0a", (26, 0, 0))):
+        w, b = params[name]
+        wp, wm = w.copy(), w.copy()
+        wp[idx] += h
+        wm[idx] -= h
+        lp, _ = orc_unet.forward_backward({**params, name: (wp, b)}, inp, labels)
+        lm, _ = orc_unet.forward_backward({**params, name: (wm, b)}, inp, labels)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - grads[name][0][idx]) <= 1e-5 * max(abs(fd), 1e-3), (name, idx, fd, grads[name][0][idx])
+    b = params["out"][1]
+    bp, bm = b.copy(), b.copy()
+    bp[3] += h
+    bm[3] -= h
+    lp, _ = orc_unet.forward_backward({**params, "out": (params["out"][0], bp)}, inp, labels)
+    lm, _ = orc_unet.forward_backward({**params, "out": (params["out"][0], bm)}, inp, labels)
+    assert abs((lp - lm) / (2 * h) - grads["out"][1][3]) <= 1e-6
