@@ -21,7 +21,9 @@ def oracle():
     return orc_unet
 
 
-def test_unet_gradients_match_cpu_oracle(gpu):
+@pytest.mark.parametrize("nch", [3, 4])
+def test_unet_gradients_match_cpu_oracle(gpu, nch):
+    """nch label channels: the velocity, and with 4 the density deviation."""
     torch = pytest.importorskip("torch")
     from sunlightlb_gb300 import warmstart as WS
     orc = oracle()
@@ -31,8 +33,9 @@ def test_unet_gradients_match_cpu_oracle(gpu):
     solid = (rng.random((B, D, H, W)) > 0.7).astype(np.uint8)
     zz, yy, xx = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
     lab = np.stack([np.sin(2 * np.pi * xx / W) * np.cos(2 * np.pi * yy / H),
-                    0.5 * np.cos(2 * np.pi * zz / D), 0.2 * np.sin(2 * np.pi * (xx + zz) / W)], axis=-1)
-    labels = np.broadcast_to(lab, (B, D, H, W, 3)) * (1 - solid[..., None])
+                    0.5 * np.cos(2 * np.pi * zz / D), 0.2 * np.sin(2 * np.pi * (xx + zz) / W),
+                    0.3 * np.cos(2 * np.pi * (yy + zz) / H)][:nch], axis=-1)
+    labels = np.broadcast_to(lab, (B, D, H, W, nch)) * (1 - solid[..., None])
     labels = np.ascontiguousarray(labels, dtype=np.float32)
     m_dev = torch.as_tensor(solid, device="cuda")
     l_dev = torch.as_tensor(labels, device="cuda")
