@@ -345,8 +345,9 @@ int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, in
  * every GPU loading the library keeps until the process exits; nblocks (the
  * number of reduction blocks) must lie in 1..SLBC_VSUM_NOALLOC_MAX_BLOCKS
  * and larger values are rejected with an error.  The first call on each
- * device looks up the array's device address; make that first call before
- * any stream capture.  Every call shares the array, so calls that overlap on
+ * device (and the first after a device reset, or with another CUDA context
+ * current on that device) looks up the array's device address; make that
+ * first call before any stream capture.  Every call shares the array, so calls that overlap on
  * the GPU (on different streams) race.  Work is queued on `stream` and not
  * synchronised. */
 #define SLBC_VSUM_NOALLOC_MAX_BLOCKS 1216

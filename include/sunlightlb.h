@@ -253,6 +253,7 @@ void mpslab(MPSys, LBReal, LBReal, LBReal, LBReal, LBReal, LBReal, LBReal); /* s
 void mpwall(MPSys, char *, int, LBReal);       /* src/mpobjs.c:75-117   */
 void mpsph(MPSys, LBReal, LBReal, LBReal, LBReal, LBReal); /* src/mpobjs.c:122-143 */
 void mpcyl(MPSys, char *, LBReal, LBReal, LBReal, LBReal); /* src/mpobjs.c:152-180 */
+void mpsubs(MPSys, char *, int, int, int, int, int, int, LBReal); /* src/mpobjs.c:188-226 */
 void mplist(MPSys, char *, LBReal);            /* src/mpobjs.c:233-261  */
 
 /* ---- Adsorption (reference src/mpads.c) ---- */

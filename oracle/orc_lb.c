@@ -804,6 +804,201 @@ void lbload(LBSys lb, char *loadfile) {
 }
 
 /* ------------------------------------------------------------------------
+ * field and object files: reference src/lbstore.c:227-296, 412-678 and
+ * src/lbmeasure.c:173-203.  Byte layouts and printf formats are the
+ * reference's (they define the file formats); the arithmetic of each value
+ * follows the reference's association.
+ * ---------------------------------------------------------------------- */
+
+/* fluid velocity of one node's populations plus fac times a force, with the
+ * density: reference src/lbstore.c:277-283 */
+static LBReal node_velocity(const LBSys lb, const LBReal *t, LBReal fac, LBReal gx, LBReal gy,
+                            LBReal gz, LBReal u[3]) {
+  LBReal rho = lb->rho0 + t[0] + t[1] + t[2] + t[3] + t[4] + t[5] + t[6] + t[7] + t[8] + t[9]
+               + t[10] + t[11] + t[12] + t[13] + t[14];
+  u[0] = (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14] + fac * gx) / rho;
+  u[1] = (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14] + fac * gy) / rho;
+  u[2] = (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14] + fac * gz) / rho;
+  return rho;
+}
+
+/* reference src/lbstore.c:227-296: the correction uses the node force
+ * arrays fx, fy, fz (as the reference does), and a solid node of a
+ * skip_solid lattice repeats the density of the node written before it */
+void lbsavevel(LBSys lb, char *savefile, char *type) {
+  int i, j, k, binary = (type[0] == 'b' || type[0] == 'B');
+  LBReal fac = 0.0, rho = 0.0, u[3];
+  FILE *fp = fopen(savefile, "w");
+  if (fp == NULL) { printf("savefile: %s could not be opened\n", savefile); return; }
+  if (lb->vel_corrected) {
+    if (lb->status == POST_PROPAGATE) fac = 0.5;
+    else if (lb->status == POST_COLLIDE) fac = -0.5;
+  }
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    long n = node(lb, i, j, k);
+    if (lb->obj[n] != NULL && lb->skip_solid) u[0] = u[1] = u[2] = 0.0;
+    else rho = node_velocity(lb, lb->a + 15 * n, fac, lb->fx[n], lb->fy[n], lb->fz[n], u);
+    if (binary) {
+      fwrite(&rho, sizeof(LBReal), 1, fp);
+      fwrite(u, sizeof(LBReal), 3, fp);
+    } else {
+      fprintf(fp, "%g %g %g %g %i %i %i\n", rho, u[0], u[1], u[2], i, j, k);
+    }
+  }
+  fclose(fp);
+}
+
+/* reference src/lbmeasure.c:173-203 */
+void vsave(LBSys lb, char *savefile) {
+  int i, j, k;
+  LBReal scale = 12.0 / lb->rho0, v[3];
+  FILE *fp = fopen(savefile, "w");
+  if (fp == NULL) { printf("savefile: %s could not be opened\n", savefile); return; }
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    long n = node(lb, i, j, k);
+    if (lb->obj[n] == NULL) { v[0] = lb->ux[n]; v[1] = lb->uy[n]; v[2] = lb->uz[n]; }
+    else if (lb->skip_solid) v[0] = v[1] = v[2] = 0.0;
+    else { v[0] = scale * lb->ux[n]; v[1] = scale * lb->uy[n]; v[2] = scale * lb->uz[n]; }
+    fprintf(fp, "%g %g %g %i %i %i\n", v[0], v[1], v[2], i, j, k);
+  }
+  fclose(fp);
+}
+
+/* the six stress moments of one node's populations: reference
+ * src/lbstore.c:446-458 */
+static void node_stress(const LBReal *t, LBReal s[6]) {
+  LBReal p12 = t[1] + t[2], p34 = t[3] + t[4], p56 = t[5] + t[6];
+  LBReal lo_sum = t[7] + t[8] + t[9] + t[10], hi_sum = t[11] + t[12] + t[13] + t[14];
+  LBReal lo_x = t[7] - t[8] + t[9] - t[10], hi_x = t[11] - t[12] + t[13] - t[14];
+  LBReal lo_y = t[7] + t[8] - t[9] - t[10], hi_y = t[11] + t[12] - t[13] - t[14];
+  LBReal lo_xy = t[7] - t[8] - t[9] + t[10], hi_xy = t[11] - t[12] - t[13] + t[14];
+  LBReal p06 = t[0] + p12 + p34 + p56, drho = p06 + (lo_sum + hi_sum);
+  LBReal sd = (2.0 / 3.0) * drho - p06;
+  s[0] = sd + p12; s[1] = sd + p34; s[2] = sd + p56;
+  s[3] = lo_xy + hi_xy; s[4] = lo_x - hi_x; s[5] = lo_y - hi_y;
+}
+
+/* reference src/lbstore.c:412-515: mean of the post-propagation and
+ * post-collision stress (one update step).  The binary form writes each
+ * LBReal with sizeof(LBStoreReal) bytes, as the reference does. */
+void lbsavestr(LBSys lb, char *savefile, char *type) {
+  long n, N = lb->nnodes;
+  int c, binary = (type[0] == 'b' || type[0] == 'B');
+  LBReal *acc = (LBReal *)zalloc(6 * N * sizeof(LBReal)), s[6];
+  FILE *fp;
+  bbl(lb); propagate(lb);
+  for (n = 0; n < N; n++) {
+    node_stress(lb->a + 15 * n, s);
+    for (c = 0; c < 6; c++) acc[6 * n + c] = s[c];
+  }
+  collide(lb);
+  for (n = 0; n < N; n++) {
+    node_stress(lb->a + 15 * n, s);
+    for (c = 0; c < 6; c++) acc[6 * n + c] += s[c];
+  }
+  if ((fp = fopen(savefile, "wb")) == NULL) { printf("savefile: %s could not be opened\n", savefile); free(acc); return; }
+  for (n = 0; n < N; n++) {
+    int fluid = lb->obj[n] == NULL;
+    for (c = 0; c < 6; c++) s[c] = (!fluid && lb->skip_solid) ? 0.0 : 0.5 * acc[6 * n + c];
+    if (binary) {
+      for (c = 0; c < 6; c++) fwrite(&s[c], sizeof(LBStoreReal), 1, fp);
+      fwrite(&fluid, sizeof(int), 1, fp);
+    } else {
+      fprintf(fp, "%f\t%f\t%f\t%f\t%f\t%f\t%i\n", s[0], s[1], s[2], s[3], s[4], s[5], fluid);
+    }
+  }
+  fclose(fp);
+  free(acc);
+}
+
+/* reference src/lbstore.c:523-545 */
+void lbsaveobj(LBSys lb, char *savefile) {
+  static const char *tag[5] = {"POS", "VEL", "ANG", "FRC", "TRQ"};
+  int console = myscmp("stdout", savefile) || myscmp("stderr", savefile), r;
+  FILE *fp = myscmp("stdout", savefile) ? stdout : myscmp("stderr", savefile) ? stderr : fopen(savefile, "w");
+  LBObj p;
+  if (fp == NULL) { printf("lbsaveobj: %s could not be opened\n", savefile); return; }
+  if (console) fprintf(fp, "START of particle data: TYPE, id, base id, x, y, z\n\n");
+  for (p = lb->obj_head; p != NULL; p = p->next_obj) {
+    LBReal v[5][3] = {{p->posx, p->posy, p->posz}, {p->velx, p->vely, p->velz},
+                      {p->angx, p->angy, p->angz}, {p->frcx, p->frcy, p->frcz},
+                      {p->trqx, p->trqy, p->trqz}};
+    for (r = 0; r < 5; r++)
+      fprintf(fp, "%s %3i %3i %f %f %f\n", tag[r], p->id, p->base_obj->id, v[r][0], v[r][1], v[r][2]);
+    if (console) fprintf(fp, "\n");
+  }
+  if (console) fprintf(fp, "END of particle data\n");
+  if (!console) fclose(fp);
+}
+
+/* reference src/lbstore.c:554-586: five records per object; positions as
+ * read, velocities and angular velocities times rescale (then reset) */
+void lbloadobj(LBSys lb, char *loadfile) {
+  int id, base, r;
+  float v[3];
+  FILE *fp = fopen(loadfile, "r");
+  LBObj p;
+  if (fp == NULL) { printf("lbloadobj: %s could not be opened\n", loadfile); return; }
+  while (fscanf(fp, "%*s%i%i%f%f%f", &id, &base, &v[0], &v[1], &v[2]) == 5) {
+    if ((p = lookupobj(lb, id)) == NULL) break;
+    if (base != id) {
+      if (lookupobj(lb, base) == NULL) break;
+      p->base_obj->id = base;
+    }
+    p->posx = v[0]; p->posy = v[1]; p->posz = v[2];
+    for (r = 1; r < 5; r++) {
+      if (fscanf(fp, "%*s%i%i%f%f%f", &id, &base, &v[0], &v[1], &v[2]) != 5) break;
+      if (r == 1) { p->velx = lb->rescale * v[0]; p->vely = lb->rescale * v[1]; p->velz = lb->rescale * v[2]; }
+      if (r == 2) { p->angx = lb->rescale * v[0]; p->angy = lb->rescale * v[1]; p->angz = lb->rescale * v[2]; }
+    }
+    if (r < 5) break;
+  }
+  fclose(fp);
+  lb->rescale = 1.0;
+}
+
+/* reference src/lbstore.c:595-640 */
+void lbsavefrc(LBSys lb, char *frcfile, char *type) {
+  int i, j, k;
+  FILE *fp = fopen(frcfile, "w");
+  if (fp == NULL) { printf("lbsavefrc: %s could not be opened\n", frcfile); exit(EXIT_FAILURE); }
+  if (type[0] == 'l' || type[0] == 'L') {
+    for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+      long n = node(lb, i, j, k);
+      LBObj p = lb->obj[n];
+      if (lb->mask[n] <= 0) continue;
+      fprintf(fp, "%i %i %i %f %f %f %i %f %f %f\n", i, j, k, lb->fx[n], lb->fy[n], lb->fz[n],
+              p->id, p->posx, p->posy, p->posz);
+    }
+  } else {
+    long n;
+    int binary = (type[0] == 'b' || type[0] == 'B');
+    for (n = 0; n < lb->nnodes; n++) {
+      LBStoreReal f[3];
+      f[0] = (LBStoreReal)lb->fx[n]; f[1] = (LBStoreReal)lb->fy[n]; f[2] = (LBStoreReal)lb->fz[n];
+      if (binary) fwrite(f, sizeof(LBStoreReal), 3, fp);
+      else fprintf(fp, "%f %f %f\n", f[0], f[1], f[2]);
+    }
+  }
+  fclose(fp);
+}
+
+/* reference src/lbstore.c:647-678 */
+void lbsavemap(LBSys lb, char *mapfile, char *type) {
+  FILE *fp = fopen(mapfile, "w");
+  if (fp == NULL) { printf("lbsavemap: %s could not be opened\n", mapfile); exit(EXIT_FAILURE); }
+  if (type[0] == 'l' || type[0] == 'L') {
+    int i, j, k;
+    for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++)
+      if (lb->obj[node(lb, i, j, k)] != NULL) fprintf(fp, "%i %i %i\n", i, j, k);
+  } else {
+    long n;
+    for (n = 0; n < lb->nnodes; n++) fputc(lb->obj[n] == NULL ? 0 : 255, fp);
+  }
+  fclose(fp);
+}
+
+/* ------------------------------------------------------------------------
  * appended helpers so drivers written for the GPU library run unchanged
  * ---------------------------------------------------------------------- */
 

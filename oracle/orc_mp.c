@@ -345,6 +345,27 @@ void mpcyl(MPSys mp, char *type, LBReal rad, LBReal a, LBReal b, LBReal pval) {
   }
 }
 
+/* reference src/mpobjs.c:188-226: a byte image of the region
+ * (ilo..ihi, jlo..jhi, klo..khi) inclusive, k fastest; a fluid node gets
+ * pval * byte / 255.  When the data run out, the rest of that k-row is
+ * skipped and every later row tries (and fails) again, as in the
+ * reference, whose break leaves only the innermost loop. */
+void mpsubs(MPSys mp, char *subsfile, int ilo, int ihi, int jlo, int jhi, int klo, int khi, LBReal pval) {
+  LBSys lb = mp->lb;
+  int i, j, k;
+  unsigned char byte;
+  FILE *fp = fopen(subsfile, "r");
+  if (fp == NULL) { printf("mpsubs: %s could not be opened\n", subsfile); return; }
+  for (i = ilo; i <= ihi; i++)
+    for (j = jlo; j <= jhi; j++)
+      for (k = klo; k <= khi; k++) {
+        long n = node(lb, i, j, k);
+        if (fscanf(fp, "%c", &byte) != 1) break;
+        if (lb->obj[n] == NULL) mp->p[n] = pval * (double)byte / 255.0;
+      }
+  fclose(fp);
+}
+
 void mplist(MPSys mp, char *file, LBReal pval) {
   LBSys lb = mp->lb;
   int i, j, k;

@@ -125,6 +125,7 @@ PROTOS = {
     "mpcopy": ("v", "MM"), "mpspread": ("d", "Ms"),
     "mpall": ("v", "Md"), "mpslab": ("v", "Mddddddd"), "mpwall": ("v", "Msid"),
     "mpsph": ("v", "Mddddd"), "mpcyl": ("v", "Msdddd"), "mplist": ("v", "Msd"),
+    "mpsubs": ("v", "Msiiiiiid"),
     "adall": ("v", "M"), "adnone": ("v", "M"), "adslab": ("v", "Mdddddd"),
     "adsph": ("v", "Mdddd"), "adcyl": ("v", "Msddd"), "adtotal": ("d", "Msi"),
     "adzero": ("v", "M"),
@@ -214,7 +215,8 @@ class LBSys(_Proxy):
 
     def pops(self):
         """Copy of the populations, shape (nnodes, 15), reference order."""
-        self._lib.call("lbpull", self)
+        if self._lib.has("lbpull"):  # a build of the reference keeps a on the host
+            self._lib.call("lbpull", self)
         return self.array("a").copy()
 
     def objects(self):

@@ -113,10 +113,13 @@ def build_oracle(with_reference=True, verbose=False):
     sources are present, oracle/_ref (test infrastructure only)."""
     odir = os.path.join(ROOT, "oracle")
     targets = ["all"]
-    ref_src = "/root/reference/src"
+    # the reference's checkout ($SLB_REFERENCE, default /root/reference);
+    # oracle/_ref is built only where its sources exist
+    ref_src = os.path.join(os.environ.get("SLB_REFERENCE", "/root/reference"), "src")
     if with_reference and os.path.isdir(ref_src):
         targets.append("ref")
-    r = subprocess.run(["make", "-s", "-C", odir] + targets, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    r = subprocess.run(["make", "-s", "-C", odir, "REF_SRC=" + ref_src] + targets,
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if verbose or r.returncode != 0:
         sys.stdout.write(r.stdout.decode(errors="replace"))
     if r.returncode != 0:

@@ -27,10 +27,45 @@ constexpr int kMaxDevices = 64;
 // same call first, so nothing needs clearing between calls.
 static __device__ __align__(256) double g_vsum_scratch[5 * kMaxBlocks];
 
-// Device address of g_vsum_scratch on each device (the host-side name is only
-// a stand-in and must never be passed to a kernel).
-void *g_scratch_addr[kMaxDevices];
+// Device address of g_vsum_scratch, cached per device together with the id
+// of the CUDA context it was looked up in (the host-side name is only a
+// stand-in and must never be passed to a kernel).  Context ids are unique for
+// the life of the process, so after a cudaDeviceReset, or with another
+// context bound on the same device, the address is looked up again instead
+// of reusing one from a context that no longer exists.
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  void *addr;
+};
+ScratchEntry g_scratch[kMaxDevices];
 std::mutex g_scratch_lock;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry-point
+// query, so the library needs no link-time dependency on libcuda.
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+bool current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+  }
+  if (get_current == nullptr || get_id == nullptr) return false;
+  void *ctx = nullptr;
+  if (get_current(&ctx) != 0 || ctx == nullptr) return false;
+  return get_id(ctx, id) == 0;
+}
 
 int scratch_for_current_device(double **out) {
   int dev = 0;
@@ -44,16 +79,21 @@ int scratch_for_current_device(double **out) {
     return 1;
   }
   std::lock_guard<std::mutex> guard(g_scratch_lock);
-  if (g_scratch_addr[dev] == nullptr) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_vsum_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      slbc::set_error(std::string("slbc_vsum_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return 1;
-    }
-    g_scratch_addr[dev] = p;
+  unsigned long long ctx = 0;
+  if (g_scratch[dev].addr != nullptr && current_context_id(&ctx) && ctx == g_scratch[dev].ctx_id) {
+    *out = (double *)g_scratch[dev].addr;
+    return 0;
   }
-  *out = (double *)g_scratch_addr[dev];
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_vsum_scratch);  // makes the device's primary context current if none is
+  if (e != cudaSuccess || p == nullptr) {
+    slbc::set_error(std::string("slbc_vsum_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    return 1;
+  }
+  // cache only what can be validated later; otherwise look it up every call
+  g_scratch[dev].addr = current_context_id(&ctx) ? p : nullptr;
+  g_scratch[dev].ctx_id = ctx;
+  *out = (double *)p;
   return 0;
 }
 

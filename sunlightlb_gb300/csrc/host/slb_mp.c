@@ -303,6 +303,44 @@ void mpcyl(MPSys mp, char *type, LBReal rad, LBReal a, LBReal b, LBReal pval) {
   mptrace(mp, "mpcyl");
 }
 
+/* reference src/mpobjs.c:188-226: a byte image of the region (ilo..ihi,
+ * jlo..jhi, klo..khi) inclusive, k fastest, read on the host; a fluid node
+ * gets pval * byte / 255.  When the data run out the rest of that k-row is
+ * skipped and each later row reports it again, as the reference's break
+ * (which leaves only the innermost loop) does.  Nodes outside the lattice
+ * use up their byte and are left alone. */
+void mpsubs(MPSys mp, char *subsfile, int ilo, int ihi, int jlo, int jhi, int klo, int khi, LBReal pval) {
+  int i, j, k, ns = 0;
+  unsigned char byte;
+  LBReal ptot = 0.0, val;
+  FILE *fp;
+  LBSys lb = mp->lb;
+  if ((fp = fopen(subsfile, "r")) == NULL) { printf("mpsubs: %s could not be opened\n", subsfile); return; }
+  if (slb_verbosity & MP_OBJECT_DETAILS) {
+    printf("\nInserting mp substrate data from %s\n", subsfile);
+    printf("Substrate region is (%i-%i,%i-%i,%i-%i) inclusive\n", ilo, ihi, jlo, jhi, klo, khi);
+  }
+  mppull(mp);
+  for (i = ilo; i <= ihi; i++)
+    for (j = jlo; j <= jhi; j++)
+      for (k = klo; k <= khi; k++) {
+        long x = slb_node(lb, i, j, k);
+        if (fscanf(fp, "%c", &byte) != 1) { printf("mpsubs: ran out of data in %s\n", subsfile); break; }
+        if (i < 0 || i >= lb->esi || j < 0 || j >= lb->esj || k < 0 || k >= lb->esk) continue;
+        if (lb->obj[x] == NULL) {
+          val = pval * (double)byte / 255.0;
+          mp->p[x] = val; ns++; ptot += val;
+        }
+      }
+  fclose(fp);
+  mppush(mp);
+  if (slb_verbosity & MP_OBJECT_DETAILS) {
+    printf("Inserted mp substrate field, %i sites set\n", ns);
+    printf("Total amount of added material is %f\n", ptot);
+  }
+  mptrace(mp, "mpsubs");
+}
+
 /* reference src/mpobjs.c:233-261: a node list is read on the host, the
  * field is updated there and sent back. */
 void mplist(MPSys mp, char *file, LBReal pval) {

@@ -587,23 +587,27 @@ def symmetry(mask, label, flip_x, flip_y, flip_z, swap_yz):
     body force along x, applied to a mask (D, H, W) over (x, y, z) and its
     steady flow (D, H, W, 3).  Reflecting y (or z) negates u_y (u_z);
     swapping y and z swaps u_y and u_z; reflecting x reverses the force, so
-    by linearity of Stokes flow the flow of the reflected bed is the
-    reflected flow with u_x kept and u_y, u_z negated."""
+    by linearity of Stokes flow the solution of the reflected bed is the
+    reflected solution negated as a whole: u_x kept, u_y and u_z negated,
+    and a density (pressure) channel after the three velocity components
+    negated too.  Other transforms move the density with the nodes."""
     import torch
     dims, sign = [], [1.0, 1.0, 1.0]
+    extra = label.shape[-1] - 3
+    scalar_sign = 1.0
     if flip_x:
         dims.append(0)
         sign[1], sign[2] = -sign[1], -sign[2]
+        scalar_sign = -1.0
     if flip_y:
         dims.append(1)
         sign[1] = -sign[1]
     if flip_z:
         dims.append(2)
         sign[2] = -sign[2]
-    extra = label.shape[-1] - 3  # a density channel is a scalar: unchanged
     if dims:
         mask, label = mask.flip(dims), label.flip(dims)
-    label = label * torch.tensor(sign + [1.0] * extra, device=label.device, dtype=label.dtype)
+    label = label * torch.tensor(sign + [scalar_sign] * extra, device=label.device, dtype=label.dtype)
     if swap_yz:
         mask = mask.transpose(1, 2)
         label = label.transpose(1, 2)[..., [0, 2, 1] + list(range(3, 3 + extra))]

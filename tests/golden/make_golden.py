@@ -3,7 +3,9 @@
 Run where the reference sources exist (they are compiled by oracle/Makefile
 into oracle/_ref/):
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [--files-only]
+
+(the reference checkout is $SLB_REFERENCE, default /root/reference).
 
 Two reference builds are driven through the same C API calls as the GPU
 library:
@@ -20,6 +22,8 @@ Fixtures (JSON):
   kat.json          known-answer runs of the reference's examples and the
                     plain-method convergence case
   rcp144.json       the 144-sphere packing of examples/rcp_spheres.dat
+  files.json        digests of the field, force, map, object and stress
+                    files, of lattices reloaded from them, and of mpsubs
 """
 
 import hashlib
@@ -37,7 +41,9 @@ sys.path.insert(0, os.path.dirname(HERE))
 from sunlightlb_gb300.binding import Library  # noqa: E402
 import scenarios as S  # noqa: E402
 
-REF_EXAMPLES = "/root/reference/examples"
+# the reference's checkout: SLB_REFERENCE overrides the default location
+REF_ROOT = os.environ.get("SLB_REFERENCE", "/root/reference")
+REF_EXAMPLES = os.path.join(REF_ROOT, "examples")
 
 
 def digest(arr):
@@ -222,8 +228,42 @@ def sphere_converge(L, n=32, rad=4.5, force=1e-5, tol=1e-8, maxsteps=60000, stop
             "discrf": L.discrf(lb), "vmeanx_at_2000": history[19] if len(history) >= 20 else None}
 
 
+FILE_CASES = {
+    "moving": dict(),
+    "skip_ns": dict(skip=1, stokes=0, tau=0.6),
+}
+
+
+def file_records(L):
+    """SHA-256 of every file the reference's file API writes for each file
+    case, of the populations after reloading the velocity files, of the
+    object table after reloading the object file, and of the tracer after
+    mpsubs and moment-propagation steps."""
+    import tempfile
+    out = {}
+    for name, cfg in FILE_CASES.items():
+        d = tempfile.mkdtemp()
+        _, files = S.file_case(L, d, **cfg)
+        rec = {"files": {k: hashlib.sha256(v).hexdigest() for k, v in files.items()}}
+        for kind in ("vel.bin", "vel.txt", "obj.txt"):
+            rec["reload_" + kind] = digest(S.reload_case(L, d, kind, **cfg)[1])
+        out[name] = rec
+    d = tempfile.mkdtemp()
+    p0, p1 = S.mpsubs_case(L, d)
+    out["mpsubs"] = {"p_injected": digest(p0), "p_after_steps": digest(p1)}
+    return out
+
+
+def write_files_fixture(strict):
+    with open(os.path.join(HERE, "files.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": file_records(strict)}, f, indent=1)
+
+
 def main():
     ref_dir = os.path.join(ROOT, "oracle", "_ref")
+    if "--files-only" in sys.argv:
+        write_files_fixture(Library(os.path.join(ref_dir, "libref_strict.so"), extended=False))
+        return
     REF_STRICT = os.path.join(ref_dir, "libref_strict.so")
     REF_SHIPPED = os.path.join(ref_dir, "libref_shipped.so")
     strict = Library(REF_STRICT, extended=False)
@@ -250,6 +290,7 @@ def main():
         json.dump({"generator": "tests/golden/make_golden.py", "cases": out["lb"]}, f, indent=1)
     with open(os.path.join(HERE, "mp_cases.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": out["mp"]}, f, indent=1)
+    write_files_fixture(strict)
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "kat": kat}, f, indent=1)
     print(json.dumps(kat, indent=1))

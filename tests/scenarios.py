@@ -63,3 +63,103 @@ def couette(L, h=10, vel1=0.11, vel2=-0.07, tau=0.8, steps=5000, precision=0):
     L.measure(lb)
     eta = lb.rho0 * (lb.tau - 0.5) / 3.0
     return lb, w1, w2, 2 * eta * (vel1 - vel2) / h
+
+
+FILE_OUTPUTS = (
+    ("vel.bin", "lbsavevel", "binary"), ("vel.txt", "lbsavevel", "ascii"),
+    ("frc.bin", "lbsavefrc", "binary"), ("frc.txt", "lbsavefrc", "ascii"), ("frc.lst", "lbsavefrc", "list"),
+    ("map.lst", "lbsavemap", "list"), ("map.chr", "lbsavemap", "char"),
+    ("obj.txt", "lbsaveobj", None), ("vsave.txt", "vsave", None),
+    ("str.bin", "lbsavestr", "binary"), ("str.txt", "lbsavestr", "ascii"),
+)
+
+
+def write_files(L, lb, outdir):
+    """Write every field and object file of the reference's file API
+    (src/lbstore.c:227-678, src/lbmeasure.c:129-203) from lb into outdir, in
+    a fixed order (lbsavestr advances the lattice one step, so it comes
+    last); returns {file name: bytes}.  vsave writes the field that vzero and
+    two vgrab calls (pre- and post-collision of one more step) accumulate."""
+    import os
+    out = {}
+    for name, fn, typ in FILE_OUTPUTS:
+        path = os.path.join(outdir, name)
+        if fn == "vsave":
+            L.vzero(lb)
+            L.vgrab(lb, 0.5)
+            L.bbl(lb); L.propagate(lb)
+            L.vgrab(lb, 0.5)
+            L.collide(lb)
+            L.vsave(lb, path)
+        elif typ is None:
+            L.call(fn, lb, path)
+        else:
+            L.call(fn, lb, path, typ)
+        with open(path, "rb") as f:
+            out[name] = f.read()
+    return out
+
+
+def file_case(L, outdir, dims=(9, 10, 11), steps=12, moving=1, skip=0, stokes=1, tau=0.8):
+    """A lattice with two spheres (moving walls by default), stepped and
+    measured so that node forces exist, then written to every file type."""
+    lb = two_spheres(L, dims=dims, steps=steps, moving=moving, skip=skip, stokes=stokes, tau=tau)
+    return lb, write_files(L, lb, outdir)
+
+
+def reload_case(L, files_dir, kind, dims=(9, 10, 11), moving=1, skip=0, stokes=1, tau=0.8):
+    """A fresh lattice of the same geometry loaded from a written file:
+    kind 'vel.bin' / 'vel.txt' through lbloadvel (then 3 steps), or
+    'obj.txt' through lbloadobj (object positions and velocities)."""
+    import os
+    lb = two_spheres(L, dims=dims, steps=0, moving=moving, skip=skip, stokes=stokes, tau=tau, measure=False)
+    path = os.path.join(files_dir, kind)
+    if kind.startswith("vel"):
+        lb.rescale = 0.75
+        L.lbloadvel(lb, path, "binary" if kind.endswith(".bin") else "ascii")
+        for _ in range(3):
+            L.lbstep(lb)
+        return lb, lb.pops()
+    for o in lb.objects():
+        o.posx = o.posy = o.posz = o.velx = o.angz = 0.0
+    lb.rescale = 2.0
+    L.lbloadobj(lb, path)
+    return lb, objects_state(lb)
+
+
+def objects_state(lb):
+    return np.array([[o.id, o.base_obj.contents.id, o.posx, o.posy, o.posz, o.velx, o.vely, o.velz,
+                      o.angx, o.angy, o.angz] for o in lb.objects()])
+
+
+def mpsubs_case(L, outdir, n=10, steps=15):
+    """Tracer set from a byte image by mpsubs over a sub-region (one run of
+    data shorter than the region, so the short-data rows are exercised),
+    then moment-propagation steps on a live flow."""
+    import os
+    lb = L.newlb(n, n + 1, n + 2, "null")
+    lb.tau = 0.7
+    L.insertsph(lb, 2.5, 4.5, 5.0, 6.0)
+    L.addbf(lb, 1e-3, 2e-4, 0)
+    for _ in range(6):
+        L.lbstep(lb)
+    mp = L.newmp(lb, "null")
+    mp.alpha = 0.25
+    L.mpinit(mp)
+    region = (1, 7, 2, 9, 0, 11)
+    count = (7 * 8 * 12) - 30  # the last 2.5 k-rows of the region get no data
+    data = bytes((37 * i + 11) % 256 for i in range(count))
+    path = os.path.join(outdir, "subs.dat")
+    with open(path, "wb") as f:
+        f.write(data)
+    L.mpsubs(mp, path, *region, 0.8)
+    if L.has("mppull"):
+        L.mppull(mp)
+    p0 = mp.field().copy()
+    for s in range(steps):
+        L.mpstep(mp)
+        if s % 3 == 2:
+            L.lbstep(lb)
+    if L.has("mppull"):
+        L.mppull(mp)
+    return p0, mp.field().copy()

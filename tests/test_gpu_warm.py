@@ -185,17 +185,22 @@ def test_symmetries_map_flows_to_flows(gpu):
     solid = WS.packing(n, 0.25, 11)
     cases = [(1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 0), (0, 0, 0, 1), (1, 1, 0, 1), (1, 1, 1, 1)]
     m0 = torch.as_tensor(solid.astype(np.uint8), device="cuda")
-    (f0,), _ = WS.converged_flows(gpu, [solid], tol=1e-11, maxsteps=40000, precision=0)
+    (f0,), _ = WS.converged_flows(gpu, [solid], tol=1e-11, maxsteps=40000, precision=0, density=True)
     l0 = WS.to_labels(f0, (n, n, n))
+    assert l0.shape[-1] == 4
     moved = [WS.symmetry(m0, l0, *c) for c in cases]
     fields, _ = WS.converged_flows(gpu, [m.cpu().numpy().astype(bool) for m, _ in moved], tol=1e-11, maxsteps=40000,
-                                   precision=0)
-    scale = float(l0.abs().max())
-    side = float(l0[..., 1:].abs().max())
+                                   precision=0, density=True)
+    scale = float(l0[..., :3].abs().max())
+    side = float(l0[..., 1:3].abs().max())
+    dscale = float(l0[..., 3].abs().max())
     assert side > 0.05 * scale  # the transverse components are not negligible
+    assert dscale > 0.0
     for c, (m, l), f in zip(cases, moved, fields):
         got = WS.to_labels(f, (n, n, n))
-        assert float((got - l).abs().max()) <= 1e-6 * scale, c
+        assert float((got[..., :3] - l[..., :3]).abs().max()) <= 1e-6 * scale, c
+        # the density channel at its own scale: a wrong sign shows as 2x
+        assert float((got[..., 3] - l[..., 3]).abs().max()) <= 1e-5 * dscale, c
 
 
 def test_trained_network_beats_plain_start(gpu):

@@ -151,17 +151,6 @@ def test_insertsph_bounding_box_equals_full_scan(gpu, orc):
         assert res[0][0] == res[1][0] and np.array_equal(res[0][1], res[1][1]) and res[0][2] == res[1][2]
 
 
-def test_struct_layout_shared_with_reference():
-    """The fields a SWIG driver sees sit at the reference's offsets; the
-    appended fields come after next_id."""
-    from sunlightlb_gb300.binding import LBSysBase, LBSysExt, MPSysBase, MPSysExt
-    for f, _ in LBSysBase._fields_:
-        assert getattr(LBSysBase, f).offset == getattr(LBSysExt, f).offset
-    assert LBSysExt.precision.offset >= LBSysBase.next_id.offset + 4
-    for f, _ in MPSysBase._fields_:
-        assert getattr(MPSysBase, f).offset == getattr(MPSysExt, f).offset
-
-
 def test_device_call_without_gpu_fails_loudly(gpu):
     """No CPU path: without a CUDA device the first device call exits with
     the reference's fatal-error convention and a clear message."""
@@ -216,10 +205,16 @@ def test_flow_symmetries_algebra():
         assert m2[where[bits]] == 1 and int(m2.sum()) == 1, bits
         m3, l3 = WS.symmetry(m2, l2, *bits)
         assert torch.equal(m3, m) and torch.equal(l3, lab), bits
-    # a density channel is a scalar: moved with the nodes, never negated or swapped
+    # a density channel moves with the nodes; the x reflection reverses the
+    # force, so by Stokes linearity the whole solution -- the density
+    # deviation included -- is negated; no other transform changes its sign
     lab4 = torch.cat([lab, torch.full((4, 4, 4, 1), 5.0)], dim=-1)
     lab4[0, 1, 2, 3] = 7.0
     for bits in want:
         m2, l2 = WS.symmetry(m, lab4, *bits)
+        s = -1.0 if bits[0] else 1.0
         assert torch.equal(l2[..., :3], WS.symmetry(m, lab, *bits)[1]), bits
-        assert float(l2[where[bits]][3]) == 7.0 and int((l2[..., 3] == 7.0).sum()) == 1, bits
+        assert float(l2[where[bits]][3]) == 7.0 * s and int((l2[..., 3] == 7.0 * s).sum()) == 1, bits
+        assert int((l2[..., 3] == 5.0 * s).sum()) == 63, bits
+    m2, l2 = WS.symmetry(m, lab4, 1, 1, 1, 1)
+    assert float(l2[..., 3].sum()) == -(7.0 + 63 * 5.0)

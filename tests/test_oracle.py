@@ -156,3 +156,32 @@ def test_network_oracle_gradients_with_density_channel():
     lp, _ = orc_unet.forward_backward({**params, "out": (params["out"][0], bp)}, inp, labels)
     lm, _ = orc_unet.forward_backward({**params, "out": (params["out"][0], bm)}, inp, labels)
     assert abs((lp - lm) / (2 * h) - grads["out"][1][3]) <= 1e-6
+
+
+def _file_records(L):
+    from golden.make_golden import file_records
+    return file_records(L)
+
+
+def test_file_api_matches_reference(orc):
+    """Velocity, force, map, object and stress files written by the oracle
+    are byte-identical to the strict reference build's (SHA-256 fixtures),
+    and so are lattices reloaded from them (lbloadvel, lbloadobj) and the
+    tracer set by mpsubs (src/lbstore.c:227-678, src/lbmeasure.c:129-203,
+    src/mpobjs.c:188-226)."""
+    g = load("files.json")["cases"]
+    assert _file_records(orc) == g
+
+
+def test_file_api_equals_reference_build_live(orc, ref_strict, tmp_path):
+    """Where the reference is built here: the same files compared byte for
+    byte, live, for one more configuration."""
+    import scenarios as S
+    cfg = dict(dims=(6, 13, 8), steps=7, moving=0, skip=0, stokes=0, tau=0.7)
+    (tmp_path / "o").mkdir()
+    (tmp_path / "r").mkdir()
+    _, fo = S.file_case(orc, str(tmp_path / "o"), **cfg)
+    _, fr = S.file_case(ref_strict, str(tmp_path / "r"), **cfg)
+    assert fo.keys() == fr.keys()
+    for k in fo:
+        assert fo[k] == fr[k], k
