@@ -344,6 +344,21 @@ LBReal mpplane(MPSys, char *, int);
  * src/lbobjs.c:128-165) held in memory instead of a file. */
 LBObj insertmask(LBSys, unsigned char *);
 
+/* Seeded random sequential addition of spheres in a periodic n^3 box (no
+ * counterpart in the reference, whose packings come from files): centres
+ * uniform in [0, n)^3 and radii uniform in [rmin, rmax] from splitmix64
+ * (four draws per try: x, y, z, r, each (z >> 11) * 2^-53); a try is
+ * accepted when its periodic minimum-image distance to every accepted
+ * sphere is at least the sum of the radii (always, with overlap != 0); each
+ * accepted sphere and its periodic images are stamped into the node mask
+ * (rsq < r^2) until the solid fraction reaches phi.  spheres gets
+ * (r, x, y, z) for each accepted sphere (room for max_spheres), solid (may
+ * be NULL) the n^3 mask, inode = n*(n*i + j) + k.  Returns the number of
+ * spheres, -1 when the packing stalls (a sphere would need more than
+ * max_tries tries), -2 when max_spheres is too small, -3 on bad arguments. */
+int rsapacking(int n, double phi, double rmin, double rmax, unsigned long long seed, int overlap,
+               long max_tries, double *spheres, int max_spheres, unsigned char *solid);
+
 /* Batches (no counterpart in the reference): many independent lattices of
  * one precision (FP32 or FP64), each set up as usual, advanced together by
  * batchsteps in one persistent GPU launch; afterwards each lattice is used

@@ -107,8 +107,33 @@ def _min_image_hits(cand, rc, cen, rad, n):
     return np.any(dist < rad + rc[:, None], axis=1)
 
 
-def rsa_packing(n, phi, rmin, rmax, seed=1, overlap=False, max_tries=50_000_000, block=4096):
-    """Random sequential addition of spheres in a periodic n^3 box.
+def rsa_packing(n, phi, rmin, rmax, seed=1, overlap=False, max_tries=50_000_000):
+    """Random sequential addition of spheres in a periodic n^3 box, computed
+    by the library's rsapacking (C, the same draws and decisions as
+    rsa_packing_numpy below, bit for bit, ~20x faster).  Returns
+    (spheres [(r, x, y, z)], solid mask (n, n, n) bool)."""
+    import ctypes as C
+    from . import library
+    f = library().dll.rsapacking
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_ulonglong, C.c_int, C.c_long,
+                  C.c_void_p, C.c_int, C.c_void_p]
+    # room for the spheres: the solid volume over the smallest sphere's, and more
+    cap = int(phi * n ** 3 / (4.0 / 3.0 * math.pi * max(rmin - 1.0, 0.5) ** 3)) * 2 + 1024
+    out = np.zeros((cap, 4), dtype=np.float64)
+    solid = np.zeros((n, n, n), dtype=np.uint8)
+    m = f(n, phi, rmin, rmax, seed & MASK64, int(bool(overlap)), max_tries, out.ctypes.data, cap,
+          solid.ctypes.data)
+    if m == -1:
+        raise RuntimeError(f"RSA stalled short of solid fraction {phi} (more than {max_tries} tries)")
+    if m < 0:
+        raise RuntimeError(f"rsapacking failed ({m})")
+    return [tuple(float(v) for v in row) for row in out[:m]], solid.view(bool)
+
+
+def rsa_packing_numpy(n, phi, rmin, rmax, seed=1, overlap=False, max_tries=50_000_000, block=4096):
+    """Random sequential addition of spheres in a periodic n^3 box (numpy
+    formulation, the definition rsapacking is tested against).
 
     Centres uniform in [0, n)^3, radii uniform in [rmin, rmax] (four
     splitmix64 draws per try: x, y, z, r); a sphere is accepted when its

@@ -183,10 +183,25 @@ def test_packings_are_seeded_and_stable():
     cases = [((128, 0.30, 4.0, 8.0, 1), {}, 986, "314597b4e685bbfd036c5c3fae1816ec"),
              ((64, 0.45, 3.0, 8.0, 12345), {"overlap": True}, 202, "c29cdae16782366f7e94f4213f942fd7")]
     for args, kw, n, digest in cases:
-        spheres, solid = W.rsa_packing(*args, **kw)
-        assert len(spheres) == n
-        assert hashlib.sha256(np.packbits(solid).tobytes()).hexdigest()[:32] == digest
-        assert solid.mean() >= args[1]
+        for fn in (W.rsa_packing, W.rsa_packing_numpy):
+            spheres, solid = fn(*args, **kw)
+            assert len(spheres) == n
+            assert hashlib.sha256(np.packbits(solid).tobytes()).hexdigest()[:32] == digest
+            assert solid.mean() >= args[1]
+
+
+def test_c_packing_equals_numpy_definition():
+    """rsapacking (the library's C routine) takes the same decisions as the
+    numpy formulation: identical sphere lists and masks on small, thin-cell,
+    overlapping and large-radius cases."""
+    from sunlightlb_gb300 import workloads as W
+    for args, kw in (((40, 0.2, 3.0, 6.0, 5), {}), ((32, 0.3, 5.0, 12.0, 3), {}),
+                     ((48, 0.45, 3.0, 8.0, 7), {"overlap": True}), ((72, 0.33, 2.0, 9.0, 11), {}),
+                     ((50, 0.25, 6.0, 12.0, 2), {})):
+        a, sa = W.rsa_packing(*args, **kw)
+        b, sb = W.rsa_packing_numpy(*args, **kw)
+        assert a == b, args
+        assert np.array_equal(sa, sb), args
 
 
 def test_flow_symmetries_algebra():
