@@ -1,11 +1,12 @@
 """Benchmark of the GB300 SunlightLB update step.
 
-Workload (the packed-bed permeability case): periodic 128^3 lattice, seeded
+Headline workload (the large packed bed): periodic 512^3 lattice, seeded
 random sequential addition of non-overlapping spheres with radius uniform in
-[4, 8] up to lattice solid fraction 0.30, fixed objects with link
-bounce-back, body force 1e-6 along x, tau = 1 (viscosity 1/6), Stokes flow,
-FP32 populations.  A step is one lattice Boltzmann update (bounce-back,
-streaming and collision of every node) of the whole lattice.
+[6, 12] up to lattice solid fraction 0.35 (23,309 spheres), fixed objects
+with link bounce-back, Navier-Stokes collision (stokes_flow = 0), tau = 1
+(viscosity 1/6), body force 1e-6 along x, FP32 populations.  A step is one
+lattice Boltzmann update (bounce-back, streaming and collision of every
+node) of the whole lattice.
 
 Metric: million lattice updates per second (all nodes, fluid and solid, as
 the reference's own fwrstats counts them, src/lbmisc.c:264-274).
@@ -18,15 +19,32 @@ updated divided by the slowest rank's time.
 
 The JSON line carries:
   value      device-resident throughput, CUDA events around each step on the
-             lattice's stream, L2 flushed (256 MiB write) between steps;
+             lattice's stream (the populations, 8 GB, are larger than L2);
   e2e        the same metric through the public C API with host buffers:
              populations, geometry and body force uploaded from the host, the
              steps run as check intervals (98 lbstep + measure, which reads
-             the mean flow and the drag back), populations read back at the end;
+             the mean flow and the drag back), populations read back at the
+             end; e2e_fp64 the same with FP64 populations (the reference's
+             own precision);
   roofline   achieved HBM GB/s of the fused step kernel against the measured
              copy bandwidth (120 algorithmic bytes per FP32 node update);
-  cpu_baseline  the CPU oracle (a restatement of the reference's C code) on
-             one host core, on a time-bounded sample of steps.
+  variants   other precisions and sizes (128^3 / 256^3 packings, FP64,
+             BF16 paired deviations) and the permeability of the 128^3
+             packing to convergence in FP64, FP32 and BF16;
+  legs       compact runs of the other workloads: batched vs one-at-a-time
+             moving-sphere domains, flow + passive scalar with partial
+             adsorption on a 256^3 bed, and the learned warm start against
+             the plain start on held-out 128^3 packings;
+  cpu_baseline  the CPU restatement of the reference's update (the oracle,
+             compiled with the reference's shipped -O3 -ffast-math flags,
+             FP32 = the reference's -D_SINGLE build and FP64 = its default)
+             on every host core, one 128^3 block of the same packing per
+             core, on a time-bounded sample of steps.
+
+--impl reference times that CPU restatement alone on the same workload
+(FP32, and FP64 beside it), one 128^3 block of the 512^3 packing per host
+core, W warm-up and K timed steps per core.  --workload tracer / batch /
+warmstart run the full-size forms of the legs.
 """
 
 import argparse
@@ -42,6 +60,10 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# headline: the large packed bed
+HEAD_N, HEAD_PHI, HEAD_RMIN, HEAD_RMAX, HEAD_SEED = 512, 0.35, 6.0, 12.0, 4
+HEAD_STOKES = 0
+# the 128^3 packed bed of the permeability runs and of the smaller variants
 N_SIDE = 128
 PHI = 0.30
 RMIN, RMAX = 4.0, 8.0
@@ -54,12 +76,16 @@ SEED = 1
 # deviations
 BYTES_PER_UPDATE = {0: 240, 1: 120, 2: 64}
 CHECK = 100                           # check interval of the e2e run (98 steps + measure)
+CPU_BLOCK = 128                       # side of the block of the packing one CPU core advances
+
+
+def head_workload():
+    return (f"packed bed, periodic {HEAD_N}^3, RSA spheres r~U[{HEAD_RMIN:g},{HEAD_RMAX:g}] to solid fraction "
+            f"{HEAD_PHI}, Navier-Stokes, body force {FORCE:g} along x, tau {TAU:g}")
 
 
 def config(prec_name, l2):
-    return {"workload": f"packed-bed permeability, periodic {N_SIDE}^3, RSA spheres r~U[{RMIN:g},{RMAX:g}] "
-                        f"to solid fraction {PHI}, body force {FORCE:g} along x, tau {TAU:g}, Stokes",
-            "lattice": [N_SIDE, N_SIDE, N_SIDE], "populations": prec_name, "seed": SEED,
+    return {"workload": head_workload(), "lattice": [HEAD_N] * 3, "populations": prec_name, "seed": HEAD_SEED,
             "velocity_set": "D3Q15", "l2": l2, "parallelism": "replicas"}
 
 
@@ -135,11 +161,11 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(prec_name):
+def profile_traffic(prec_name, n=HEAD_N):
     """DRAM bytes per launch of the fused step (mean of the odd and even
-    step) from the committed ncu summary profiles/lb_step_128.md, line
-    'traffic_per_launch_<precision>: <bytes>'."""
-    p = os.path.join(ROOT, "profiles", "lb_step_128.md")
+    step) at an n^3 lattice from the committed ncu summary
+    profiles/lb_step_<n>.md, line 'traffic_per_launch_<precision>: <bytes>'."""
+    p = os.path.join(ROOT, "profiles", f"lb_step_{n}.md")
     try:
         with open(p) as f:
             for line in f:
@@ -151,10 +177,19 @@ def profile_traffic(prec_name):
     return None
 
 
-def build_lattice(L, precision, spheres, solid):
+def make_lattice(L, solid, precision, stokes=1, force=FORCE, tau=TAU):
+    """A periodic lattice whose solid nodes are `solid` (one object), body
+    force along x."""
     from sunlightlb_gb300 import workloads as W
-    lb, _, _ = W.packed_bed(L, n=N_SIDE, phi=PHI, rmin=RMIN, rmax=RMAX, seed=SEED, force=FORCE, tau=TAU,
-                            precision=precision, spheres=spheres)
+    n = solid.shape
+    lb = L.newlb(n[0], n[1], n[2], "null")
+    lb.precision = precision
+    lb.tau = tau
+    lb.stokes_flow = stokes
+    W.insert_solid(L, lb, solid)
+    L.flattenobj(lb)
+    L.syncobjs(lb)
+    L.addbf(lb, force, 0.0, 0.0)
     return lb
 
 
@@ -171,13 +206,18 @@ class Flusher:
         self.buf.sum()
 
 
-def time_steps(torch, L, lb, steps, warmup, flusher=None):
+def time_steps(torch, L, lb, steps, warmup, flusher=None, kinds=None):
     """Per-step device times (ms) of `steps` lbstep calls, CUDA events on
-    the lattice's own stream, optional L2 flush before each timed step."""
+    the lattice's own stream, optional L2 flush before each timed step.
+    With a list `kinds`, appends per step whether it was the pull-and-push
+    update (the layout before it was the one an even update leaves)."""
     stream = torch.cuda.ExternalStream(L.lbgetstream(lb))
     for _ in range(warmup):
         L.lbstep(lb)
     torch.cuda.synchronize()
+    if kinds is not None:
+        first = L.lblayout(lb) == 1
+        kinds.extend((first if s % 2 == 0 else not first) for s in range(steps))
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     with torch.cuda.stream(stream):
@@ -202,28 +242,30 @@ def tuning(L, lb):
             "odd": {"rows_per_thread": cfg[2], "threads_k": cfg[3]}}
 
 
-def variant_line(torch, L, name, n, solid, precision, steps, flush):
-    from sunlightlb_gb300 import workloads as W
-    lb = L.newlb(n, n, n, "null")
-    lb.precision = precision
-    lb.tau = TAU
-    lb.stokes_flow = 1
-    W.insert_solid(L, lb, solid)
-    L.flattenobj(lb)
-    L.syncobjs(lb)
-    L.addbf(lb, FORCE, 0.0, 0.0)
+PREC_NAMES = {0: "fp64", 1: "fp32", 2: "fp32 moments + bf16 paired deviations"}
+
+
+def variant_line(torch, L, n, solid, precision, steps, flush, stokes=1):
+    lb = make_lattice(L, solid, precision, stokes=stokes)
     L.lbsteps(lb, 2)
-    ms = time_steps(torch, L, lb, steps, 3, Flusher(torch) if flush else None)
+    kinds = []
+    ms = time_steps(torch, L, lb, steps, 3, Flusher(torch) if flush else None, kinds)
     mean = sum(ms) / len(ms)
+    split = {}
+    for name, want in (("pull_push", True), ("local", False)):
+        sel = [m for m, k in zip(ms, kinds) if k == want]
+        if sel:
+            split[name] = round(statistics.mean(sel), 5)
     nodes = lb.nnodes
-    peak, kind = measured_peak()
+    peak, _ = measured_peak()
     gbs = BYTES_PER_UPDATE[precision] * nodes / (mean * 1e-3) / 1e9
-    out = {"lattice": n, "populations": {0: "fp64", 1: "fp32", 2: "fp32 moments + bf16 paired deviations"}[precision],
+    out = {"lattice": n, "populations": PREC_NAMES[precision], "collision": "Stokes" if stokes else "Navier-Stokes",
            "MLUPS": round(nodes / (mean * 1e-3) / 1e6, 1), "bytes_per_update": BYTES_PER_UPDATE[precision],
-           "ms_per_step": round(mean, 5), "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
+           "ms_per_step": round(mean, 5), "ms_per_step_by_update": split if precision != 2 else None,
+           "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
            "l2": "flushed" if flush else "lattice larger than L2", "tuning": tuning(L, lb)}
     L.freelb(lb)
-    return name, out
+    return out
 
 
 def permeability_run(torch, L, solid, precision, tol, maxsteps):
@@ -231,14 +273,7 @@ def permeability_run(torch, L, solid, precision, tol, maxsteps):
     change of the mean flow is below tol): update steps, wall time and the
     Darcy constant k = vmeanx * eta / b."""
     from sunlightlb_gb300 import workloads as W
-    lb = L.newlb(N_SIDE, N_SIDE, N_SIDE, "null")
-    lb.precision = precision
-    lb.tau = TAU
-    lb.stokes_flow = 1
-    W.insert_solid(L, lb, solid)
-    L.flattenobj(lb)
-    L.syncobjs(lb)
-    L.addbf(lb, FORCE, 0.0, 0.0)
+    lb = make_lattice(L, solid, precision, stokes=1)
     L.lbsteps(lb, 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -266,13 +301,14 @@ def run_mine(args):
     L = sunlightlb_gb300.library()
     precision = {"fp64": 0, "fp32": 1, "bf16dev": 2}[args.precision]
     prec_name = args.precision
-    spheres, solid = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
-    lb = build_lattice(L, precision, spheres, solid)
+    t0 = time.perf_counter()
+    _, solid = W.rsa_packing(HEAD_N, HEAD_PHI, HEAD_RMIN, HEAD_RMAX, HEAD_SEED)
+    t_pack = time.perf_counter() - t0
+    lb = make_lattice(L, solid, precision, stokes=HEAD_STOKES)
     nodes = lb.nnodes
 
     # -------- device-resident throughput: one step per timed iteration --------
     L.lbsteps(lb, 2)  # first device call: upload, autotune
-    flusher = Flusher(torch)
     for _ in range(args.warmup):
         L.lbstep(lb)
     torch.cuda.synchronize()
@@ -280,10 +316,13 @@ def run_mine(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    kinds = []
     with Clocks(local) as clk:
         t0 = time.perf_counter()
-        step_ms = time_steps(torch, L, lb, args.steps, 0, flusher)
+        step_ms = time_steps(torch, L, lb, args.steps, 0, None, kinds)
         wall = time.perf_counter() - t0
+    by_kind = {"pull_push": [m for m, k in zip(step_ms, kinds) if k],
+               "local": [m for m, k in zip(step_ms, kinds) if not k]}
     launches = L.lbkernelcount() - k0
     total_ms = sum(step_ms)
     value, ms_per_step = aggregate(total_ms, nodes, args.steps, world,
@@ -293,28 +332,40 @@ def run_mine(args):
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_UPDATE[precision] * nodes / (ms_per_step * 1e-3) / 1e9
     tune = tuning(L, lb)
+    L.freelb(lb)
 
     # -------- end-to-end through the public API with host buffers -------------
-    e2e = run_e2e(L, precision, spheres, solid, args)
+    e2e = run_e2e(L, precision, solid, args.e2e_intervals)
+    e2e64 = run_e2e(L, 0, solid, args.e2e_fp64_intervals) if precision != 0 and args.e2e_fp64_intervals > 0 else None
 
-    # -------- other precisions and sizes of the same packing ------------------
+    # -------- other precisions and sizes --------------------------------------
     variants = {}
-    if not args.no_variants and rank == 0:
-        big = np.tile(solid, (2, 2, 2))  # 256^3, the 128^3 packing repeated periodically
-        for name, n, sol, prec, flush in (("fp32_256", 256, big, 1, False),
-                                          ("bf16dev_128", N_SIDE, solid, 2, True),
-                                          ("bf16dev_256", 256, big, 2, False),
-                                          ("fp64_128", N_SIDE, solid, 0, True)):
-            k, v = variant_line(torch, L, name, n, sol, prec, min(args.steps, 30), flush)
-            variants[k] = v
-
     perm = {}
-    if not args.no_convergence and rank == 0:
-        for name, prec in (("fp64", 0), ("fp32", 1), ("bf16dev", 2)):
-            perm[name] = permeability_run(torch, L, solid, prec, 1e-8, args.max_converge_steps)
-        if "fp64" in perm and perm["fp64"]["k"]:
-            for name in perm:
-                perm[name]["k_rel_error_vs_fp64"] = abs(perm[name]["k"] - perm["fp64"]["k"]) / abs(perm["fp64"]["k"])
+    legs = {}
+    if rank == 0:
+        _, small = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
+        if not args.no_variants:
+            big = np.tile(small, (2, 2, 2))  # 256^3, the 128^3 packing repeated periodically
+            nv = min(args.steps, 30)
+            for name, n, sol, prec, flush, stokes, k in (
+                    ("fp32_128", N_SIDE, small, 1, True, 1, nv),
+                    ("fp32_256", 256, big, 1, False, 1, nv),
+                    ("bf16dev_128", N_SIDE, small, 2, True, 1, nv),
+                    ("bf16dev_256", 256, big, 2, False, 1, nv),
+                    ("bf16dev_512", HEAD_N, solid, 2, False, HEAD_STOKES, nv),
+                    ("fp64_128", N_SIDE, small, 0, True, 1, nv),
+                    ("fp64_512", HEAD_N, solid, 0, False, HEAD_STOKES, 5)):
+                variants[name] = variant_line(torch, L, n, sol, prec, k, flush, stokes=stokes)
+        if not args.no_convergence:
+            for name, prec in (("fp64", 0), ("fp32", 1), ("bf16dev", 2)):
+                perm[name] = permeability_run(torch, L, small, prec, 1e-8, args.max_converge_steps)
+            if "fp64" in perm and perm["fp64"]["k"]:
+                for name in perm:
+                    perm[name]["k_rel_error_vs_fp64"] = abs(perm[name]["k"] - perm["fp64"]["k"]) / abs(perm["fp64"]["k"])
+        if not args.no_legs:
+            legs["batch"] = batch_leg(torch, L, args)
+            legs["tracer"] = tracer_leg(torch, L, args)
+            legs["warmstart"] = warm_leg(torch, L, args)
 
     if rank != 0:
         return
@@ -331,34 +382,37 @@ def run_mine(args):
         "vs_baseline": None,
         "dtype": {0: "f64", 1: "f32", 2: "f32 arithmetic, bf16 paired-deviation storage"}[precision],
         "data": "synthetic seeded RSA sphere packing (the reference publishes no benchmark data set)",
-        "config": dict(config(prec_name, "flushed between timed steps (256 MiB write, then read)"), autotune=tune),
+        "config": dict(config(prec_name, f"not flushed: the populations ({BYTES_PER_UPDATE[precision] // 2 * nodes / 1e9:.1f} GB) "
+                                         "are larger than L2"), autotune=tune, packing_s=round(t_pack, 2)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": profile_traffic(prec_name),
                      "bytes_per_update": BYTES_PER_UPDATE[precision],
                      "kernel": "k_step_pair (paired-deviation update)" if precision == 2 else "k_step (fused AA update)"},
         "e2e": e2e,
+        "e2e_fp64": e2e64,
+        "ms_per_step_by_update": {k: round(statistics.mean(v), 5) for k, v in by_kind.items() if v},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed": round(wall, 4),
         "variants": variants,
-        "permeability": dict(perm, criterion="|d vmeanx| / vmeanx < 1e-8 between 100-step checks"),
+        "permeability": dict(perm, lattice=N_SIDE, criterion="|d vmeanx| / vmeanx < 1e-8 between 100-step checks"),
+        "legs": legs,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(spheres, solid, budget_s=args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(solid, budget_s=args.cpu_seconds)
     print(json.dumps(line), flush=True)
 
 
-def run_e2e(L, precision, spheres, solid, args):
+def run_e2e(L, precision, solid, intervals):
     """MLUPS of check intervals run through the public API, host buffers:
     a fresh lattice whose populations come from the host (lbpush uploads
     them with the geometry and body force), intervals of 98 lbstep + measure
     (mean flow and drag read back each interval), populations read back."""
-    import numpy as np
     import torch
-    lb = build_lattice(L, precision, spheres, solid)
+    lb = make_lattice(L, solid, precision, stokes=HEAD_STOKES)
     n = lb.nnodes
-    intervals = max(1, args.e2e_intervals)
+    intervals = max(1, intervals)
     L.lbpull(lb)  # allocates the host mirror (zero populations)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -375,9 +429,11 @@ def run_e2e(L, precision, spheres, solid, args):
     d2h += pops.nbytes
     dt = time.perf_counter() - t0
     steps = intervals * CHECK
+    L.freelb(lb)
     return {"value": round(n * steps / dt / 1e6, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps),
-            "steps": steps, "note": "public C API: lbpush, lbsteps + measure per 100 steps, lbpull"}
+            "steps": steps, "populations": PREC_NAMES[precision], "wall_s": round(dt, 3),
+            "note": "public C API: lbpush, lbsteps + measure per 100 steps, lbpull"}
 
 
 def oracle_lib():
@@ -389,63 +445,119 @@ def oracle_lib():
     return Library(path, extended=True)
 
 
-def _cpu_worker(spheres, solid, budget_s, out, slot):
-    L = oracle_lib()
-    from sunlightlb_gb300 import workloads as W
-    lb = L.newlb(N_SIDE, N_SIDE, N_SIDE, "null")
-    lb.tau = TAU
-    lb.stokes_flow = 1
-    W.insert_solid(L, lb, solid)
-    L.flattenobj(lb)
-    L.syncobjs(lb)
-    L.addbf(lb, FORCE, 0.0, 0.0)
-    L.lbstep(lb)
-    steps = 0
-    t0 = time.perf_counter()
-    while steps < 2 or time.perf_counter() - t0 < budget_s:
-        L.lbstep(lb)
-        steps += 1
-    out[slot] = (steps, time.perf_counter() - t0, lb.nnodes)
+def timing_lib(bits):
+    """The oracle's timing build (reference shipped flags), LBReal of `bits`."""
+    import ctypes as C
+    from sunlightlb_gb300 import build as b
+    path = os.path.join(ROOT, "oracle", f"liboracle_time{bits}.so")
+    if not os.path.exists(path):
+        b.build_oracle(with_reference=False)
+    lib = C.CDLL(path)
+    f = lib.orc_time_steps
+    f.restype = C.c_double
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
+                  C.c_void_p]
+    return f
 
 
-def cpu_baseline(spheres, solid, budget_s=10.0, threads=1):
-    """The CPU oracle (restatement of the reference's single-threaded C
-    update, strict FP64) on host cores; one lattice per thread."""
+def cpu_blocks(solid, count):
+    """`count` distinct CPU_BLOCK^3 blocks of the packing (k fastest), each a
+    periodic lattice of its own."""
+    import numpy as np
+    per = solid.shape[0] // CPU_BLOCK
+    out = []
+    for b in range(count):
+        b %= per ** 3  # more cores than blocks: blocks repeat
+        i, j, k = (b // (per * per)) % per, (b // per) % per, b % per
+        out.append(np.ascontiguousarray(solid[i * CPU_BLOCK:(i + 1) * CPU_BLOCK, j * CPU_BLOCK:(j + 1) * CPU_BLOCK,
+                                              k * CPU_BLOCK:(k + 1) * CPU_BLOCK], dtype=np.uint8))
+    return out
+
+
+def cpu_run(solid, bits, threads, warmup, steps):
+    """Every thread advances its own block of the packing by warmup, then
+    `steps` timed update steps (the oracle's timing build; ctypes releases
+    the interpreter lock, so the threads run on separate cores).  Returns
+    (MLUPS of all threads over the slowest thread's time, steps)."""
+    import ctypes as C
+    f = timing_lib(bits)
+    blocks = cpu_blocks(solid, threads)
     out = [None] * threads
-    ts = [threading.Thread(target=_cpu_worker, args=(spheres, solid, budget_s, out, s)) for s in range(threads)]
+
+    def work(t):
+        cs = C.c_double()
+        out[t] = f(blocks[t].ctypes.data, CPU_BLOCK, CPU_BLOCK, CPU_BLOCK, TAU, HEAD_STOKES, FORCE, warmup, steps,
+                   C.byref(cs))
+
+    ts = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
     for t in ts:
         t.start()
     for t in ts:
         t.join()
-    total = sum(s * n for s, _, n in out) / max(dt for _, dt, _ in out) / 1e6
-    steps = [s for s, _, _ in out]
-    return {"value": round(total, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
-            "sample": f"{min(steps)}-{max(steps)} FP64 update steps per thread of the same {N_SIDE}^3 packing "
-                      f"({threads} lattice(s), about {budget_s:g} s of CPU time each)"}
+    if any(v is None or v <= 0 for v in out):
+        raise RuntimeError("CPU baseline failed")
+    return threads * CPU_BLOCK ** 3 * steps / max(out) / 1e6
+
+
+def cpu_steps_for(solid, bits, budget_s):
+    """Steps per thread that take about budget_s (one calibration step)."""
+    import ctypes as C
+    f = timing_lib(bits)
+    blk = cpu_blocks(solid, 1)[0]
+    cs = C.c_double()
+    dt = f(blk.ctypes.data, CPU_BLOCK, CPU_BLOCK, CPU_BLOCK, TAU, HEAD_STOKES, FORCE, 0, 1, C.byref(cs))
+    return max(2, int(budget_s / max(dt, 1e-3)))
+
+
+def cpu_baseline(solid, budget_s=10.0):
+    """The CPU restatement of the reference's update under its shipped flags
+    on every host core, FP32 (-D_SINGLE) and FP64, one 128^3 block of the
+    packing per core, about budget_s of steps per core each."""
+    threads = os.cpu_count() or 1
+    res = {}
+    for bits, name in ((32, "fp32"), (64, "fp64")):
+        steps = cpu_steps_for(solid, bits, budget_s)
+        res[name] = (round(cpu_run(solid, bits, threads, 1, steps), 3), steps)
+    v32, s32 = res["fp32"]
+    v64, s64 = res["fp64"]
+    return {"value": v32, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "build": "oracle restatement of the reference's update, -O3 -ffast-math (the reference's shipped "
+                     "flags), -D_SINGLE for FP32",
+            "sample": f"{s32} FP32 / {s64} FP64 update steps per core of a distinct {CPU_BLOCK}^3 block of the "
+                      f"same {HEAD_N}^3 packing (periodic), {threads} cores",
+            "fp64": {"value": v64, "unit": "MLUPS", "cores": threads}}
 
 
 def run_reference(args):
-    """The reference's CPU implementation of the path (the oracle port of its
-    C code: a build of the reference needs its sources, which this machine
-    may not hold) on every host core: one lattice per thread, aggregate MLUPS
-    per step."""
+    """The reference's CPU implementation of the path (the oracle port of
+    its C code under the reference's shipped flags: a build of the reference
+    itself needs its sources, which this machine may not hold) on every host
+    core, FP32 (the reference's -D_SINGLE build) as the value and FP64 (its
+    default build) beside it; one 128^3 block of the headline packing per
+    core, W warm-up and K timed steps per core."""
     from sunlightlb_gb300 import workloads as W
     world, rank, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    spheres, solid = W.rsa_packing(N_SIDE, PHI, RMIN, RMAX, SEED)
-    budget = max(5.0, min(60.0, args.cpu_seconds * 2))
-    cb = cpu_baseline(spheres, solid, budget_s=budget, threads=threads)
+    _, solid = W.rsa_packing(HEAD_N, HEAD_PHI, HEAD_RMIN, HEAD_RMAX, HEAD_SEED)
+    v32 = cpu_run(solid, 32, threads, args.warmup, args.steps)
+    v64 = cpu_run(solid, 64, threads, args.warmup, args.steps)
+    sample = (f"{args.warmup} warm-up + {args.steps} timed update steps per core, each core a distinct "
+              f"{CPU_BLOCK}^3 block of the {HEAD_N}^3 packing (periodic), {threads} cores")
     line = {
         "impl": "reference",
         "metric": "MLUPS (million lattice updates per second, all nodes), packed-bed lattice Boltzmann step",
-        "value": cb["value"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "value": round(v32, 3), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic seeded RSA sphere packing",
-        "config": config("fp64 (CPU reference code)", "n/a (CPU)"),
-        "cpu_baseline": cb,
-        "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": config("fp32 (the reference's -D_SINGLE build, on the CPU)", "n/a (CPU)"),
+        "cpu_baseline": {"value": round(v32, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "build": "oracle restatement of the reference's update, -O3 -ffast-math, -D_SINGLE",
+                         "sample": sample},
+        "fp64": {"value": round(v64, 3), "unit": "MLUPS", "cores": threads,
+                 "build": "the same restatement, LBReal double (the reference's default build)"},
+        "e2e": {"value": round(v32, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -501,19 +613,12 @@ def cpu_tracer_baseline(budget_s):
             "sample": f"{steps} FP64 tracer updates (with the source plane) of a 64^3 packing of the same kind"}
 
 
-def run_tracer(args):
+def tracer_result(torch, L, n, fp32_steps, fp64_steps, sample_every, maxsteps, kernel_steps=50):
     """Large packed bed, flow at pore Reynolds number about 1, then a passive
-    scalar with partial adsorption carried through the frozen flow."""
-    import torch
-    import sunlightlb_gb300
+    scalar with partial adsorption carried through the frozen flow, in FP32
+    and FP64 tracers; kernel rates, breakthrough and mass balance."""
     from sunlightlb_gb300 import workloads as W
-
-    world, rank, local = dist_env()
-    if rank != 0:
-        return
-    torch.cuda.set_device(local)
-    L = sunlightlb_gb300.library()
-    n = args.side
+    local = dist_env()[2]
     t0 = time.perf_counter()
     lb, spheres = W.large_bed(L, n, TRACER_PHI, TRACER_RMIN, TRACER_RMAX, TRACER_SEED, precision=1)
     t_build = time.perf_counter() - t0
@@ -522,7 +627,7 @@ def run_tracer(args):
     L.lbsteps(lb, 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    flow = W.calibrated_flow(L, lb, diameter, re_target=1.0, maxsteps=args.max_converge_steps)
+    flow = W.calibrated_flow(L, lb, diameter, re_target=1.0, maxsteps=maxsteps)
     torch.cuda.synchronize()
     flow["wall_s"] = round(time.perf_counter() - t0, 2)
     flow["fluid_fraction"] = L.countfluid(lb) / nodes
@@ -535,16 +640,16 @@ def run_tracer(args):
                    "frac_of_measured_hbm": round(BYTES_PER_UPDATE[1] * nodes / (step_ms * 1e-3) / 1e9 / peak, 4),
                    "bytes_per_update": BYTES_PER_UPDATE[1], "clocks": clk.summary()}
     tracers = {}
-    for name, prec, nsteps in (("fp32", 1, args.tracer_steps), ("fp64", 0, args.fp64_tracer_steps)):
+    for name, prec, nsteps in (("fp32", 1, fp32_steps), ("fp64", 0, fp64_steps)):
         if nsteps <= 0:
             continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         mp, curve, bals = W.tracer_breakthrough(L, lb, nsteps, precision=prec, alpha=TRACER_ALPHA,
-                                                adprob=TRACER_ADPROB, sample_every=args.sample_every)
+                                                adprob=TRACER_ADPROB, sample_every=sample_every)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        kms = time_tracer(torch, L, lb, mp, 50) / 50
+        kms = time_tracer(torch, L, lb, mp, kernel_steps) / kernel_steps
         gbs = TRACER_BYTES[prec] * nodes / (kms * 1e-3) / 1e9
         _, fl, ad, al, inj = bals[-1]
         tracers[name] = {
@@ -573,9 +678,8 @@ def run_tracer(args):
             "breakthrough_max_abs_diff": max(abs(c32[s] - c64[s]) for s in common) if common else None,
             "adsorbed_rel_diff": abs(b32[last][2] - b64[last][2]) / max(abs(b64[last][2]), 1e-300) if last else None,
             "held_rel_diff": abs(b32[last][3] - b64[last][3]) / max(abs(b64[last][3]), 1e-300) if last else None}
-    line = {
+    out = {
         "workload": f"flow and passive scalar, periodic {n}^3 packed bed",
-        "metric": "MLUPS of the flow and tracer kernels; breakthrough and tracer mass balance",
         "config": {"lattice": [n, n, n], "solid_fraction_target": TRACER_PHI,
                    "radii": [TRACER_RMIN, TRACER_RMAX], "seed": TRACER_SEED, "spheres": len(spheres),
                    "mean_diameter": diameter, "tau": 1.0, "flow": "Navier-Stokes (stokes_flow = 0), FP32 populations",
@@ -585,10 +689,35 @@ def run_tracer(args):
         "build_s": round(t_build, 1), "flow": flow, "flow_kernel": flow_kernel, "tracer": tracers,
         "measured_peak_gbs": peak, "peak_kind": peak_kind,
     }
+    L.freelb(lb)
+    return out
+
+
+def run_tracer(args):
+    import torch
+    import sunlightlb_gb300
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    L = sunlightlb_gb300.library()
+    line = {"metric": "MLUPS of the flow and tracer kernels; breakthrough and tracer mass balance"}
+    line.update(tracer_result(torch, L, args.side, args.tracer_steps, args.fp64_tracer_steps, args.sample_every,
+                              args.max_converge_steps))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_tracer_baseline(args.cpu_seconds)
     print(json.dumps(line), flush=True)
-    L.freelb(lb)
+
+
+def tracer_leg(torch, L, args):
+    """Compact form for the default line: 256^3 bed, 2000 FP32 and 2000
+    FP64 tracer updates (mass balance and FP32 vs FP64)."""
+    out = tracer_result(torch, L, args.leg_tracer_side, args.leg_tracer_steps, args.leg_tracer_steps, 500,
+                        args.max_converge_steps)
+    for t in ("fp32", "fp64"):
+        if t in out["tracer"]:
+            out["tracer"][t].pop("balances", None)
+    return out
 
 
 # ---- batched ensemble of small moving-sphere domains ------------------------
@@ -645,22 +774,15 @@ def _oracle_domain(spec, steps, out, slot):
     out[slot] = drag(lb)
 
 
-def run_batch(args):
-    """Many independent moving-sphere domains: one persistent launch for
-    all of them (batchsteps) against the same domains one at a time
-    (lbsteps per domain), per-domain drag compared; a seeded subset against
-    the CPU oracle (FP64)."""
-    import torch
-    import sunlightlb_gb300
-
-    world, rank, local = dist_env()
-    if rank != 0:
-        return
-    torch.cuda.set_device(local)
-    L = sunlightlb_gb300.library()
-    specs = batch_domains(args.domains)
+def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=True):
+    """Many independent moving-sphere domains advanced together (batchsteps,
+    packed tiles, one launch per step from a CUDA graph) against the same
+    domains one at a time (lbsteps per domain), per-domain drag compared;
+    optionally the other batch mode and a seeded subset against the CPU
+    oracle (FP64)."""
+    local = dist_env()[2]
+    specs = batch_domains(ndom)
     nodes = sum(s[0] ** 3 for s in specs)
-    steps = args.batch_steps
     t0 = time.perf_counter()
     batch = [build_domain(L, *sp) for sp in specs]
     alone = [build_domain(L, *sp) for sp in specs]
@@ -676,11 +798,15 @@ def run_batch(args):
         L.lbsteps(lb, 2)  # the same step count
     torch.cuda.synchronize()
     k0 = L.lbkernelcount()
-    with Clocks(local) as clk:
-        t0 = time.perf_counter()
-        L.batchsteps(b, steps)
-        torch.cuda.synchronize()
-        t_batch = time.perf_counter() - t0
+    clk = Clocks(local) if clocks else None
+    if clk:
+        clk.__enter__()
+    t0 = time.perf_counter()
+    L.batchsteps(b, steps)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    if clk:
+        clk.__exit__(None, None, None)
     launches = L.lbkernelcount() - k0
     t0 = time.perf_counter()
     for lb in alone:
@@ -695,41 +821,42 @@ def run_batch(args):
         d1, d2 = drag(lb1), drag(lb2)
         drags.append(d1)
         worst = max(worst, max(abs(x - y) for x, y in zip(d1, d2)))
-    # the other batch mode (one persistent launch, blocks owning whole
-    # lattices), timed on the same lattices after the drag comparison
-    psteps = max(2, steps // 10)
-    L.batchmode(b, 1)
-    L.batchsteps(b, 2)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    L.batchsteps(b, psteps)
-    torch.cuda.synchronize()
-    t_pers = time.perf_counter() - t0
     peak, peak_kind = measured_peak()
     gbs = BYTES_PER_UPDATE[1] * nodes * steps / t_batch / 1e9
-    line = {
-        "workload": f"batched ensemble: {args.domains} periodic moving-sphere domains, sides {list(BATCH_SIDES)}",
-        "metric": "MLUPS of all domains together, batched vs one domain at a time",
-        "config": {"domains": args.domains, "cells": nodes, "steps": steps, "radii": [BATCH_RMIN, BATCH_RMAX],
-                   "speed": BATCH_SPEED, "seed": BATCH_SEED, "tau": 1.0, "flow": "Stokes",
-                   "populations": "fp32", "boundary": "moving-wall link bounce-back on the fixed node map (vspread)"},
+    out = {
+        "config": {"domains": ndom, "sides": list(BATCH_SIDES), "cells": nodes, "steps": steps,
+                   "radii": [BATCH_RMIN, BATCH_RMAX], "speed": BATCH_SPEED, "seed": BATCH_SEED, "tau": 1.0,
+                   "flow": "Stokes", "populations": "fp32",
+                   "boundary": "moving-wall link bounce-back on the fixed node map (vspread)"},
         "build_s": round(t_build, 1),
-        "batched": {"mode": "packed tiles, one launch per step, CUDA graph", "wall_s": round(t_batch, 3), "MLUPS": round(nodes * steps / t_batch / 1e6, 1),
-                    "hbm_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4),
-                    "gpu_launches": launches, "clocks": clk.summary()},
-        "batched_persistent_mode": {"steps": psteps, "wall_s": round(t_pers, 3),
-                                    "MLUPS": round(nodes * psteps / t_pers / 1e6, 1)},
+        "batched": {"mode": "packed tiles, one launch per step, CUDA graph", "wall_s": round(t_batch, 3),
+                    "MLUPS": round(nodes * steps / t_batch / 1e6, 1), "hbm_gbs": round(gbs, 1),
+                    "frac_of_measured_hbm": round(gbs / peak, 4), "gpu_launches": launches,
+                    "clocks": clk.summary() if clk else None},
         "one_at_a_time": {"wall_s": round(t_alone, 3), "MLUPS": round(nodes * steps / t_alone / 1e6, 1)},
         "speedup": round(t_alone / t_batch, 2),
         "drag_max_abs_diff_batched_vs_one_at_a_time": worst,
         "measured_peak_gbs": peak, "peak_kind": peak_kind,
     }
-    if args.cpu_subset > 0:
-        # the smallest domains, FP64 on the CPU oracle, one thread each
-        sub = sorted(range(len(specs)), key=lambda d: (specs[d][0], d))[:args.cpu_subset]
-        out = [None] * len(sub)
+    if persistent:
+        # the other batch mode (one persistent launch, blocks owning whole
+        # lattices), timed on the same lattices after the drag comparison
+        psteps = max(2, steps // 10)
+        L.batchmode(b, 1)
+        L.batchsteps(b, 2)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ts = [threading.Thread(target=_oracle_domain, args=(specs[d], steps + 4, out, n)) for n, d in enumerate(sub)]
+        L.batchsteps(b, psteps)
+        torch.cuda.synchronize()
+        t_pers = time.perf_counter() - t0
+        out["batched_persistent_mode"] = {"steps": psteps, "wall_s": round(t_pers, 3),
+                                          "MLUPS": round(nodes * psteps / t_pers / 1e6, 1)}
+    if cpu_subset > 0:
+        # the smallest domains, FP64 on the CPU oracle, one thread each
+        sub = sorted(range(len(specs)), key=lambda d: (specs[d][0], d))[:cpu_subset]
+        res = [None] * len(sub)
+        t0 = time.perf_counter()
+        ts = [threading.Thread(target=_oracle_domain, args=(specs[d], steps + 4, res, n)) for n, d in enumerate(sub)]
         for t in ts:
             t.start()
         for t in ts:
@@ -740,14 +867,38 @@ def run_batch(args):
         eta = 72.0 * (1.0 - 0.5) / 3.0
         rel = []
         for n, d in enumerate(sub):
-            ref = out[n]
             scale = 6.0 * math.pi * eta * specs[d][1] * BATCH_SPEED
-            rel.append(max(abs(x - y) for x, y in zip(drags[d], ref)) / scale)
-        line["cpu_subset"] = {"domains": sub, "steps": steps + 4, "wall_s": round(t_cpu, 2), "cores": len(sub),
-                              "MLUPS": round(sum(specs[d][0] ** 3 for d in sub) * (steps + 4) / t_cpu / 1e6, 2),
-                              "kind": "port", "drag_max_diff_over_stokes_drag_gpu_fp32_vs_cpu_fp64": max(rel)}
-    print(json.dumps(line), flush=True)
+            rel.append(max(abs(x - y) for x, y in zip(drags[d], res[n])) / scale)
+        out["cpu_subset"] = {"domains": sub, "steps": steps + 4, "wall_s": round(t_cpu, 2), "cores": len(sub),
+                             "MLUPS": round(sum(specs[d][0] ** 3 for d in sub) * (steps + 4) / t_cpu / 1e6, 2),
+                             "kind": "port", "drag_max_diff_over_stokes_drag_gpu_fp32_vs_cpu_fp64": max(rel)}
     L.freebatch(b)
+    for lb in batch + alone:
+        L.freelb(lb)
+    return out
+
+
+def run_batch(args):
+    import torch
+    import sunlightlb_gb300
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    L = sunlightlb_gb300.library()
+    out = batch_result(torch, L, args.domains, args.batch_steps, cpu_subset=args.cpu_subset)
+    line = {"workload": f"batched ensemble: {args.domains} periodic moving-sphere domains, sides {list(BATCH_SIDES)}",
+            "metric": "MLUPS of all domains together, batched vs one domain at a time"}
+    line.update(out)
+    print(json.dumps(line), flush=True)
+
+
+def batch_leg(torch, L, args):
+    """Compact form for the default line: 64 domains, 2000 steps."""
+    out = batch_result(torch, L, args.leg_domains, args.leg_batch_steps, cpu_subset=2, persistent=False,
+                       clocks=False)
+    out["workload"] = f"batched ensemble, {args.leg_domains} moving-sphere domains"
+    return out
 
 
 # ---- learned warm start ------------------------------------------------------
@@ -881,26 +1032,84 @@ def run_warmstart(args):
     }
     print(json.dumps(line), flush=True)
     if args.save_weights:
-        torch.save({n: {k: v.cpu() for k, v in p.items() if k in ("w", "b")} for n, p in net.params.items()},
-                   args.save_weights)
+        WS.save_weights(net, args.save_weights,
+                        meta={"train_samples": args.train, "train_side": side, "epochs": args.epochs,
+                              "iterations": iters, "seed": WARM_SEED, "label_tol": args.label_tol,
+                              "final_loss": hist[-1] if hist else None})
+
+
+def warm_leg(torch, L, args):
+    """Compact form for the default line: the committed network
+    (sunlightlb_gb300/data/warm_unet.npz, trained by --workload warmstart
+    --save-weights on the GPU) against the plain start on the first
+    `--leg-warm-eval` held-out 128^3 packings of the warmstart workload;
+    steps and wall time to permeability within 1e-4 of the plain converged
+    value, checks every 50 steps in both arms, inference timed."""
+    import numpy as np
+    from sunlightlb_gb300 import warmstart as WS
+    if not os.path.exists(WS.WEIGHTS):
+        return {"skipped": "no trained weights in sunlightlb_gb300/data/warm_unet.npz"}
+    params, widths, features, meta = WS.load_weights()
+    force, side = WARM_FORCE, args.eval_side
+    ntrain = int(meta.get("train_samples", args.train))
+    specs = WS.packing_specs(ntrain + args.eval, WARM_SEED)[ntrain:ntrain + args.leg_warm_eval]
+    inf = WS.UNet(L, side, side, side, batch=1, widths=widths, params=params, features=features)
+    rows = []
+    for phi, sd in specs:
+        solid = WS.packing(side, phi, sd)
+        traj = WS.permeability_run(L, solid, force)
+        k_conv = traj[-1][1]
+        sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
+        plain = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, check=50), k_conv, 1e-4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u, drho = WS.predict_state(inf, sdev, force, WS.ETA_TAU1)
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t0
+        warm = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho,
+                                                   check=50), k_conv, 1e-4)
+        rows.append({"phi": round(phi, 4), "k": k_conv, "plain_steps": plain[0] if plain else None,
+                     "plain_wall_s": round(plain[1], 4) if plain else None,
+                     "warm_steps": warm[0] if warm else None,
+                     "warm_wall_s": round(warm[1] + t_inf, 4) if warm else None, "inference_s": round(t_inf, 4)})
+    ok = [r for r in rows if r["plain_wall_s"] and r["warm_wall_s"]]
+    tot_p = sum(r["plain_wall_s"] for r in ok)
+    tot_w = sum(r["warm_wall_s"] for r in ok)
+    return {"workload": f"learned warm start, {len(rows)} held-out {side}^3 packings",
+            "network": {"widths": list(widths), "trained": meta},
+            "criterion": "permeability within 1e-4 of the plain converged value, checks every 50 steps",
+            "samples": len(ok), "plain_wall_total_s": round(tot_p, 3), "warm_wall_total_s": round(tot_w, 3),
+            "total_wall_ratio": round(tot_p / tot_w, 3) if tot_w else None,
+            "wall_speedup_mean": round(float(np.mean([r["plain_wall_s"] / r["warm_wall_s"] for r in ok])), 3) if ok else None,
+            "steps_ratio_total": round(sum(r["plain_steps"] for r in ok) / sum(r["warm_steps"] for r in ok), 3) if ok else None,
+            "rows": rows}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16dev"])
     ap.add_argument("--e2e-intervals", type=int, default=20)
+    ap.add_argument("--e2e-fp64-intervals", type=int, default=2)
+    ap.add_argument("--no-legs", action="store_true", help="default workload: skip the batch, tracer and "
+                                                         "warm-start legs")
+    ap.add_argument("--leg-domains", type=int, default=64)
+    ap.add_argument("--leg-batch-steps", type=int, default=2000)
+    ap.add_argument("--leg-tracer-side", type=int, default=256)
+    ap.add_argument("--leg-tracer-steps", type=int, default=2000)
+    ap.add_argument("--leg-warm-eval", type=int, default=10)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-convergence", action="store_true")
     ap.add_argument("--max-converge-steps", type=int, default=60000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="packed", choices=["packed", "tracer", "batch", "warmstart"],
-                    help="packed: the 128^3 packed-bed step (default); tracer: large bed, flow + passive "
-                         "scalar; batch: many small moving-sphere domains in one launch")
+                    help="packed: the 512^3 packed-bed step with its variants and legs (default); tracer: "
+                         "large bed, flow + passive scalar; batch: many small moving-sphere domains in one "
+                         "launch; warmstart: train and evaluate the learned warm start")
     ap.add_argument("--domains", type=int, default=512, help="batch workload: number of domains")
     ap.add_argument("--batch-steps", type=int, default=20000)
     ap.add_argument("--cpu-subset", type=int, default=8, help="batch workload: domains checked on the CPU oracle")

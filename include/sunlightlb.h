@@ -306,6 +306,11 @@ long lbkernelcount(void);
  * along k} (BF16 lattices: planes per block in place of rows per thread);
  * returns 1 tuned, -1 defaults, 0 not decided yet. */
 int lbtuning(LBSys, int *);
+/* Storage layout of the device populations of lb: 0 the reference's order
+ * (after an upload), 1 after an even update (the next update is the
+ * pull-and-push one), 2 after an odd update; -1 before the first device
+ * call. */
+int lblayout(LBSys);
 /* Release every host and device resource of mp. */
 void freemp(MPSys);
 /* Host mirror mp->p: mppull copies the device tracer into it, mppush marks

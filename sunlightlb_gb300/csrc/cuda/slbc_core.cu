@@ -469,7 +469,7 @@ int autotune(Lattice &L) {
 
 int autotune_time(Lattice &L) {
   // FP64/FP32: {rows per thread, threads along k}; BF16: {planes per block, 32}
-  static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}};
+  static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}, {4, 64}, {4, 128}};
   const bool bf = L.precision == 2;
   // BF16: powers of two, and the plane counts that fill one or two waves of
   // three blocks per SM evenly
@@ -486,7 +486,7 @@ int autotune_time(Lattice &L) {
     }
   }
   const int (*cand)[2] = bf ? cand_bf : cand_fp;
-  const int ncand = bf ? nbf : 6;
+  const int ncand = bf ? nbf : 8;
   const char *env = getenv("SLB_AUTOTUNE");
   for (int p = 0; p < 2; p++) {
     L.tuned[p].npt = bf ? bf16_default_planes(L) : 1;
@@ -817,8 +817,8 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
     if (L.precision == 2) {
       if (npt < 1 || npt > 64 || bx != 32)
         return fail_msg("slbc_set_tuning: BF16 lattices take 1 to 64 planes per block and 32 threads along k");
-    } else if ((npt != 1 && npt != 2) || (bx != 32 && bx != 64 && bx != 128 && bx != 256)) {
-      return fail_msg("slbc_set_tuning: rows per thread must be 1 or 2 and threads along k 32, 64, 128 or 256");
+    } else if ((npt != 1 && npt != 2 && npt != 4) || (bx != 32 && bx != 64 && bx != 128 && bx != 256)) {
+      return fail_msg("slbc_set_tuning: rows per thread must be 1, 2 or 4 and threads along k 32, 64, 128 or 256");
     }
     L.tuned[p].npt = npt;
     L.tuned[p].block_k = bx;

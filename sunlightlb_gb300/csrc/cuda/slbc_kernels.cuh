@@ -205,19 +205,13 @@ __device__ __forceinline__ void apply_wall(T (&t)[15], uint16_t fl, bool solid, 
   }
 }
 
-// Fused update (bounce-back + streaming + collision) of node (i, j, k).
-// ODD = false: C1 -> C0 (local), ODD = true: C0 -> C1 (pull and push).
-// MOVING compiles the wall terms in, BFU selects a uniform body force (a
-// kernel constant) over per-node arrays.
-template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
-__device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, int k) {
-  T *__restrict__ P = a.p.pop;
-  const long long S = a.p.npad;
-  const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, a.p.esk);
-  const int x = nb.at(0, 0, 0);
-  const uint16_t fl = __ldg(a.p.flags + x);
-  const bool solid = (fl & FLAG_SOLID) != 0;
-  T t[15];
+// Populations of node x entering a fused update.  ODD = false (C1 -> C0):
+// the node's own slots; ODD = true (C0 -> C1): pulled from the upstream
+// neighbours x - c_q, or from the node's own slot q across a bounce-back
+// link (bit q of fl).
+template <typename T, bool ODD>
+__device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, const Nbr &nb, int x,
+                                          uint16_t fl, T (&t)[15]) {
   if (!ODD) {
 #pragma unroll
     for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
@@ -231,6 +225,17 @@ __device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, in
       t[q] = P[slot * S + src];
     }
   }
+}
+
+// Wall terms, collision and the write-back of node x (the slots load_pops
+// read: locally reversed for the even step, pushed to the neighbours, or to
+// the node's own opposite slot across a bounce-back link, for the odd one).
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+__device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb, int x, uint16_t fl,
+                                            T (&t)[15]) {
+  T *__restrict__ P = a.p.pop;
+  const long long S = a.p.npad;
+  const bool solid = (fl & FLAG_SOLID) != 0;
   if (MOVING && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
   if (!(a.skip_solid && solid)) {
     T bx = a.bfx, by = a.bfy, bz = a.bfz;
@@ -252,19 +257,61 @@ __device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, in
   }
 }
 
-// One fused update step of every node.  NPT is the number of rows along j
-// one thread updates (more memory requests in flight per thread).
+// Fused update (bounce-back + streaming + collision) of node (i, j, k).
+// ODD = false: C1 -> C0 (local), ODD = true: C0 -> C1 (pull and push).
+// MOVING compiles the wall terms in, BFU selects a uniform body force (a
+// kernel constant) over per-node arrays.
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+__device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, int k) {
+  const Nbr nb = make_nbr(i, j, k, a.p.esi, a.p.esj, a.p.esk);
+  const int x = nb.at(0, 0, 0);
+  const uint16_t fl = __ldg(a.p.flags + x);
+  T t[15];
+  load_pops<T, ODD>(a.p.pop, a.p.npad, nb, x, fl, t);
+  finish_node<T, ODD, EXACT, MOVING, BFU>(a, nb, x, fl, t);
+}
+
+// One fused update step of every node.  A thread updates NPT consecutive
+// rows along j at one (i, k), software-pipelined: the flag words of all its
+// rows are loaded first, and the populations of row r + 1 are loaded before
+// row r is collided and written back.  This is safe in place because, in
+// the AA pattern, every node reads exactly the slots it writes, so no two
+// nodes' slot sets meet; it keeps about two rows of loads in flight per
+// thread and removes the flag-then-populations round trip of the odd step
+// from every row but the first.
 // Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).
 template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT>
 __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.z;
   if (k >= a.p.esk) return;
+  const int j0 = blockIdx.y * NPT;
+  const int nrow = min(NPT, a.p.esj - j0);
+  const T *P = a.p.pop;
+  const long long S = a.p.npad;
+  uint16_t fl[NPT];
+#pragma unroll
+  for (int r = 0; r < NPT; r++)
+    if (r < nrow) fl[r] = __ldg(a.p.flags + ((i * a.p.esj + j0 + r) * a.p.esk + k));
+  Nbr nb = make_nbr(i, j0, k, a.p.esi, a.p.esj, a.p.esk);
+  T cur[15];
+  load_pops<T, ODD>(P, S, nb, nb.at(0, 0, 0), fl[0], cur);
 #pragma unroll
   for (int r = 0; r < NPT; r++) {
-    const int j = blockIdx.y * NPT + r;
-    if (NPT > 1 && j >= a.p.esj) break;
-    step_node<T, ODD, EXACT, MOVING, BFU>(a, i, j, k);
+    if (r >= nrow) break;
+    T nxt[15];
+    Nbr nbn = nb;
+    const bool more = r + 1 < nrow;
+    if (more) {
+      nbn = make_nbr(i, j0 + r + 1, k, a.p.esi, a.p.esj, a.p.esk);
+      load_pops<T, ODD>(P, S, nbn, nbn.at(0, 0, 0), fl[r + 1 < NPT ? r + 1 : r], nxt);
+    }
+    finish_node<T, ODD, EXACT, MOVING, BFU>(a, nb, nb.at(0, 0, 0), fl[r], cur);
+    if (more) {
+#pragma unroll
+      for (int q = 0; q < 15; q++) cur[q] = nxt[q];
+      nb = nbn;
+    }
   }
 }
 

@@ -53,7 +53,8 @@ static int flat_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 template <bool ODD, bool MOVING, bool BFU>
 static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
   const dim3 grid((unsigned)((L.esk + bx - 1) / bx), (unsigned)((L.esj + npt - 1) / npt), (unsigned)L.esi);
-  if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2><<<grid, bx, 0, L.stream>>>(a);
+  if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4><<<grid, bx, 0, L.stream>>>(a);
+  else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2><<<grid, bx, 0, L.stream>>>(a);
   else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1><<<grid, bx, 0, L.stream>>>(a);
 }
 

@@ -381,6 +381,11 @@ int lbtuning(LBSys lb, int *cfg) {
   return slbc_get_tuning(st->dev, cfg);
 }
 
+int lblayout(LBSys lb) {
+  slb_priv *st = slb_state(lb);
+  return st->dev == NULL ? -1 : slbc_layout(st->dev);
+}
+
 /* ---- printing and bookkeeping (reference src/lbmisc.c:156-412) ---------- */
 
 void about() {

@@ -25,6 +25,7 @@ populations, converged flow at body force b), see converged_flows.
 
 import ctypes as C
 import math
+import os
 import time
 
 import numpy as np
@@ -380,6 +381,47 @@ class UNet:
 
 
 # ---- data ------------------------------------------------------------------------
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warm_unet.npz")
+
+
+def save_weights(net, path, meta=None):
+    """The network's weights and biases as BF16 bit patterns (the precision
+    the tensor-core kernels use) in an .npz file, with the widths and any
+    metadata (a JSON string)."""
+    import json
+    arrays = {}
+    for name, *_ in net.layers:
+        for key in ("w", "b"):
+            t = net.params[name][key].detach().float().contiguous().cpu()
+            bits = t.view(-1).numpy().view(np.uint32)
+            # round to nearest even BF16
+            rounded = ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16)
+            arrays[f"{name}.{key}"] = rounded.reshape(tuple(t.shape))
+    arrays["widths"] = np.array(net.widths, dtype=np.int32)
+    arrays["features"] = np.array([net.features], dtype=np.int32)
+    arrays["meta"] = np.frombuffer(json.dumps(meta or {}).encode(), dtype=np.uint8)
+    tmp = path + ".tmp.npz"
+    np.savez_compressed(tmp, **arrays)
+    os.replace(tmp, path)
+
+
+def load_weights(path=WEIGHTS):
+    """(params, widths, features, meta) of a file written by save_weights;
+    params as FP32 device tensors, the form UNet(params=...) takes."""
+    import json
+    import torch
+    z = np.load(path)
+    params = {}
+    for key in z.files:
+        if "." not in key:
+            continue
+        name, kind = key.split(".")
+        f32 = (z[key].astype(np.uint32) << 16).view(np.float32)
+        params.setdefault(name, {})[kind] = torch.as_tensor(f32.copy(), device="cuda")
+    meta = json.loads(bytes(z["meta"]).decode()) if "meta" in z.files else {}
+    return params, tuple(int(v) for v in z["widths"]), int(z["features"][0]), meta
+
 
 def packing_specs(n, seed, phi_range=(0.1, 0.5), r_range=(3.0, 8.0)):
     """Seeded (phi, packing seed) pairs; spheres may overlap (a Boolean model),

@@ -185,3 +185,42 @@ def test_file_api_equals_reference_build_live(orc, ref_strict, tmp_path):
     assert fo.keys() == fr.keys()
     for k in fo:
         assert fo[k] == fr[k], k
+
+
+def _time_lib(path):
+    import ctypes as C
+    lib = C.CDLL(path)
+    f = lib.orc_time_steps
+    f.restype = C.c_double
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
+                  C.c_void_p]
+    return lib, f
+
+
+@pytest.mark.parametrize("bits", ["64", "32"])
+def test_timing_builds_step_like_reference(bits):
+    """The CPU-baseline builds (the oracle under the reference's shipped
+    -O3 -ffast-math flags, double and -D_SINGLE) advance a packed lattice
+    like the reference's own sources compiled the same way: the population
+    sums after 40 Navier-Stokes steps agree to the precision's round-off."""
+    import ctypes as C
+    from sunlightlb_gb300 import build as b
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    mine = os.path.join(root, "oracle", f"liboracle_time{bits}.so")
+    ref = os.path.join(root, "oracle", "_ref", f"libref_time{bits}.so")
+    if not os.path.exists(mine):
+        b.build_oracle(with_reference=False)
+    if not os.path.exists(ref):
+        pytest.skip("reference build not available (built only where the reference sources are)")
+    from sunlightlb_gb300 import workloads as W
+    _, solid = W.rsa_packing(24, 0.3, 2.0, 4.0, 9)
+    mask = np.ascontiguousarray(solid, dtype=np.uint8)
+    sums = []
+    for path in (mine, ref):
+        lib, f = _time_lib(path)
+        assert lib.orc_real_size() == int(bits) // 8
+        cs = C.c_double()
+        assert f(mask.ctypes.data, 24, 24, 24, 0.7, 0, 1e-3, 0, 40, C.byref(cs)) >= 0.0
+        sums.append(cs.value)
+    tol = 1e-10 if bits == "64" else 2e-4
+    assert abs(sums[0] - sums[1]) <= tol * max(abs(sums[1]), 1e-30), sums
