@@ -86,6 +86,27 @@ int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj,
 /* Adsorption bits (0x4000 of the reference mask) of every node, 1 byte per
  * node (reference src/mpads.c:28-44). */
 int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads);
+/* 1 when the body force is one constant over the fluid nodes (returned in
+ * b), 0 when it is held per node. */
+int slbc_bodyforce_uniform(slbc_lattice *h, double b[3]);
+/* Translate the spherical object of dense index obj (radius rad, centre
+ * oldc, with its periodic images) to the centre newc, on the GPU (no
+ * counterpart in the reference, which can only remove and re-insert
+ * objects).  Nodes of the object the sphere no longer covers become fluid
+ * at the equilibrium of density rho0 and the wall velocity vel + ang x r
+ * (r = node - newc); fluid nodes it now covers join the object, their
+ * populations unchanged; nodes of other objects are left alone; with
+ * with_wallvel the wall velocities of the object's nodes are recomputed
+ * (the vspread formula).  The changes come back in changed[2 * e] (node)
+ * and changed[2 * e + 1] (new object index or -1), room for cap of them,
+ * their number in *nchanged.  The flag words are rebuilt and the boundary
+ * list with them, grouped by the caller's host copy of the dense object map
+ * objidx_host (nobj objects), which this call updates with the changes; the
+ * list comes back as in slbc_set_geometry_auto. */
+int slbc_move_sphere(slbc_lattice *h, int obj, double rad, const double oldc[3], const double newc[3],
+                     const double vel[3], const double ang[3], int with_wallvel, int *changed, long cap,
+                     long *nchanged, int nobj, int *objidx_host, long **bnd_node, int **bnd_obj,
+                     long *nbnd);
 int slbc_set_params(slbc_lattice *h, const slbc_params *p);
 /* Body force per node (NULL = zero); a force uniform over the fluid nodes is
  * detected and kept as a kernel constant (reference src/lbobjs.c:593-619). */

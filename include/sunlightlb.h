@@ -364,6 +364,17 @@ LBObj insertmask(LBSys, unsigned char *);
 int rsapacking(int n, double phi, double rmin, double rmax, unsigned long long seed, int overlap,
                long max_tries, double *spheres, int max_spheres, unsigned char *solid);
 
+/* Move the spherical object obj of radius rad (a sphere with its periodic
+ * images, as insertsph + flattenobj build it) so that its centre is
+ * (x, y, z): the node set is re-rasterised on the GPU, nodes the sphere
+ * leaves become fluid at the equilibrium of density rho0 and the wall
+ * velocity v + w x r there, fluid nodes it reaches join the object, and the
+ * flag words, boundary list, mask, a uniform body force, the object's wall
+ * velocities (when objects move) and obj->pos follow.  No counterpart in the
+ * reference, which can only remove objects and insert new ones
+ * (src/lbobjs.c:433-453).  FP32 or FP64 populations. */
+void lbtranslate(LBSys, LBObj, LBReal, LBReal, LBReal, LBReal);
+
 /* Batches (no counterpart in the reference): many independent lattices of
  * one precision (FP32 or FP64), each set up as usual, advanced together by
  * batchsteps in one persistent GPU launch; afterwards each lattice is used

@@ -999,6 +999,96 @@ void lbsavemap(LBSys lb, char *mapfile, char *type) {
 }
 
 /* ------------------------------------------------------------------------
+ * translating a spherical object -- an extension of the GPU library with no
+ * counterpart in the reference (which can only remove objects and insert
+ * new ones, src/lbobjs.c:433-453); this is the rule the library's
+ * lbtranslate implements, written plainly:
+ *  - nodes examined: the box around the old and the new sphere (one node of
+ *    margin), taken modulo the lattice;
+ *  - a node is inside when rsq < rad^2 for the new centre or one of its 26
+ *    periodic images (insertsph's test, src/lbobjs.c:214-215);
+ *  - a node of the object that is no longer inside becomes fluid with the
+ *    equilibrium populations of density rho0 and velocity v + w x r
+ *    (r = node - new centre, the vspread convention), rebuilt as lbloadvel
+ *    does (src/lbstore.c:352-389); with a uniform body force it gets that
+ *    force;
+ *  - a fluid node now inside joins the object (populations unchanged, body
+ *    force removed when uniform); other objects' nodes are left alone;
+ *  - the mask of the changed nodes and their neighbours is rebuilt (their
+ *    adsorption bits cleared), the object's wall velocities recomputed when
+ *    objects move, pos set to the new centre.
+ * ---------------------------------------------------------------------- */
+void lbtranslate(LBSys lb, LBObj p, LBReal rad, LBReal x, LBReal y, LBReal z) {
+  int dims[3] = {lb->esi, lb->esj, lb->esk}, lo[3], len[3], a, ia, ib, ic, uniform = 1, found = 0;
+  double c[3] = {x, y, z}, oc[3] = {p->posx, p->posy, p->posz}, b[3] = {0.0, 0.0, 0.0}, rr = rad * rad;
+  long n, nn = lb->nnodes;
+  unsigned char *touched = (unsigned char *)zalloc(nn);
+  for (n = 0; n < nn && uniform; n++) {
+    if (lb->obj[n] != NULL) continue;
+    if (!found) { b[0] = lb->bx[n]; b[1] = lb->by[n]; b[2] = lb->bz[n]; found = 1; }
+    else if (lb->bx[n] != b[0] || lb->by[n] != b[1] || lb->bz[n] != b[2]) uniform = 0;
+  }
+  for (a = 0; a < 3; a++) {
+    double l0 = floor((oc[a] < c[a] ? oc[a] : c[a]) - rad - 1.0);
+    double l1 = ceil((oc[a] > c[a] ? oc[a] : c[a]) + rad + 1.0);
+    long s0 = (long)l0, ln = (long)l1 - s0 + 1;
+    if (ln >= dims[a] || !(ln > 0)) { s0 = 0; ln = dims[a]; }
+    s0 %= dims[a];
+    if (s0 < 0) s0 += dims[a];
+    lo[a] = (int)s0; len[a] = (int)ln;
+  }
+  for (ia = 0; ia < len[0]; ia++) for (ib = 0; ib < len[1]; ib++) for (ic = 0; ic < len[2]; ic++) {
+    int node3[3] = {(lo[0] + ia) % dims[0], (lo[1] + ib) % dims[1], (lo[2] + ic) % dims[2]}, di, dj, dk, inside = 0;
+    double r[3], v[3];
+    for (di = -1; di <= 1; di++) for (dj = -1; dj <= 1; dj++) for (dk = -1; dk <= 1; dk++) {
+      double ic0 = c[0] + di * dims[0], ic1 = c[1] + dj * dims[1], ic2 = c[2] + dk * dims[2];
+      double rsq = (node3[0] - ic0) * (node3[0] - ic0) + (node3[1] - ic1) * (node3[1] - ic1)
+                   + (node3[2] - ic2) * (node3[2] - ic2);
+      if (rsq < rr) inside = 1;
+    }
+    n = node(lb, node3[0], node3[1], node3[2]);
+    if (lb->obj[n] == p && !inside) {
+      LBReal rux, ruy, ruz, sxx = 0.0, syy = 0.0, szz = 0.0, sxy = 0.0, sxz = 0.0, syz = 0.0;
+      for (a = 0; a < 3; a++) r[a] = node3[a] - c[a];
+      v[0] = p->velx + p->angy * r[2] - p->angz * r[1];
+      v[1] = p->vely + p->angz * r[0] - p->angx * r[2];
+      v[2] = p->velz + p->angx * r[1] - p->angy * r[0];
+      rux = lb->rho0 * v[0]; ruy = lb->rho0 * v[1]; ruz = lb->rho0 * v[2];
+      if (!lb->stokes_flow) {
+        sxx = v[0] * rux; sxy = v[0] * ruy; sxz = v[0] * ruz;
+        syy = v[1] * ruy; syz = v[1] * ruz; szz = v[2] * ruz;
+      }
+      rebuild(lb->a + 15 * n, 0.0, rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
+      lb->obj[n] = NULL;
+      if (uniform) { lb->bx[n] = b[0]; lb->by[n] = b[1]; lb->bz[n] = b[2]; }
+      touched[n] = 1;
+    } else if (lb->obj[n] == NULL && inside) {
+      lb->obj[n] = p;
+      if (uniform) lb->bx[n] = lb->by[n] = lb->bz[n] = 0.0;
+      touched[n] = 1;
+    }
+  }
+  p->posx = x; p->posy = y; p->posz = z;
+  /* mask of the changed nodes and their neighbours (reference makemask rule) */
+  for (n = 0; n < nn; n++) {
+    int i, j, k, q;
+    if (!touched[n]) continue;
+    k = (int)(n % lb->esk); j = (int)((n / lb->esk) % lb->esj); i = (int)(n / ((long)lb->esk * lb->esj));
+    for (q = 0; q < 15; q++) {
+      int ii = (i + CX[q] + lb->esi) % lb->esi, jj = (j + CY[q] + lb->esj) % lb->esj;
+      int kk = (k + CZ[q] + lb->esk) % lb->esk, r2, val = 0;
+      long m = node(lb, ii, jj, kk);
+      if (lb->obj[m] != NULL)
+        for (r2 = 1; r2 < 15; r2++)
+          if (lb->obj[nbr(lb, ii, jj, kk, r2)] == NULL) val |= 1 << (r2 - 1);
+      lb->mask[m] = val;
+    }
+  }
+  free(touched);
+  if (lb->objects_moving) vspread(lb);
+}
+
+/* ------------------------------------------------------------------------
  * appended helpers so drivers written for the GPU library run unchanged
  * ---------------------------------------------------------------------- */
 

@@ -12,6 +12,7 @@
 #include <vector>
 #include <atomic>
 #include <algorithm>
+#include <cmath>
 
 #include "slbc_internal.cuh"
 #include "slbc_kernels.cuh"
@@ -905,11 +906,22 @@ int slbc_set_geometry(slbc_lattice *h, const int *objidx, int nobj, const long *
   return geometry_boundary(L, nobj, bnd_node, bnd_obj, nbnd);
 }
 
+// boundary nodes in node order, found on the GPU from the flag words, then
+// grouped by object (objidx: the host copy of the object map)
+static int boundary_from_flags(Lattice &L, const int *objidx, int nobj, long **bnd_node_out, int **bnd_obj_out,
+                               long *nbnd_out);
+
 int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj, long **bnd_node_out,
                            int **bnd_obj_out, long *nbnd_out) {
   Lattice &L = h->L;
   *bnd_node_out = nullptr; *bnd_obj_out = nullptr; *nbnd_out = 0;
   if (geometry_flags(L, h, objidx)) return 1;
+  return boundary_from_flags(L, objidx, nobj, bnd_node_out, bnd_obj_out, nbnd_out);
+}
+
+static int boundary_from_flags(Lattice &L, const int *objidx, int nobj, long **bnd_node_out, int **bnd_obj_out,
+                               long *nbnd_out) {
+  *bnd_node_out = nullptr; *bnd_obj_out = nullptr; *nbnd_out = 0;
   // boundary nodes in node order, found on the GPU from the flag words
   const int nb = (int)((L.nnodes + kBndChunk - 1) / kBndChunk);
   int *counts = nullptr, *list = nullptr;
@@ -954,6 +966,75 @@ int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj, long **
   if (geometry_boundary(L, nobj, bn, bo, total)) { free(bn); free(bo); return 1; }
   *bnd_node_out = bn; *bnd_obj_out = bo; *nbnd_out = total;
   return 0;
+}
+
+int slbc_bodyforce_uniform(slbc_lattice *h, double b[3]) {
+  const Lattice &L = h->L;
+  b[0] = L.bf_const[0]; b[1] = L.bf_const[1]; b[2] = L.bf_const[2];
+  return L.bf_uniform;
+}
+
+int slbc_move_sphere(slbc_lattice *h, int obj, double rad, const double oldc[3], const double newc[3],
+                     const double vel[3], const double ang[3], int with_wallvel, int *changed, long cap,
+                     long *nchanged, int nobj, int *objidx_host, long **bnd_node_out, int **bnd_obj_out,
+                     long *nbnd_out) {
+  Lattice &L = h->L;
+  *nchanged = 0;
+  if (L.precision == 2) return fail_msg("moving a sphere needs FP32 or FP64 populations (lb->precision)");
+  if (!(rad > 0.0) || obj < 0 || obj >= nobj) return fail_msg("slbc_move_sphere: bad object or radius");
+  if (with_wallvel && L.uw == nullptr) return fail_msg("slbc_move_sphere: no wall velocity arrays");
+  if (L.layout == SLBC_LAYOUT_C1 && to_natural(L)) return 1;
+  // the box: old and new node sets with a node of margin, at most the lattice
+  MoveArgs m;
+  const int dims[3] = {L.esi, L.esj, L.esk};
+  for (int a = 0; a < 3; a++) {
+    const double lo = std::min(oldc[a], newc[a]) - rad - 1.0, hi = std::max(oldc[a], newc[a]) + rad + 1.0;
+    long long l0 = (long long)std::floor(lo), len = (long long)std::ceil(hi) - l0 + 1;
+    if (len >= dims[a] || !(len > 0)) { l0 = 0; len = dims[a]; }
+    l0 %= dims[a];
+    if (l0 < 0) l0 += dims[a];
+    m.lo[a] = (int)l0;
+    m.len[a] = (int)len;
+    m.c[a] = newc[a];
+    m.vel[a] = vel[a];
+    m.ang[a] = ang[a];
+  }
+  m.rad = rad;
+  m.rho0 = L.par.rho0;
+  m.obj = obj;
+  m.stokes = L.par.stokes_flow;
+  m.layout = L.layout;
+  m.objidx = L.objidx;
+  m.cap = (int)std::min<long>(cap, 1L << 30);
+  int *dev_list = nullptr;
+  CK(cudaMalloc(&dev_list, (size_t)(2 * (long)m.cap + 1) * sizeof(int)));
+  m.nchanged = dev_list;
+  m.changed = dev_list + 1;
+  cudaError_t e = cudaMemsetAsync(dev_list, 0, sizeof(int), L.stream);
+  if (e == cudaSuccess) e = DISPATCH(L, launch_move_sphere, L, m, with_wallvel);
+  int count = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&count, dev_list, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  if (e == cudaSuccess && count > 0)
+    e = cudaMemcpy(changed, dev_list + 1, (size_t)2 * std::min(count, m.cap) * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dev_list);
+  if (e != cudaSuccess) return fail("slbc_move_sphere", e);
+  *nchanged = count;
+  if (count > m.cap) return fail_msg("slbc_move_sphere: more changed nodes than the list holds");
+  for (int c = 0; c < count; c++) {
+    h->solid_host[changed[2 * c]] = changed[2 * c + 1] >= 0;
+    objidx_host[changed[2 * c]] = changed[2 * c + 1];
+  }
+  L.state_version++;
+  L.ads_version++;  // the boundary links change
+  L.generation++;
+  // flag words from the updated map, then the boundary list
+  const int bx = L.esk >= 128 ? 128 : 32;
+  dim3 grid((L.esk + bx - 1) / bx, L.esj, L.esi);
+  k_flags<<<grid, bx, 0, L.stream>>>(L.objidx, L.flags, L.esi, L.esj, L.esk);
+  count_launch();
+  CK(cudaGetLastError());
+  return boundary_from_flags(L, objidx_host, nobj, bnd_node_out, bnd_obj_out, nbnd_out);
 }
 
 int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads) {

@@ -152,6 +152,8 @@ struct ForceArgs {
   double *f;     // 3 * nbnd
 };
 
+struct MoveArgs;
+
 // Per-precision launchers (defined in slbc_f64.cu / slbc_f32.cu).
 // Device side of a batch of lattices advanced by one persistent launch.
 // Lattices of one batch launch share whether walls move and whether the
@@ -200,6 +202,8 @@ struct BatchState {
                                      long long x0, long long n, int has_rho,    \
                                      int skip_solid);                           \
   cudaError_t launch_mp_rhoinit_##SUFFIX(Lattice &L);                           \
+  cudaError_t launch_move_sphere_##SUFFIX(Lattice &L, const MoveArgs &m,       \
+                                          int with_uw);                         \
   cudaError_t launch_mp_step_##SUFFIX(Lattice &L, const void *p_in, void *p_out, \
                                       int tp_f64, double alpha, double adprob,  \
                                       int moving, const double *objstate,       \

@@ -719,6 +719,102 @@ __global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long l
   for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = t[q];
 }
 
+// Translation of one spherical object (appended operation, no counterpart
+// in the reference, which can only remove objects and insert new ones):
+// every node of the box `lo`, `len` (indices taken modulo the lattice, so
+// the box may wrap) is tested against the sphere of radius rad at the new
+// centre and its periodic images -- rsq < rad^2 per image, evaluated like
+// insertsph (reference src/lbobjs.c:214-215), without FMA contraction so the
+// set is the same as on the host.  A node of the object that the sphere no
+// longer covers becomes fluid with the equilibrium populations of density
+// rho0 and the wall velocity v + w x r there (r = node - new centre, the
+// reference's vspread convention), rebuilt like lbloadvel's
+// (src/lbstore.c:352-389); a fluid node it now covers joins the object with
+// its populations left as they are.  Nodes of other objects are left alone.
+// Wall velocities rho0 (v + w x r) / 12 (src/lbobjs.c:580-582) are written
+// for every node of the object in the box when uw is given.  Each change is
+// appended to `changed` as (node, new object index or -1), atomically, at
+// most `cap` of them (the count keeps going, so the host sees an overflow).
+// The state must be in a local layout: N (pop[q][x] = a_q(x)) or C0
+// (pop[opp q][x] = a_q(x)).
+struct MoveArgs {
+  double c[3];
+  double rad, rho0;
+  double vel[3], ang[3];
+  int obj, stokes, layout;
+  int lo[3], len[3];
+  int *objidx;
+  int *changed;
+  int *nchanged;
+  int cap;
+};
+
+template <typename T, bool EXACT>
+__global__ void k_move_sphere(PopArgs<T> p, MoveArgs m, T *uw) {
+  const long long nbox = (long long)m.len[0] * m.len[1] * m.len[2];
+  const double rr = __dmul_rn(m.rad, m.rad);
+  const int L3[3] = {p.esi, p.esj, p.esk};
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nbox;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(e / ((long long)m.len[1] * m.len[2]));
+    const int b = (int)((e / m.len[2]) % m.len[1]);
+    const int c = (int)(e % m.len[2]);
+    const int n3[3] = {wrap_index(m.lo[0] + a, p.esi), wrap_index(m.lo[1] + b, p.esj), wrap_index(m.lo[2] + c, p.esk)};
+    bool inside = false;
+    for (int di = -1; di <= 1 && !inside; di++)
+      for (int dj = -1; dj <= 1 && !inside; dj++)
+        for (int dk = -1; dk <= 1 && !inside; dk++) {
+          const int d3[3] = {di, dj, dk};
+          double sq = 0.0;
+#pragma unroll
+          for (int q = 0; q < 3; q++) {
+            const double cq = __dadd_rn(m.c[q], (double)(d3[q] * L3[q]));
+            const double dq = __dsub_rn((double)n3[q], cq);
+            sq = q == 0 ? __dmul_rn(dq, dq) : __dadd_rn(sq, __dmul_rn(dq, dq));
+          }
+          inside = sq < rr;
+        }
+    const int x = (n3[0] * p.esj + n3[1]) * p.esk + n3[2];
+    const int o = m.objidx[x];
+    const bool uncovered = o == m.obj && !inside;
+    const bool covered = o == -1 && inside;
+    // wall velocity at the node (reference vspread: r = node - centre)
+    const double rx = __dsub_rn((double)n3[0], m.c[0]);
+    const double ry = __dsub_rn((double)n3[1], m.c[1]);
+    const double rz = __dsub_rn((double)n3[2], m.c[2]);
+    const double vx = __dsub_rn(__dadd_rn(m.vel[0], __dmul_rn(m.ang[1], rz)), __dmul_rn(m.ang[2], ry));
+    const double vy = __dsub_rn(__dadd_rn(m.vel[1], __dmul_rn(m.ang[2], rx)), __dmul_rn(m.ang[0], rz));
+    const double vz = __dsub_rn(__dadd_rn(m.vel[2], __dmul_rn(m.ang[0], ry)), __dmul_rn(m.ang[1], rx));
+    if (uncovered) {
+      const T r0 = (T)m.rho0, ux = (T)vx, uy = (T)vy, uz = (T)vz;
+      const T rux = r0 * ux, ruy = r0 * uy, ruz = r0 * uz;
+      T sxx = T(0), syy = T(0), szz = T(0), sxy = T(0), sxz = T(0), syz = T(0);
+      if (!m.stokes) {
+        sxx = ux * rux; sxy = ux * ruy; sxz = ux * ruz;
+        syy = uy * ruy; syz = uy * ruz; szz = uz * ruz;
+      }
+      T t[15];
+      rebuild<T, EXACT>(t, T(0), rux, ruy, ruz, sxx, syy, szz, sxy, sxz, syz);
+#pragma unroll
+      for (int q = 0; q < 15; q++) p.pop[(m.layout == SLBC_LAYOUT_C0 ? OPP(q) : q) * p.npad + x] = t[q];
+    }
+    if (uncovered || covered) {
+      m.objidx[x] = covered ? m.obj : -1;
+      const int slot = atomicAdd(m.nchanged, 1);
+      if (slot < m.cap) {
+        m.changed[2 * slot] = x;
+        m.changed[2 * slot + 1] = covered ? m.obj : -1;
+      }
+    }
+    if (uw != nullptr && (uncovered || inside && (o == m.obj || o == -1))) {
+      const double s = m.rho0;
+      uw[x] = uncovered ? T(0) : (T)__ddiv_rn(__dmul_rn(s, vx), 12.0);
+      uw[p.npad + x] = uncovered ? T(0) : (T)__ddiv_rn(__dmul_rn(s, vy), 12.0);
+      uw[2 * p.npad + x] = uncovered ? T(0) : (T)__ddiv_rn(__dmul_rn(s, vz), 12.0);
+    }
+  }
+}
+
 // Velocity field u = (sum_q c_q a_q + fac * b) / (rho0 + sum_q a_q) of the
 // post-collision state (any layout) on fluid nodes, 0 on solid nodes, as
 // three FP32 arrays (the per-node form of the accvmean sum).

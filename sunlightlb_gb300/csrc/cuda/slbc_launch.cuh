@@ -282,6 +282,14 @@ cudaError_t SLBC_FN(launch_setvel)(Lattice &L, const double *stage, long long x0
   return cudaGetLastError();
 }
 
+cudaError_t SLBC_FN(launch_move_sphere)(Lattice &L, const MoveArgs &m, int with_uw) {
+  const long long nbox = (long long)m.len[0] * m.len[1] * m.len[2];
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((nbox + 255) / 256, 152LL * 8));
+  k_move_sphere<T_, SLBC_EXACT><<<blocks, 256, 0, L.stream>>>(pop_args(L), m, with_uw ? (T_ *)L.uw : nullptr);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t SLBC_FN(launch_velocity)(Lattice &L, double fac, float *u, float *drho) {
   const int blocks = (int)std::min<long long>((L.nnodes + 255) / 256, 152LL * 16);
   k_velocity<T_><<<blocks, 256, 0, L.stream>>>(pop_args(L), L.layout, L.par.rho0, fac, L.bf_uniform, L.bf_const[0],

@@ -225,7 +225,8 @@ static void upload_geometry(LBSys lb) {
   free(st->objs);
   st->objs = objs;
   st->nobj = nobj;
-  free(objidx);
+  free(st->objidx);
+  st->objidx = objidx;  /* kept: moves of objects update it in place */
   st->geom_sent = st->geom_gen;
   /* solidity changed: body-force uniformity must be re-checked */
   st->bf_sent = 0;
@@ -360,7 +361,7 @@ void freelb(LBSys lb) {
   st = slb_state(lb);
   if (st->dev) slbc_destroy(st->dev);
   if (st->a_pinned) slbc_host_free(lb->a); else free(lb->a);
-  free(st->objs); free(st->bnd_node); free(st->bnd_obj); free(st);
+  free(st->objs); free(st->objidx); free(st->bnd_node); free(st->bnd_obj); free(st);
   p = lb->obj_head;
   while (p != NULL) { pp = p; p = p->next_obj; free(pp); }
   free(lb->mask); free(lb->obj);

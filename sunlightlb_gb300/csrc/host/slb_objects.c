@@ -421,6 +421,120 @@ void vspread(LBSys lb) {
   slb_trace(lb, "vspread");
 }
 
+/* mask bits of one node (reference src/lbobjs.c:537-556): bit q-1 when the
+ * node is solid and its neighbour along c_q is fluid; clears 0x4000 */
+static void mask_node(LBSys lb, int i, int j, int k) {
+  long x = slb_node(lb, i, j, k);
+  int q, val = 0;
+  if (lb->obj[x] != NULL)
+    for (q = 1; q < 15; q++) {
+      int ii = (i + LX[q] + lb->esi) % lb->esi;
+      int jj = (j + LY[q] + lb->esj) % lb->esj;
+      int kk = (k + LZ[q] + lb->esk) % lb->esk;
+      if (lb->obj[slb_node(lb, ii, jj, kk)] == NULL) val |= 1 << (q - 1);
+    }
+  lb->mask[x] = val;
+}
+
+/* appended, no counterpart in the reference (which can only remove objects
+ * and insert new ones): move the spherical object p of radius rad -- a
+ * sphere and its periodic images, as insertsph and flattenobj build it --
+ * so that its centre is (x, y, z).  The node set is re-rasterised on the
+ * GPU; nodes the sphere leaves become fluid at the equilibrium of density
+ * rho0 and the wall velocity there (v + w x r, r = node - new centre),
+ * fluid nodes it reaches join the object with their populations as they
+ * are; nodes of other objects are left alone.  The host copies follow:
+ * object map, mask (adsorption bits of the changed nodes and their
+ * neighbours cleared), fluid count, a uniform body force (given to the new
+ * fluid nodes and taken from the new solid ones; a per-node force is left
+ * as it is), the wall velocities of the object when objects move, and
+ * p->pos.  FP32 or FP64 populations. */
+void lbtranslate(LBSys lb, LBObj p, LBReal rad, LBReal x, LBReal y, LBReal z) {
+  slb_priv *st;
+  slbc_lattice *dev;
+  int oi = -1, e, uniform, ads_touched = 0, a;
+  double oldc[3], newc[3], vel[3], ang[3], b[3];
+  long cap, nch = 0, nb = 0, box = 1;
+  int *changed;
+  if (p == NULL) { printf("lbtranslate: no object\n"); return; }
+  if (lb->changed_objects) syncobjs(lb);
+  dev = slb_device(lb);
+  st = slb_state(lb);
+  for (e = 0; e < st->nobj; e++) if (st->objs[e] == p) { oi = e; break; }
+  if (oi < 0) { printf("lbtranslate: object %i has no nodes on the lattice\n", p->id); return; }
+  oldc[0] = p->posx; oldc[1] = p->posy; oldc[2] = p->posz;
+  newc[0] = x; newc[1] = y; newc[2] = z;
+  vel[0] = p->velx; vel[1] = p->vely; vel[2] = p->velz;
+  ang[0] = p->angx; ang[1] = p->angy; ang[2] = p->angz;
+  {
+    int dims[3] = {lb->esi, lb->esj, lb->esk};
+    for (a = 0; a < 3; a++) {
+      double span = fabs(newc[a] - oldc[a]) + 2.0 * rad + 4.0;
+      box *= span < dims[a] ? (long)span : dims[a];
+    }
+  }
+  cap = box;
+  changed = (int *)xcalloc(2 * (size_t)cap, sizeof(int));
+  uniform = slbc_bodyforce_uniform(dev, b);
+  free(st->bnd_node); free(st->bnd_obj);
+  st->bnd_node = NULL; st->bnd_obj = NULL;
+  slb_check(slbc_move_sphere(dev, oi, rad, oldc, newc, vel, ang, lb->objects_moving && st->uw_sent == st->uw_gen,
+                             changed, cap, &nch, st->nobj, st->objidx, &st->bnd_node, &st->bnd_obj, &nb),
+            "sphere translation");
+  st->nbnd = nb;
+  p->posx = x; p->posy = y; p->posz = z;
+  for (e = 0; e < nch; e++) {
+    long n = changed[2 * e];
+    int now_solid = changed[2 * e + 1] >= 0;
+    lb->obj[n] = now_solid ? p : NULL;
+    st->nfluid += now_solid ? -1 : 1;
+    if (uniform) {
+      lb->bx[n] = now_solid ? 0.0 : b[0];
+      lb->by[n] = now_solid ? 0.0 : b[1];
+      lb->bz[n] = now_solid ? 0.0 : b[2];
+    }
+    if (lb->objects_moving && !now_solid) lb->ux[n] = lb->uy[n] = lb->uz[n] = 0.0;
+  }
+  /* mask of the changed nodes and of their neighbours */
+  for (e = 0; e < nch; e++) {
+    long n = changed[2 * e];
+    int k = (int)(n % lb->esk), j = (int)((n / lb->esk) % lb->esj), i = (int)(n / ((long)lb->esk * lb->esj)), q;
+    for (q = 0; q < 15; q++) {
+      int ii = (i + LX[q] + lb->esi) % lb->esi, jj = (j + LY[q] + lb->esj) % lb->esj;
+      int kk = (k + LZ[q] + lb->esk) % lb->esk;
+      long m = slb_node(lb, ii, jj, kk);
+      if (lb->mask[m] & 0x4000) ads_touched = 1;  /* adsorption bit, cleared by the rebuild */
+      mask_node(lb, ii, jj, kk);
+    }
+  }
+  /* wall velocities of the object's nodes around the sphere (vspread) */
+  if (lb->objects_moving) {
+    int lo[3], len[3], dims[3] = {lb->esi, lb->esj, lb->esk}, ia, ib, ic;
+    LBReal u[3];
+    for (a = 0; a < 3; a++) {
+      double l0 = floor(newc[a] - rad - 1.0), l1 = ceil(newc[a] + rad + 1.0);
+      lo[a] = (int)l0;
+      len[a] = (int)(l1 - l0) + 1;
+      if (len[a] >= dims[a]) { lo[a] = 0; len[a] = dims[a]; }
+    }
+    for (ia = 0; ia < len[0]; ia++) for (ib = 0; ib < len[1]; ib++) for (ic = 0; ic < len[2]; ic++) {
+      int i = ((lo[0] + ia) % dims[0] + dims[0]) % dims[0];
+      int j = ((lo[1] + ib) % dims[1] + dims[1]) % dims[1];
+      int k = ((lo[2] + ic) % dims[2] + dims[2]) % dims[2];
+      long n = slb_node(lb, i, j, k);
+      if (lb->obj[n] != p) continue;
+      wall_u(lb, p, i, j, k, u);
+      lb->ux[n] = u[0]; lb->uy[n] = u[1]; lb->uz[n] = u[2];
+    }
+    if (st->uw_sent != st->uw_gen) slb_mark_wallvel(lb);  /* not on the GPU yet: full upload */
+  }
+  free(changed);
+  if (ads_touched) slb_mark_ads(lb);
+  st->host_f_valid = 0;
+  lb->changed_objects = 0;
+  slb_trace(lb, "lbtranslate");
+}
+
 /* reference src/lbobjs.c:593-604 */
 void zerobf(LBSys lb) {
   long x;

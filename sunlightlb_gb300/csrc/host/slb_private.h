@@ -26,6 +26,7 @@ typedef struct slb_priv {
   /* dense object table of the last geometry upload */
   int nobj;
   LBObj *objs;                /* index -> object */
+  int *objidx;                /* dense object index per node (-1 fluid), as on the GPU */
   long nbnd;
   long *bnd_node;             /* solid nodes with a fluid neighbour */
   int *bnd_obj;

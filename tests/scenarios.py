@@ -163,3 +163,47 @@ def mpsubs_case(L, outdir, n=10, steps=15):
     if L.has("mppull"):
         L.mppull(mp)
     return p0, mp.field().copy()
+
+
+def translate_case(L, dims=(20, 18, 22), rad=3.6, centre=(17.3, 8.1, 1.7), step=(0.61, -0.43, 0.29), moves=6,
+                   every=7, moving=1, stokes=1, skip=0, tau=0.8, precision=0, bf=(1e-4, 2e-5, 0.0),
+                   ang=(0.0, 0.0, 1e-3), measure=True):
+    """A sphere (with its periodic images, flattened into one object) near
+    the periodic boundary, translated by `step` every `every` update steps
+    (an odd count, so moves meet both storage layouts), `moves` times, then
+    measured.  Returns (lb, obj)."""
+    from sunlightlb_gb300 import workloads as W
+    lb = L.newlb(dims[0], dims[1], dims[2], "null")
+    if L.extended:
+        lb.precision = precision
+    lb.tau = tau
+    lb.stokes_flow = stokes
+    lb.skip_solid = skip
+    lb.objects_moving = moving
+    c = list(centre)
+    for im in W.images(dims, rad, c):
+        L.insertsph(lb, rad, im[0], im[1], im[2])
+    obj = L.flattenobj(lb)
+    obj.posx, obj.posy, obj.posz = c  # flattenobj leaves the centroid of the nodes
+    obj.velx, obj.vely, obj.velz = (step[0] / every * 0.05, step[1] / every * 0.05, step[2] / every * 0.05)
+    obj.angx, obj.angy, obj.angz = ang
+    L.syncobjs(lb)
+    if moving:
+        L.vspread(lb)
+    L.addbf(lb, *bf)
+    for _ in range(moves):
+        for _ in range(every):
+            L.lbstep(lb)
+        c = [c[a] + step[a] for a in range(3)]
+        L.lbtranslate(lb, obj, rad, *c)
+    if measure:
+        for _ in range(every):
+            L.lbstep(lb)
+        L.measure(lb)
+    return lb, obj
+
+
+def object_ids(lb):
+    ids = {o.address: o.id for o in lb.objects()}
+    raw = lb.array("obj")
+    return np.array([ids.get(int(p), -2) if p else -1 for p in raw])

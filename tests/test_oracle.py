@@ -224,3 +224,24 @@ def test_timing_builds_step_like_reference(bits):
         sums.append(cs.value)
     tol = 1e-10 if bits == "64" else 2e-4
     assert abs(sums[0] - sums[1]) <= tol * max(abs(sums[1]), 1e-30), sums
+
+
+def test_translated_sphere_node_set(orc):
+    """The translation rule (an extension without a reference counterpart):
+    after each move the object's node set is exactly the sphere with its
+    periodic images at the new centre (numpy rasterisation), the mask
+    equals a full makemask of the new map, and the fluid count follows."""
+    import scenarios as S
+    from sunlightlb_gb300 import workloads as W
+    dims, rad = (20, 18, 22), 3.6
+    lb, obj = S.translate_case(orc, dims=dims, rad=rad, moves=5, measure=False)
+    c = (obj.posx, obj.posy, obj.posz)
+    want = np.zeros(dims, dtype=bool)
+    for im in W.images(dims, rad, c):
+        want |= W.sphere_nodes(dims, rad, im)
+    got = S.object_ids(lb).reshape(dims) >= 0
+    assert np.array_equal(got, want)
+    mask = lb.array("mask").copy()
+    orc.makemask(lb)
+    assert np.array_equal(lb.array("mask"), mask)
+    assert orc.countfluid(lb) == int((~want).sum())
