@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + IN
 # FP64 kernels: no FMA contraction, so FP64 results equal the reference's
 PER_FILE = {"slbc_f64.cu": ["-fmad=false"], "slbc_noalloc.cu": ["-fmad=false"]}
 # host C: strict IEEE double (no contraction, which gcc applies on aarch64)
-CC_FLAGS = ["-O2", "-fPIC", "-std=gnu99", "-Wall", "-Wno-unused-result",
+CC_FLAGS = ["-O2", "-fPIC", "-std=gnu99", "-Wall", "-Wno-unused-result", "-Werror=implicit-function-declaration",
             "-fno-fast-math", "-ffp-contract=off", "-I" + INC, "-I" + HOST_DIR]
 
 
@@ -98,7 +98,7 @@ def build(force=False, verbose=False):
         raise RuntimeError("build of libsunlightlb.so failed:\n" + msg)
     tmp = LIB + ".tmp"
     link = [nvcc] + ARCH + ["-shared", "-Xlinker", "-soname=libsunlightlb.so.1",
-                            "-Xlinker", "-Bsymbolic", "-o", tmp] + objs + ["-lm"]
+                            "-Xlinker", "-Bsymbolic", "-Xlinker", "--no-undefined", "-o", tmp] + objs + ["-lm"]
     if verbose:
         print(" ".join(link))
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)

@@ -474,7 +474,8 @@ void lbtranslate(LBSys lb, LBObj p, LBReal rad, LBReal x, LBReal y, LBReal z) {
     }
   }
   cap = box;
-  changed = (int *)xcalloc(2 * (size_t)cap, sizeof(int));
+  changed = (int *)calloc(2 * (size_t)cap, sizeof(int));
+  if (changed == NULL) error("No room for the changed-node list");
   uniform = slbc_bodyforce_uniform(dev, b);
   free(st->bnd_node); free(st->bnd_obj);
   st->bnd_node = NULL; st->bnd_obj = NULL;
