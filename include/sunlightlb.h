@@ -303,9 +303,15 @@ void lbsetstream(LBSys, void *);
 long lbkernelcount(void);
 /* Launch shape the autotuner chose for the fused step of lb, cfg[4] = {even
  * rows per thread, even threads along k, odd rows per thread, odd threads
- * along k} (BF16 lattices: planes per block in place of rows per thread);
- * returns 1 tuned, -1 defaults, 0 not decided yet. */
+ * along k} (BF16 lattices: planes per block in place of rows per thread;
+ * rows per thread -4: the 128-bit form, 4 nodes along k per thread, 128
+ * threads per block); returns 1 tuned, -1 defaults, 0 not decided yet. */
 int lbtuning(LBSys, int *);
+/* Set the launch shape of the fused step of lb (same cfg as lbtuning; rows
+ * per thread -4 selects the 128-bit form, 4 nodes along k per thread and
+ * 128 threads per block, FP32 populations with esk a multiple of 4);
+ * returns 0, or non-zero (with a message) for a shape it does not take. */
+int lbsettuning(LBSys, int *);
 /* Storage layout of the device populations of lb: 0 the reference's order
  * (after an upload), 1 after an even update (the next update is the
  * pull-and-push one), 2 after an odd update; -1 before the first device

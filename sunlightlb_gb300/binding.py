@@ -132,7 +132,7 @@ PROTOS = {
     # appended API
     "lbpull": ("v", "L"), "lbpush": ("v", "L"), "lbsteps": ("v", "Li"),
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
-    "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "lblayout": ("i", "L"), "freemp": ("v", "M"),
+    "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "lbsettuning": ("i", "Lp"), "lblayout": ("i", "L"), "freemp": ("v", "M"),
     "lbsetvel": ("v", "LDDDD"), "lbsetveldev": ("v", "Lp"), "lbvelocity": ("v", "Lp"),
     "lbstate": ("v", "Lpp"), "lbsetstatedev": ("v", "Lpp"), "lbtranslate": ("v", "LOdddd"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
     "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"), "batchmode": ("v", "pi"),

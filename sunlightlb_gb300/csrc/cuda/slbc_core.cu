@@ -453,6 +453,14 @@ std::mutex g_tuned_lock;
 
 int autotune_time(Lattice &L);
 
+}  // namespace
+
+namespace slbc {
+bool vec4_ok(const Lattice &L) { return L.precision == 1 && L.esk % 4 == 0 && L.npad % 4 == 0; }
+}  // namespace slbc
+
+namespace {
+
 int autotune(Lattice &L) {
   {
     std::lock_guard<std::mutex> guard(g_tuned_lock);
@@ -470,7 +478,8 @@ int autotune(Lattice &L) {
 
 int autotune_time(Lattice &L) {
   // FP64/FP32: {rows per thread, threads along k}; BF16: {planes per block, 32}
-  static const int cand_fp[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {1, 256}, {2, 256}, {4, 64}, {4, 128}};
+  static const int cand_fp[][2] = {{1, 64},  {1, 128}, {2, 64}, {2, 128}, {1, 256},
+                                   {2, 256}, {4, 64},  {4, 128}, {kStepVec4, kV4Threads}};
   const bool bf = L.precision == 2;
   // BF16: powers of two, and the plane counts that fill one or two waves of
   // three blocks per SM evenly
@@ -487,7 +496,7 @@ int autotune_time(Lattice &L) {
     }
   }
   const int (*cand)[2] = bf ? cand_bf : cand_fp;
-  const int ncand = bf ? nbf : 8;
+  const int ncand = bf ? nbf : (vec4_ok(L) ? 9 : 8);
   const char *env = getenv("SLB_AUTOTUNE");
   for (int p = 0; p < 2; p++) {
     L.tuned[p].npt = bf ? bf16_default_planes(L) : 1;
@@ -818,6 +827,10 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
     if (L.precision == 2) {
       if (npt < 1 || npt > 64 || bx != 32)
         return fail_msg("slbc_set_tuning: BF16 lattices take 1 to 64 planes per block and 32 threads along k");
+    } else if (npt == kStepVec4) {
+      if (!vec4_ok(L) || bx != kV4Threads)
+        return fail_msg("slbc_set_tuning: the 4-wide form needs FP32 populations, esk a multiple of 4 and "
+                        "128 threads per block");
     } else if ((npt != 1 && npt != 2 && npt != 4) || (bx != 32 && bx != 64 && bx != 128 && bx != 256)) {
       return fail_msg("slbc_set_tuning: rows per thread must be 1, 2 or 4 and threads along k 32, 64, 128 or 256");
     }

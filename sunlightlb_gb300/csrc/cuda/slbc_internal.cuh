@@ -46,9 +46,13 @@ constexpr uint16_t FLAG_SOLID = 0x8000u;
 constexpr uint16_t FLAG_LINKS = 0x7FFEu;
 
 // Launch shape of the fused step (chosen by the autotuner per parity).
+// npt = kStepVec4 selects the 128-bit form (FP32 populations, esk a
+// multiple of 4): 4 nodes along k per thread, block_k threads per block.
+constexpr int kStepVec4 = -4;
+constexpr int kV4Threads = 128;  // threads per block of the 4-wide form
 struct StepConfig {
-  int npt = 0;      // rows along j per thread (1 or 2); 0 = not tuned
-  int block_k = 0;  // threads along k
+  int npt = 0;      // rows along j per thread (1, 2 or 4), or kStepVec4; 0 = not tuned
+  int block_k = 0;  // threads along k (threads per block for kStepVec4)
 };
 
 // Device state of one lattice.
@@ -125,6 +129,10 @@ struct Lattice {
   StepConfig tuned[2];        // [0] even step, [1] odd step
   int tune_state = 0;         // 0 not tuned, 1 tuned, -1 tuning disabled
 };
+
+// whether the 128-bit form of the fused step applies to a lattice
+struct Lattice;
+bool vec4_ok(const Lattice &L);
 
 // Arguments shared by the population kernels.
 template <typename T>

@@ -7,8 +7,11 @@
 #include <cstring>
 #include <vector>
 
+#include <type_traits>
+
 #include "slbc_kernels.cuh"
 #include "slbc_mp.cuh"
+#include "slbc_step_v4.cuh"
 
 #define SLBC_CAT2(a, b) a##_##b
 #define SLBC_CAT(a, b) SLBC_CAT2(a, b)
@@ -52,6 +55,16 @@ static int flat_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 template <bool ODD, bool MOVING, bool BFU>
 static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
+  if (npt == kStepVec4) {  // 128-bit form: 4 nodes along k per thread, bx threads per block
+    if constexpr (std::is_same<T_, float>::value) {
+      const int lanes_k = std::min(32, L.esk / 4);
+      const dim3 block((unsigned)lanes_k, (unsigned)(kV4Threads / lanes_k));
+      const dim3 grid((unsigned)((L.esk / 4 + lanes_k - 1) / lanes_k), (unsigned)((L.esj + block.y - 1) / block.y),
+                      (unsigned)L.esi);
+      k_step_v4<ODD, MOVING, BFU><<<grid, block, 0, L.stream>>>(a);
+    }
+    return;
+  }
   const dim3 grid((unsigned)((L.esk + bx - 1) / bx), (unsigned)((L.esj + npt - 1) / npt), (unsigned)L.esi);
   if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4><<<grid, bx, 0, L.stream>>>(a);
   else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2><<<grid, bx, 0, L.stream>>>(a);
@@ -197,7 +210,9 @@ cudaError_t SLBC_FN(launch_step)(Lattice &L, int odd) {
   const StepConfig &c = L.tuned[odd ? 1 : 0];
   int bx = c.block_k, npt = c.npt;
   if (bx <= 0) { bx = 128; npt = 1; }
-  while (bx > 32 && bx / 2 >= L.esk) bx /= 2;
+  if (npt == kStepVec4 && !vec4_ok(L)) npt = 1;
+  if (npt != kStepVec4)
+    while (bx > 32 && bx / 2 >= L.esk) bx /= 2;
   if (L.esj < 2) npt = 1;
   StepArgs<T_> a = step_args(L);
   if (odd) step_dispatch<true>(L, a, npt, bx);

@@ -382,6 +382,12 @@ int lbtuning(LBSys lb, int *cfg) {
   return slbc_get_tuning(st->dev, cfg);
 }
 
+int lbsettuning(LBSys lb, int *cfg) {
+  int rc = slbc_set_tuning(slb_device(lb), cfg);
+  if (rc) printf("lbsettuning: %s\n", slbc_last_error());
+  return rc;
+}
+
 int lblayout(LBSys lb) {
   slb_priv *st = slb_state(lb);
   return st->dev == NULL ? -1 : slbc_layout(st->dev);
