@@ -86,6 +86,16 @@ int slbc_set_geometry_auto(slbc_lattice *h, const int *objidx, int nobj,
 /* Adsorption bits (0x4000 of the reference mask) of every node, 1 byte per
  * node (reference src/mpads.c:28-44). */
 int slbc_set_adsorption(slbc_lattice *h, const unsigned char *ads);
+/* Node tests of n insertsph calls at once, on the GPU (reference
+ * src/lbobjs.c:204-232 per sphere; no counterpart for many): spheres
+ * sph[4s..4s+3] = (r, x, y, z) in insertion order on an esi x esj x esk
+ * lattice whose nodes taken[x] != 0 already belong to an object.  Returns
+ * last[x] = the highest s whose sphere covers node x (-1 none) -- the
+ * sphere that holds the node after the n insertions --, count[s] = the
+ * nodes sphere s covers, overlap[s] = 1 when one of them was taken or is
+ * covered by an earlier sphere.  Host arrays; blocking. */
+int slbc_raster_spheres(int esi, int esj, int esk, int nsph, const double *sph, const unsigned char *taken,
+                        int *last, int *count, unsigned char *overlap);
 /* 1 when the body force is one constant over the fluid nodes (returned in
  * b), 0 when it is held per node. */
 int slbc_bodyforce_uniform(slbc_lattice *h, double b[3]);

@@ -370,6 +370,13 @@ LBObj insertmask(LBSys, unsigned char *);
 int rsapacking(int n, double phi, double rmin, double rmax, unsigned long long seed, int overlap,
                long max_tries, double *spheres, int max_spheres, unsigned char *solid);
 
+/* n calls of insertsph (rad[s], x[s], y[s], z[s]) in order, with the node
+ * tests on the GPU: the same objects (one per sphere that covers a node,
+ * pos = its centre), the same object map (a later sphere takes a node over)
+ * and the same messages.  Returns the number of objects created.  No
+ * counterpart in the reference (insertsph, src/lbobjs.c:204-232, one
+ * sphere at a time). */
+int insertspheres(LBSys, int, LBReal *, LBReal *, LBReal *, LBReal *);
 /* Move the spherical object obj of radius rad (a sphere with its periodic
  * images, as insertsph + flattenobj build it) so that its centre is
  * (x, y, z): the node set is re-rasterised on the GPU, nodes the sphere

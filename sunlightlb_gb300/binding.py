@@ -134,7 +134,7 @@ PROTOS = {
     "lbconverge": ("i", "Lidi"), "freelb": ("v", "L"), "lbgetstream": ("p", "L"),
     "lbsetstream": ("v", "Lp"), "lbkernelcount": ("l", ""), "lbtuning": ("i", "Lp"), "lbsettuning": ("i", "Lp"), "lblayout": ("i", "L"), "freemp": ("v", "M"),
     "lbsetvel": ("v", "LDDDD"), "lbsetveldev": ("v", "Lp"), "lbvelocity": ("v", "Lp"),
-    "lbstate": ("v", "Lpp"), "lbsetstatedev": ("v", "Lpp"), "lbtranslate": ("v", "LOdddd"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
+    "lbstate": ("v", "Lpp"), "lbsetstatedev": ("v", "Lpp"), "lbtranslate": ("v", "LOdddd"), "insertspheres": ("i", "LiDDDD"), "mptotal": ("d", "Ms"), "mpplane": ("d", "Msi"),
     "newbatch": ("p", ""), "batchadd": ("v", "pL"), "batchsteps": ("v", "pi"), "batchsize": ("i", "p"), "batchmode": ("v", "pi"),
     "freebatch": ("v", "p"), "mppull": ("v", "M"), "mppush": ("v", "M"),
 }

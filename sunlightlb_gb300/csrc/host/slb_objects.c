@@ -206,6 +206,53 @@ LBObj insertsph(LBSys lb, LBReal rad, LBReal ox, LBReal oy, LBReal oz) {
   return p;
 }
 
+/* appended: n insertsph calls (reference src/lbobjs.c:204-232) at once, the
+ * node tests done on the GPU: the same objects (one per sphere that covers
+ * a node, ids in order, pos = centre), the same map (a later sphere takes a
+ * node over from an earlier one) and the same messages.  Returns the number
+ * of objects created. */
+int insertspheres(LBSys lb, int n, LBReal *rad, LBReal *ox, LBReal *oy, LBReal *oz) {
+  long x, nn = lb->nnodes;
+  int s, made = 0;
+  double *sph;
+  int *last, *count;
+  unsigned char *taken, *overlap;
+  LBObj *objs;
+  if (n <= 0) return 0;
+  sph = (double *)malloc((size_t)n * 4 * sizeof(double));
+  count = (int *)calloc((size_t)n, sizeof(int));
+  overlap = (unsigned char *)calloc((size_t)n, 1);
+  objs = (LBObj *)calloc((size_t)n, sizeof(LBObj));
+  last = (int *)malloc((size_t)nn * sizeof(int));
+  taken = (unsigned char *)malloc((size_t)nn);
+  if (!sph || !count || !overlap || !objs || !last || !taken) error("No room for the sphere list");
+  for (s = 0; s < n; s++) {
+    sph[4 * s] = rad[s]; sph[4 * s + 1] = ox[s]; sph[4 * s + 2] = oy[s]; sph[4 * s + 3] = oz[s];
+  }
+  for (x = 0; x < nn; x++) taken[x] = lb->obj[x] != NULL;
+  slb_check(slbc_raster_spheres(lb->esi, lb->esj, lb->esk, n, sph, taken, last, count, overlap),
+            "sphere rasterisation");
+  for (s = 0; s < n; s++) {
+    LBObj p = addobj(lb);
+    zeroobj(p);
+    if (slb_verbosity & OBJECT_DETAILS) {
+      printf("Sphere radius %5.2f at %6.2f %6.2f %6.2f ", rad[s], ox[s], oy[s], oz[s]);
+      printf("id = %5i, # nodes = %i", p->id, count[s]);
+      printf(overlap[s] ? " (overlaps)\n" : "\n");
+    }
+    if (count[s] == 0) { drop_new(lb, p, 1); continue; }
+    p->posx = ox[s]; p->posy = oy[s]; p->posz = oz[s];
+    objs[s] = p;
+    made++;
+  }
+  for (x = 0; x < nn; x++)
+    if (last[x] >= 0) lb->obj[x] = objs[last[x]];
+  if (made) map_changed(lb);
+  free(sph); free(count); free(overlap); free(objs); free(last); free(taken);
+  slb_trace(lb, "insertspheres");
+  return made;
+}
+
 /* reference src/lbobjs.c:241-287 */
 LBObj insertcyl(LBSys lb, char *type, LBReal rad, LBReal a, LBReal b) {
   int i, j, k, ns = 0, overlap = 0, within;

@@ -223,9 +223,19 @@ def insert_spheres(L, lb, spheres, flatten=True):
     """insertsph for every sphere and each periodic image that meets the
     lattice (the scheme of examples/rcp_perm.pl:105-116), then flattenobj."""
     shape = (lb.esi, lb.esj, lb.esk)
-    for r, x, y, z in spheres:
-        for c in images(shape, r, (x, y, z)):
-            L.insertsph(lb, r, c[0], c[1], c[2])
+    if L.has("insertspheres"):  # the node tests of all of them on the GPU
+        rad, cen = [], []
+        for r, x, y, z in spheres:
+            for c in images(shape, r, (x, y, z)):
+                rad.append(r)
+                cen.append(c)
+        if rad:
+            cen = np.array(cen, dtype=np.float64)
+            L.insertspheres(lb, len(rad), np.array(rad, dtype=np.float64), cen[:, 0], cen[:, 1], cen[:, 2])
+    else:
+        for r, x, y, z in spheres:
+            for c in images(shape, r, (x, y, z)):
+                L.insertsph(lb, r, c[0], c[1], c[2])
     if flatten:
         L.flattenobj(lb)
 
