@@ -57,7 +57,9 @@ template <bool ODD, bool MOVING, bool BFU>
 static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
   if (npt == kStepVec4) {  // 128-bit form: 4 nodes along k per thread, bx threads per block
     if constexpr (std::is_same<T_, float>::value) {
-      const int lanes_k = std::min(32, L.esk / 4);
+      // lanes along k: a power of two, so a block is whole warps
+      int lanes_k = 32;
+      while (lanes_k > 1 && lanes_k > L.esk / 4) lanes_k /= 2;
       const dim3 block((unsigned)lanes_k, (unsigned)(kV4Threads / lanes_k));
       const dim3 grid((unsigned)((L.esk / 4 + lanes_k - 1) / lanes_k), (unsigned)((L.esj + block.y - 1) / block.y),
                       (unsigned)L.esi);

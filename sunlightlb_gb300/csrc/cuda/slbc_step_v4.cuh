@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kV4Threads, ODD ? (MOVING ? 2 : 3) : 4) k_step
   float *__restrict__ P = a.p.pop;
   const long long S = a.p.npad;
   const int esi = a.p.esi, esj = a.p.esj, esk = a.p.esk;
-  const int lane = threadIdx.x & 31;
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;  // a warp may span several rows
   const int kq = blockIdx.x * blockDim.x + threadIdx.x;  // k / 4
   const int k0 = 4 * kq;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
