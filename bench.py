@@ -937,7 +937,7 @@ def run_warmstart(args):
     masks = torch.as_tensor(np.stack(solids).astype(np.uint8), device="cuda")
     labels = torch.stack([WS.to_labels(f, (side, side, side)) for f in fields])
     del fields
-    net = WS.UNet(L, side, side, side, batch=args.batch, seed=1)
+    net = WS.UNet(L, side, side, side, batch=args.batch, seed=1, features=args.features)
     iters = max(1, args.epochs * args.train // args.batch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -950,7 +950,7 @@ def run_warmstart(args):
     t_train = time.perf_counter() - t0
     tc_status = net.status()
     # held-out packings at the evaluation size
-    inf = WS.UNet(L, ev_side, ev_side, ev_side, batch=1, params=net.params)
+    inf = WS.UNet(L, ev_side, ev_side, ev_side, batch=1, params=net.params, features=args.features)
     rows = []
     for phi, sd in ev_specs:
         solid = WS.packing(ev_side, phi, sd)
@@ -1012,7 +1012,9 @@ def run_warmstart(args):
                    "phi": [0.1, 0.5], "radii": [3.0, 8.0], "spheres_overlap": True, "force": force, "tau": 1.0,
                    "widths": list(net.widths), "batch": args.batch, "iterations": iters,
                    "lr": f"{args.lr:g} -> {args.lr * 0.01:g} (half cosine)",
-                   "input": "solid mask + periodic wall distance d/5 and (d/5)^2 (d capped at 5)",
+                   "input": {0: "solid mask", 1: "solid mask + periodic wall distance d/5 and (d/5)^2 (d capped at 5)",
+                             2: "solid mask + periodic wall distance d/12, (d/12)^2 (capped at 12) and min(d,5)/5"}[
+                                 args.features],
                    "output": "velocity and density deviation; set with u - F / (2 rho0) and rho0 + drho",
                    "labels": f"FP32 populations, converged to |d vmeanx|/vmeanx < {args.label_tol:g} per 200 steps",
                    "precision": "BF16 weights/activations, FP32 accumulation (tcgen05)"},
@@ -1123,6 +1125,8 @@ def main():
     ap.add_argument("--label-tol", type=float, default=1e-7)
     ap.add_argument("--label-maxsteps", type=int, default=20000)
     ap.add_argument("--save-weights", default="")
+    ap.add_argument("--features", type=int, default=1, choices=[0, 1, 2],
+                    help="warmstart workload: input encoding (wall distance searched to 5 or 12)")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")
     ap.add_argument("--tracer-steps", type=int, default=50000)
     ap.add_argument("--fp64-tracer-steps", type=int, default=10000)

@@ -322,9 +322,10 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
  * buffer, label [n][D][H][W][3], per-sample weights w or null for 1), grad
  * (BF16, gctot channels) = its derivative in channels 0..2, 0 in the
  * others.  encode: channel 0 = 1 on
- * solid nodes; with features, channels 1 and 2 = d / 5 and (d / 5)^2, d the
- * periodic distance of a fluid node to the nearest solid node (capped at
- * 5); the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
+ * solid nodes; with features = 1, channels 1 and 2 = d / 5 and (d / 5)^2, d
+ * the periodic distance of a fluid node to the nearest solid node (capped
+ * at 5); with features = 2, d / 12 and (d / 12)^2 (capped at 12) and
+ * min(d, 5) / 5 in channel 3; the rest 0.  decode: scale * pred[0..2] on fluid nodes (0 on
  * solid) into u[c * N + e], the layout of lbsetveldev. */
 int slbc_nn_pool(const void *in, int in_ctot, int in_coff, void *out, int out_ctot, int out_coff, int B, int D, int H,
                  int W, int C, void *stream);

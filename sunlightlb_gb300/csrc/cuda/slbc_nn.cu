@@ -303,24 +303,29 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, int nch
 }
 
 // input encoding: channel 0 = 1 on solid nodes, 0 on fluid; with
-// features, channel 1 = d / R and channel 2 = (d / R)^2 where d is the
+// features = 1, channel 1 = d / R and channel 2 = (d / R)^2 where d is the
 // periodic distance from a fluid node to the nearest solid node, searched
-// over a cube of half-width R (d = R when none is that close; 0 on solid
-// nodes); other channels zero (interior; the halo is filled afterwards)
-constexpr int kDistR = 5, kDistCap = kDistR * kDistR;
+// over a cube of half-width R = 5 (d = R when none is that close; 0 on
+// solid nodes); with features = 2 the search reaches R = 12 (the pores of
+// open packings are wider than 5) and channel 3 carries min(d, 5) / 5, the
+// near-wall form of the first encoding; other channels zero (interior; the
+// halo is filled afterwards)
+constexpr int kDistR1 = 5, kDistR2 = 12;
 
 // The squared distance min over the cube of dx^2 + dy^2 + dz^2 (solid
-// nodes, capped at R^2) separates into three one-axis passes (a minimum
-// of sums is the nested minimum), each over 2R + 1 neighbours instead of
-// (2R + 1)^3.  Values stay integers, so the result equals the cube search.
+// nodes, capped at R^2 <= 144, so it fits a byte) separates into three
+// one-axis passes (a minimum of sums is the nested minimum), each over
+// 2R + 1 neighbours instead of (2R + 1)^3.  Values stay integers, so the
+// result equals the cube search.
 // Pass 1 (along x, stride 1): nearest solid node on the row.
+template <int R>
 __global__ void k_dist_x(const unsigned char *solid, long long total, int W, unsigned char *a) {
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(e % W);
     const unsigned char *row = solid + (e - x);
-    int best = kDistCap;
+    int best = R * R;
 #pragma unroll
-    for (int dx = -kDistR; dx <= kDistR; dx++)
+    for (int dx = -R; dx <= R; dx++)
       if (dx * dx < best && row[((x + dx) % W + W) % W]) best = dx * dx;
     a[e] = (unsigned char)best;
   }
@@ -328,20 +333,22 @@ __global__ void k_dist_x(const unsigned char *solid, long long total, int W, uns
 
 // Passes 2 and 3 (along y, stride W, extent H; along z, stride W H,
 // extent D): b = min over |d| <= R of d^2 + a at the node d steps away.
+template <int R>
 __global__ void k_dist_min(const unsigned char *a, long long total, int n, long long stride, unsigned char *b) {
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     const int p = (int)((e / stride) % n);
     const unsigned char *col = a + (e - (long long)p * stride);
-    int best = kDistCap;
+    int best = R * R;
 #pragma unroll
-    for (int d = -kDistR; d <= kDistR; d++) best = min(best, d * d + (int)col[(long long)(((p + d) % n + n) % n) * stride]);
+    for (int d = -R; d <= R; d++) best = min(best, d * d + (int)col[(long long)(((p + d) % n + n) % n) * stride]);
     b[e] = (unsigned char)best;
   }
 }
 
-// dist2: the squared distances of the passes above (null without features)
-__global__ void k_encode(const unsigned char *solid, const unsigned char *dist2, int B, int D, int H, int W, bf16 *out,
-                         int ctot) {
+// dist2: the squared distances of the passes above (null without features),
+// searched to radius R
+__global__ void k_encode(const unsigned char *solid, const unsigned char *dist2, int R, int B, int D, int H, int W,
+                         bf16 *out, int ctot) {
   const long long total = (long long)B * D * H * W;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     long long r = e;
@@ -354,9 +361,11 @@ __global__ void k_encode(const unsigned char *solid, const unsigned char *dist2,
     const bool s = solid[e] != 0;
     p[0] = __float2bfloat16(s ? 1.0f : 0.0f);
     if (dist2 && !s) {
-      const float d = sqrtf((float)dist2[e]) * (1.0f / kDistR);
+      const float dist = sqrtf((float)dist2[e]);
+      const float d = dist * (1.0f / (float)R);
       p[1] = __float2bfloat16(d);
       p[2] = __float2bfloat16(d * d);
+      if (R != kDistR1) p[3] = __float2bfloat16(fminf(dist, (float)kDistR1) * (1.0f / kDistR1));
     }
   }
 }
@@ -511,12 +520,19 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
     const cudaError_t e = cudaMallocAsync((void **)&a, 2 * total, st);
     if (e != cudaSuccess) return bad((std::string("slbc_nn_encode scratch: ") + cudaGetErrorString(e)).c_str());
     unsigned char *b = a + total;
-    k_dist_x<<<grid_for(total), 256, 0, st>>>(solid, total, W, a);
-    k_dist_min<<<grid_for(total), 256, 0, st>>>(a, total, H, W, b);
-    k_dist_min<<<grid_for(total), 256, 0, st>>>(b, total, D, (long long)W * H, a);
+    if (features == 2) {
+      k_dist_x<kDistR2><<<grid_for(total), 256, 0, st>>>(solid, total, W, a);
+      k_dist_min<kDistR2><<<grid_for(total), 256, 0, st>>>(a, total, H, W, b);
+      k_dist_min<kDistR2><<<grid_for(total), 256, 0, st>>>(b, total, D, (long long)W * H, a);
+    } else {
+      k_dist_x<kDistR1><<<grid_for(total), 256, 0, st>>>(solid, total, W, a);
+      k_dist_min<kDistR1><<<grid_for(total), 256, 0, st>>>(a, total, H, W, b);
+      k_dist_min<kDistR1><<<grid_for(total), 256, 0, st>>>(b, total, D, (long long)W * H, a);
+    }
     slbc::count_launch(3);
   }
-  k_encode<<<grid_for(total), 256, 0, st>>>(solid, a, B, D, H, W, (bf16 *)out, ctot);
+  k_encode<<<grid_for(total), 256, 0, st>>>(solid, a, features == 2 ? kDistR2 : kDistR1, B, D, H, W, (bf16 *)out,
+                                            ctot);
   const int rc = launched("slbc_nn_encode");
   if (a) {
     const cudaError_t e = cudaFreeAsync(a, st);

@@ -95,7 +95,9 @@ class UNet:
     def __init__(self, lib, D, H, W_, batch, widths=(32, 64, 128, 256), seed=0, params=None, features=1):
         import torch
         self.torch = torch
-        self.features = features  # input: mask (0) or mask + wall-distance channels (1)
+        # input: mask (0), mask + wall distance searched to 5 (1), or to 12
+        # with the near-wall distance beside it (2)
+        self.features = features
         self.k = Kernels(lib.dll)
         self.D, self.H, self.W, self.B = D, H, W_, batch
         self.widths = w0, w1, w2, w3 = widths
@@ -153,7 +155,7 @@ class UNet:
         for name, lv, cin, cout, *_ in self.layers:
             std = math.sqrt(2.0 / (27 * cin))
             if name == "e0a":
-                std = math.sqrt(2.0 / (27 * (1 + 2 * self.features)))  # live input channels
+                std = math.sqrt(2.0 / (27 * (1 + {0: 0, 1: 2, 2: 3}[self.features])))  # live input channels
             w = torch.randn(27, cout, cin, generator=g) * std
             b = torch.zeros(cout)
             if name == "out":

@@ -86,6 +86,41 @@ def test_wall_distance_features(gpu):
     assert np.abs(got[..., 2] - np.where(s, 0.0, d * d)).max() <= 4e-3
 
 
+def test_wall_distance_features_wide(gpu):
+    """features = 2: the distance searched to 12 (capped there) / 12 and its
+    square in channels 1 and 2, min(d, 5) / 5 in channel 3 -- against the
+    cube search over periodic images with numpy."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    k = WS.Kernels(gpu.dll)
+    B, D, H, W = 2, 20, 24, 30
+    rng = np.random.default_rng(17)
+    solid = (rng.random((B, D, H, W)) > 0.995).astype(np.uint8)
+    out = torch.zeros((B, D + 2, H + 2, W + 2, 32), device="cuda", dtype=torch.bfloat16)
+    k.nn_encode(torch.as_tensor(solid, device="cuda").data_ptr(), B, D, H, W, out.data_ptr(), 32, 2,
+                torch.cuda.current_stream().cuda_stream)
+    got = out[:, 1:-1, 1:-1, 1:-1, :].float().cpu().numpy()
+    R = 12
+    for b in range(B):
+        s = solid[b].astype(bool)
+        best = np.full((D, H, W), float(R * R))
+        for dz in range(-R, R + 1):
+            for dy in range(-R, R + 1):
+                for dx in range(-R, R + 1):
+                    d2 = dx * dx + dy * dy + dz * dz
+                    if d2 >= R * R:
+                        continue
+                    hit = np.roll(s, shift=(-dz, -dy, -dx), axis=(0, 1, 2))
+                    best = np.where(hit & (d2 < best), d2, best)
+        dist = np.sqrt(best)
+        d = np.where(s, 0.0, dist / R)
+        assert np.array_equal(got[b, ..., 0], s.astype(np.float32))
+        assert np.abs(got[b, ..., 1] - d).max() <= 4e-3
+        assert np.abs(got[b, ..., 2] - np.where(s, 0.0, d * d)).max() <= 4e-3
+        assert np.abs(got[b, ..., 3] - np.where(s, 0.0, np.minimum(dist, 5.0) / 5.0)).max() <= 4e-3
+        assert not got[b, ..., 4:].any()
+
+
 @pytest.mark.parametrize("B,D,H,W,frac", [(2, 4, 8, 16, 0.98), (1, 12, 3, 40, 0.995), (3, 16, 16, 16, 0.9)])
 def test_wall_distance_small_and_wrapped(gpu, B, D, H, W, frac):
     """The separable distance passes on grids thinner than the search cube
