@@ -247,6 +247,12 @@ void mprescale(MPSys, LBReal);                 /* src/mpmisc.c:214-225  */
 void mpcopy(MPSys, MPSys);                     /* src/mpmisc.c:233-246  */
 LBReal mpspread(MPSys, char *);                /* src/mpmisc.c:466-499  */
 
+/* ---- Tracer velocity autocorrelation (reference src/mpvacf.c) ---- */
+void mpvacfinit(MPSys, MPSys, char *, int);    /* src/mpvacf.c:39-293   */
+void mpvacfinit2(MPSys, MPSys);                /* src/mpvacf.c:298-335  */
+void mpvacf(MPSys, MPSys);                     /* src/mpvacf.c:337-389  */
+LBReal mpvacfwr(MPSys, MPSys, char *, int);    /* src/mpvacf.c:391-428  */
+
 /* ---- Tracer injection (reference src/mpobjs.c) ---- */
 void mpall(MPSys, LBReal);                     /* src/mpobjs.c:28-43    */
 void mpslab(MPSys, LBReal, LBReal, LBReal, LBReal, LBReal, LBReal, LBReal); /* src/mpobjs.c:50-68 */

@@ -441,6 +441,166 @@ void adzero(MPSys mp) {
   for (n = 0; n < mp->lb->nnodes; n++) if (mp->lb->mask[n] & ADSORB) mp->p[n] = 0.0;
 }
 
+/* ---- tracer velocity autocorrelation: reference src/mpvacf.c:28-428 ----
+ * Two tracer fields: P carries the start-direction velocity of the tagged
+ * tracer, P2 counts the tracer.  The reference's arithmetic is kept as it
+ * is, including what it does in three places that look unintended and that
+ * a driver's numbers depend on: the rest-population term of P2 goes to the
+ * +x neighbour (src/mpvacf.c:120-121), the bounce-back term of link 10
+ * misses its velocity factor (:211-213), and the zero-time normalisation
+ * adds both sum psi P2 and sum psi^2 rho (:277-280).  State is
+ * process-wide, as in the reference. */
+static int vacf_l1, vacf_l2, vacf_n, vacf_max;
+static LBReal *vacf_arr;
+
+static int vacf_axis(char ch) {
+  switch (ch) {
+    case 'x': case 'i': return 0;
+    case 'y': case 'j': return 1;
+    case 'z': case 'k': return 2;
+  }
+  return -1;
+}
+
+void mpvacfinit(MPSys mp, MPSys mp2, char *vacfdir, int reqnvacf) {
+  LBSys lb = mp->lb;
+  int i, j, k, q, m;
+  LBReal *a = lb->a, *p = mp->p, *p2 = mp2->p, *rho = lb->rho, *psi = lb->psi;
+  LBReal rho0 = lb->rho0, alpha = mp->alpha, wfac = 1.0, vacftot = 0.0, ntracers = 0.0;
+  const LBReal onebyb = 1.0 / 72.0, eightbyb = 8.0 / 72.0, css = 1.0 / 3.0;
+  long n;
+  free(vacf_arr);
+  vacf_arr = (LBReal *)malloc((reqnvacf + 1) * sizeof(LBReal));
+  if (vacf_arr == NULL) return;
+  vacf_max = reqnvacf;
+  vacf_l1 = vacf_axis(vacfdir[0]);
+  if (vacf_l1 < 0) error("mpvacfinit: unrecognised initial direction");
+  vacf_l2 = vacf_axis(vacfdir[1]);
+  if (vacf_l2 < 0) error("mpvacfinit: unrecognised final direction");
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    long x = node(lb, i, j, k);
+    if (lb->obj[x] == NULL) {
+      LBReal piece = onebyb * (rho0 - alpha * rho[x]), piece8 = 8.0 * piece;
+      if (psi != NULL) wfac = psi[x];
+      for (q = 1; q < 15; q++)
+        p[nbr(lb, i, j, k, q)] += wfac * lb->c[3 * q + vacf_l1] * (a[q + 15 * x] + (q < 7 ? piece8 : piece));
+      p2[nbr(lb, i, j, k, 1)] += wfac * (a[15 * x] + 16.0 * piece + alpha * rho[x]);
+      for (q = 1; q < 15; q++) p2[nbr(lb, i, j, k, q)] += wfac * (a[q + 15 * x] + (q < 7 ? piece8 : piece));
+    } else if ((m = lb->mask[x]) && !(m & 0x4000)) {
+      for (q = 1; q < 15; q++) {
+        long y;
+        LBReal pc, term;
+        if (!(m & (1 << (q - 1)))) continue;
+        y = nbr(lb, i, j, k, q);
+        pc = (q < 7 ? eightbyb : onebyb) * (rho0 - alpha * rho[y]);
+        if (psi != NULL) wfac = psi[y];
+        term = a[OPP[q] + 15 * y] + pc;
+        p[y] += q == 10 ? wfac * term : wfac * lb->c[3 * OPP[q] + vacf_l1] * term;
+        p2[y] += wfac * term;
+      }
+    }
+  }
+  for (n = 0; n < lb->nnodes; n++)
+    if (lb->obj[n] != NULL) p[n] = p2[n] = 0.0;
+  wfac = 1.0;
+  for (n = 0; n < lb->nnodes; n++) {
+    const LBReal *t = a + 15 * n;
+    LBReal t1p2, t3p4, t5p6, lo_sum, hi_sum, lo_x, hi_x, lo_y, hi_y, lo_xy, hi_xy, t0p6, sd, s[6], piece;
+    if (lb->obj[n] != NULL) continue;
+    t1p2 = t[1] + t[2]; t3p4 = t[3] + t[4]; t5p6 = t[5] + t[6];
+    lo_sum = t[7] + t[8] + t[9] + t[10]; hi_sum = t[11] + t[12] + t[13] + t[14];
+    lo_x = t[7] - t[8] + t[9] - t[10]; hi_x = t[11] - t[12] + t[13] - t[14];
+    lo_y = t[7] + t[8] - t[9] - t[10]; hi_y = t[11] + t[12] - t[13] - t[14];
+    lo_xy = t[7] - t[8] - t[9] + t[10]; hi_xy = t[11] - t[12] - t[13] + t[14];
+    t0p6 = t[0] + t1p2 + t3p4 + t5p6;
+    sd = 2.0 * (t0p6 + (lo_sum + hi_sum)) / 3.0 - t0p6;
+    s[0] = sd + t1p2; s[1] = sd + t3p4; s[2] = sd + t5p6;
+    s[3] = lo_xy + hi_xy; s[4] = lo_x - hi_x; s[5] = lo_y - hi_y;
+    if (psi != NULL) wfac = psi[n];
+    ntracers += wfac * p2[n];
+    wfac = wfac * wfac;
+    ntracers += wfac * rho[n];
+    piece = rho[n] * css * (1.0 - alpha);
+    if (vacf_l1 == vacf_l2) vacftot += wfac * (piece + s[vacf_l1]);
+    else vacftot += wfac * s[vacf_l1 + vacf_l2 + 2];  /* xy 3, xz 4, yz 5 */
+  }
+  vacf_arr[0] = vacftot / ntracers;
+  vacf_n = 1;
+}
+
+void mpvacfinit2(MPSys mp, MPSys mp2) {
+  LBSys lb = mp->lb;
+  long n;
+  LBReal wfac = 1.0;
+  for (n = 0; n < lb->nnodes; n++) {
+    const LBReal *t = lb->a + 15 * n;
+    LBReal u, r;
+    if (lb->obj[n] != NULL) continue;
+    r = lb->rho[n];
+    u = vacf_l1 == 0 ? (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14]) / r
+      : vacf_l1 == 1 ? (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14]) / r
+                     : (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14]) / r;
+    if (lb->psi != NULL) wfac = lb->psi[n];
+    mp->p[n] = wfac * u;
+    mp2->p[n] = wfac;
+  }
+  vacf_n = 0;
+}
+
+void mpvacf(MPSys mp, MPSys mp2) {
+  LBSys lb = mp->lb;
+  long n;
+  LBReal wfac = 1.0, ptot = 0.0, psitot = 0.0, pmean, vacftot = 0.0, ntracers = 0.0;
+  if (vacf_n > vacf_max) { fprintf(stderr, "Ran out of storage after %i vacf values\n", vacf_max); return; }
+  for (n = 0; n < lb->nnodes; n++) {
+    if (lb->obj[n] != NULL) continue;
+    if (lb->psi != NULL) wfac = lb->psi[n];
+    ptot += wfac * mp->p[n]; psitot += wfac * wfac;
+  }
+  pmean = ptot / psitot;
+  for (n = 0; n < lb->nnodes; n++) {
+    if (lb->obj[n] != NULL) continue;
+    if (lb->psi != NULL) wfac = lb->psi[n];
+    mp->p[n] -= wfac * pmean;
+  }
+  wfac = 1.0;
+  for (n = 0; n < lb->nnodes; n++) {
+    const LBReal *t = lb->a + 15 * n;
+    LBReal u, r;
+    if (lb->obj[n] != NULL) continue;
+    r = lb->rho[n];
+    u = vacf_l2 == 0 ? (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14]) / r
+      : vacf_l2 == 1 ? (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14]) / r
+                     : (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14]) / r;
+    if (lb->psi != NULL) wfac = lb->psi[n];
+    vacftot += wfac * mp->p[n] * u;
+    ntracers += wfac * mp2->p[n];
+  }
+  vacf_arr[vacf_n++] = vacftot / ntracers;
+}
+
+/* reference src/mpvacf.c:391-428: returns the diffusion coefficient
+ * 0.5 vacf(0) + sum_{i>0} vacf(i); the file gets every (nvacf / nvals)-th
+ * value.  (The reference divides by zero when nvals > nvacf and closes a
+ * null file for "null"; both are guarded here.) */
+LBReal mpvacfwr(MPSys mp, MPSys mp2, char *vacffile, int nvals) {
+  int i, ntrck = nvals > 0 ? vacf_n / nvals : 0;
+  LBReal diffcon = 0.5 * vacf_arr[0];
+  FILE *fp = NULL;
+  (void)mp; (void)mp2;
+  if (!myscmp("null", vacffile) && (fp = fopen(vacffile, "w")) == NULL) {
+    fprintf(stderr, "%s could not be opened\n", vacffile);
+    return 0.0;
+  }
+  if (ntrck < 1) ntrck = 1;
+  for (i = 1; i < vacf_n; i++) {
+    diffcon += vacf_arr[i];
+    if (fp != NULL && i % ntrck == 0) fprintf(fp, "%6i %g %g\n", i, vacf_arr[i], diffcon);
+  }
+  if (fp != NULL) fclose(fp);
+  return diffcon;
+}
+
 void mppull(MPSys mp) { (void)mp; }
 void mppush(MPSys mp) { (void)mp; }
 

@@ -126,6 +126,7 @@ PROTOS = {
     "mpall": ("v", "Md"), "mpslab": ("v", "Mddddddd"), "mpwall": ("v", "Msid"),
     "mpsph": ("v", "Mddddd"), "mpcyl": ("v", "Msdddd"), "mplist": ("v", "Msd"),
     "mpsubs": ("v", "Msiiiiiid"),
+    "mpvacfinit": ("v", "MMsi"), "mpvacfinit2": ("v", "MM"), "mpvacf": ("v", "MM"), "mpvacfwr": ("d", "MMsi"),
     "adall": ("v", "M"), "adnone": ("v", "M"), "adslab": ("v", "Mdddddd"),
     "adsph": ("v", "Mdddd"), "adcyl": ("v", "Msddd"), "adtotal": ("d", "Msi"),
     "adzero": ("v", "M"),

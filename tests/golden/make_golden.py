@@ -3,7 +3,7 @@
 Run where the reference sources exist (they are compiled by oracle/Makefile
 into oracle/_ref/):
 
-    make -C oracle ref && python tests/golden/make_golden.py [--files-only]
+    make -C oracle ref && python tests/golden/make_golden.py [--files-only | --vacf-only]
 
 (the reference checkout is $SLB_REFERENCE, default /root/reference).
 
@@ -24,6 +24,8 @@ Fixtures (JSON):
   rcp144.json       the 144-sphere packing of examples/rcp_spheres.dat
   files.json        digests of the field, force, map, object and stress
                     files, of lattices reloaded from them, and of mpsubs
+  vacf.json         tracer velocity autocorrelation: diffusion coefficient
+                    and digests of both tracer fields
 """
 
 import hashlib
@@ -254,6 +256,18 @@ def file_records(L):
     return out
 
 
+def write_vacf_fixture(strict):
+    import tempfile
+    sys.path.insert(0, os.path.dirname(HERE))
+    from test_oracle import VACF_CASES
+    cases = []
+    for kw in VACF_CASES:
+        d, p, p2, _ = S.vacf_case(strict, tempfile.mkdtemp(), **kw)
+        cases.append({"config": kw, "diffusion": d, "p_sha256": digest(p), "p2_sha256": digest(p2)})
+    with open(os.path.join(HERE, "vacf.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
+
+
 def write_files_fixture(strict):
     with open(os.path.join(HERE, "files.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": file_records(strict)}, f, indent=1)
@@ -263,6 +277,9 @@ def main():
     ref_dir = os.path.join(ROOT, "oracle", "_ref")
     if "--files-only" in sys.argv:
         write_files_fixture(Library(os.path.join(ref_dir, "libref_strict.so"), extended=False))
+        return
+    if "--vacf-only" in sys.argv:
+        write_vacf_fixture(Library(os.path.join(ref_dir, "libref_strict.so"), extended=False))
         return
     REF_STRICT = os.path.join(ref_dir, "libref_strict.so")
     REF_SHIPPED = os.path.join(ref_dir, "libref_shipped.so")
@@ -291,6 +308,7 @@ def main():
     with open(os.path.join(HERE, "mp_cases.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": out["mp"]}, f, indent=1)
     write_files_fixture(strict)
+    write_vacf_fixture(strict)
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "kat": kat}, f, indent=1)
     print(json.dumps(kat, indent=1))

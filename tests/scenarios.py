@@ -207,3 +207,46 @@ def object_ids(lb):
     ids = {o.address: o.id for o in lb.objects()}
     raw = lb.array("obj")
     return np.array([ids.get(int(p), -2) if p else -1 for p in raw])
+
+
+def vacf_case(L, outdir, dims=(12, 13, 14), steps=25, direction="xx", second_init=False, psi=False, alpha=0.25,
+              ads=False):
+    """Tracer velocity autocorrelation (src/mpvacf.c) on a frozen flow past a
+    sphere with an adsorbing patch: mpvacfinit (or mpvacfinit2), then per
+    step an update of both tracer fields and mpvacf; returns (diffusion
+    coefficient, P, P2, file bytes)."""
+    import os
+    lb = L.newlb(dims[0], dims[1], dims[2], "null")
+    lb.tau = 0.7
+    L.insertsph(lb, 3.2, 5.5, 6.0, 7.2)
+    L.addbf(lb, 2e-3, 5e-4, -3e-4)
+    if psi:
+        w = np.linspace(0.6, 1.4, lb.nnodes)
+        lb._keep_psi = w
+        import ctypes as C
+        lb.psi = w.ctypes.data_as(C.POINTER(C.c_double))
+    for _ in range(30):
+        L.lbstep(lb)
+    mp, mp2 = L.newmp(lb, "null"), L.newmp(lb, "null")
+    for m in (mp, mp2):
+        m.alpha = alpha
+        L.mpinit(m)
+    if ads:  # adsorbing boundary nodes on half the sphere: their links are left out
+        L.adslab(mp, -1.0, 5.5, -1.0, 20.0, -1.0, 20.0)
+    if second_init:
+        L.mpvacfinit(mp, mp2, direction, steps + 2)
+        L.mpvacfinit2(mp, mp2)
+    else:
+        L.mpvacfinit(mp, mp2, direction, steps + 2)
+    for _ in range(steps):
+        L.mpstep(mp)
+        L.mpstep(mp2)
+        L.mpvacf(mp, mp2)
+    path = os.path.join(outdir, "vacf.dat")
+    d = L.mpvacfwr(mp, mp2, path, 5)
+    if L.has("mppull"):
+        L.mppull(mp)
+        L.mppull(mp2)
+    with open(path, "rb") as f:
+        data = f.read()
+    return d, mp.field().copy(), mp2.field().copy(), data

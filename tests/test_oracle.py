@@ -245,3 +245,33 @@ def test_translated_sphere_node_set(orc):
     orc.makemask(lb)
     assert np.array_equal(lb.array("mask"), mask)
     assert orc.countfluid(lb) == int((~want).sum())
+
+
+VACF_CASES = [dict(), dict(direction="xy"), dict(direction="zz", psi=True), dict(second_init=True, direction="yx"),
+              dict(ads=True, direction="yy", alpha=0.0)]
+
+
+def test_vacf_matches_reference(orc, ref_strict, tmp_path):
+    """The tracer velocity autocorrelation (src/mpvacf.c) restated: the
+    diffusion coefficient, both tracer fields and the written file equal
+    the strict reference build's bit for bit."""
+    import scenarios as S
+    for n, kw in enumerate(VACF_CASES):
+        (tmp_path / f"o{n}").mkdir()
+        (tmp_path / f"r{n}").mkdir()
+        a = S.vacf_case(orc, str(tmp_path / f"o{n}"), **kw)
+        b = S.vacf_case(ref_strict, str(tmp_path / f"r{n}"), **kw)
+        assert a[0] == b[0], kw
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]), kw
+        assert a[3] == b[3], kw
+
+
+def test_vacf_golden(orc, tmp_path):
+    import scenarios as S
+    g = load("vacf.json")["cases"]
+    for n, kw in enumerate(VACF_CASES):
+        (tmp_path / f"o{n}").mkdir()
+        d, p, p2, data = S.vacf_case(orc, str(tmp_path / f"o{n}"), **kw)
+        rec = g[n]
+        assert d == rec["diffusion"], kw
+        assert digest(p) == rec["p_sha256"] and digest(p2) == rec["p2_sha256"], kw
