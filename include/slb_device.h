@@ -207,6 +207,13 @@ int slbc_mp_step(slbc_tracer *t, int n, double alpha, double adprob, int moving,
  * nodes along axis (0,1,2; -1 none): reference src/mpmisc.c:121-158,466-499,
  * src/mpads.c:149-172. */
 int slbc_mp_sums(slbc_tracer *t, int axis, double out[5]);
+/* One step of the tracer velocity autocorrelation (reference
+ * src/mpvacf.c:337-389) on FP64 tracers t (P) and t2 (P2) of one lattice:
+ * P -= psi * pmean on fluid nodes (pmean = sum psi P / sum psi^2), then
+ * out[0] = sum psi P u_axis, out[1] = sum psi P2 over the fluid nodes, u
+ * from the populations and the density snapshot; psi_host per-node weights
+ * (host) or null. */
+int slbc_mp_vacf(slbc_tracer *t, slbc_tracer *t2, int axis, const double *psi_host, double out[2]);
 /* Extremes of p over fluid nodes (reference src/mpmisc.c:164-208). */
 int slbc_mp_minmax(slbc_tracer *t, double out[2]);
 /* Set p = value on the fluid nodes of a region (reference src/mpobjs.c):

@@ -1517,6 +1517,65 @@ static int mp_reduce(slbc_tracer *t, int axis, double out[5]) {
 
 int slbc_mp_sums(slbc_tracer *t, int axis, double out[5]) { return mp_reduce(t, axis, out); }
 
+namespace slbc {
+// pass 1 of the tracer velocity autocorrelation: sums of psi P and psi^2
+__global__ void __launch_bounds__(kReduceThreads) k_vacf_mean(const double *p, const uint16_t *flags,
+                                                            const double *psi, long long n, double *partials) {
+  double v[2] = {0.0, 0.0};
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    if (flags[x] & FLAG_SOLID) continue;
+    const double w = psi ? psi[x] : 1.0;
+    v[0] += w * p[x];
+    v[1] += w * w;
+  }
+  block_sum<2>(v);
+  if (threadIdx.x == 0) { partials[2 * blockIdx.x] = v[0]; partials[2 * blockIdx.x + 1] = v[1]; }
+}
+
+}  // namespace slbc
+
+int slbc_mp_vacf(slbc_tracer *t, slbc_tracer *t2, int axis, const double *psi_host, double out[2]) {
+  Lattice &L = t->h->L;
+  if (t2->h != t->h) return fail_msg("slbc_mp_vacf: the two tracers belong to different lattices");
+  if (!t->f64 || !t2->f64) return fail_msg("the tracer velocity autocorrelation needs FP64 tracers (mp->precision)");
+  if (L.precision == 2) return fail_msg("the tracer velocity autocorrelation needs FP32 or FP64 populations");
+  if (axis < 0 || axis > 2 || !L.mp_rho64) return fail_msg("slbc_mp_vacf: bad direction or no density snapshot");
+  const int nb = 152 * 4;
+  if (ensure_partials(L, 2 * nb + 8)) return 1;
+  double *psi = nullptr;
+  if (psi_host) {
+    CK(cudaMalloc(&psi, (size_t)L.nnodes * sizeof(double)));
+    CK(cudaMemcpyAsync(psi, psi_host, (size_t)L.nnodes * sizeof(double), cudaMemcpyHostToDevice, L.stream));
+  }
+  double sums[2];
+  cudaError_t e = cudaSuccess;
+  k_vacf_mean<<<nb, kReduceThreads, 0, L.stream>>>((const double *)t->p, L.flags, psi, L.nnodes, L.partials);
+  count_launch();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_final_sum_tree<2><<<1, 256, 0, L.stream>>>(L.partials, nb, L.partials + 2 * nb);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sums, L.partials + 2 * nb, 2 * sizeof(double), cudaMemcpyDeviceToHost, L.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  if (e == cudaSuccess) e = DISPATCH(L, launch_vacf_sums, L, (double *)t->p, (const double *)t2->p, psi, sums[0] / sums[1],
+                                     axis, L.partials, nb);
+  if (e == cudaSuccess) {
+    k_final_sum_tree<2><<<1, 256, 0, L.stream>>>(L.partials, nb, L.partials + 2 * nb);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, L.partials + 2 * nb, 2 * sizeof(double), cudaMemcpyDeviceToHost, L.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+  if (psi) cudaFree(psi);
+  if (e != cudaSuccess) return fail("slbc_mp_vacf", e);
+  L.state_version++;  // the tracer changed
+  return 0;
+}
+
+
+
 int slbc_mp_minmax(slbc_tracer *t, double out[2]) {
   Lattice &L = t->h->L;
   const int nb = 152 * 2;

@@ -212,6 +212,9 @@ struct BatchState {
   cudaError_t launch_mp_rhoinit_##SUFFIX(Lattice &L);                           \
   cudaError_t launch_move_sphere_##SUFFIX(Lattice &L, const MoveArgs &m,       \
                                           int with_uw);                         \
+  cudaError_t launch_vacf_sums_##SUFFIX(Lattice &L, double *p, const double *p2, \
+                                        const double *psi, double pmean,        \
+                                        int axis, double *partials, int nblocks); \
   cudaError_t launch_mp_step_##SUFFIX(Lattice &L, const void *p_in, void *p_out, \
                                       int tp_f64, double alpha, double adprob,  \
                                       int moving, const double *objstate,       \

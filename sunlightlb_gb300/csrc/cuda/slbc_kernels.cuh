@@ -719,6 +719,42 @@ __global__ void k_setvel(PopArgs<T> p, const double *stage, long long x0, long l
   for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = t[q];
 }
 
+// Tracer velocity autocorrelation (reference src/mpvacf.c:337-389), FP64
+// tracer fields P and P2, over the fluid nodes (psi weights or 1):
+//   pass 1: sums of psi P and psi^2;
+//   pass 2: P -= psi * pmean, then sums of psi P u_axis and psi P2, with
+//   u_axis = (sum_q c_q,axis a_q) / rho from the post-collision populations
+//   (any layout) and the density snapshot rho of mprhoinit.
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_vacf_sums(PopArgs<T> pa, int layout, const double *rho,
+                                                            double *p, const double *p2, const double *psi,
+                                                            double pmean, int axis, double *partials) {
+  const long long n = (long long)pa.esi * pa.esj * pa.esk;
+  double v[2] = {0.0, 0.0};
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)e;
+    const uint16_t fl = pa.flags[x];
+    if (fl & FLAG_SOLID) continue;
+    const double w = psi ? psi[x] : 1.0;
+    const double pv = p[x] - w * pmean;
+    p[x] = pv;
+    int i, j, k;
+    decode(x, pa.esj, pa.esk, i, j, k);
+    const Nbr nb = make_nbr(i, j, k, pa.esi, pa.esj, pa.esk);
+    double t[15];
+#pragma unroll
+    for (int q = 0; q < 15; q++) t[q] = (double)post_value<T>(pa.pop, pa.npad, layout, q, x, fl, nb);
+    double mom;
+    if (axis == 0) mom = t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14];
+    else if (axis == 1) mom = t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14];
+    else mom = t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14];
+    v[0] += w * pv * (mom / rho[x]);
+    v[1] += w * p2[x];
+  }
+  block_sum<2>(v);
+  if (threadIdx.x == 0) { partials[2 * blockIdx.x] = v[0]; partials[2 * blockIdx.x + 1] = v[1]; }
+}
+
 // Translation of one spherical object (appended operation, no counterpart
 // in the reference, which can only remove objects and insert new ones):
 // every node of the box `lo`, `len` (indices taken modulo the lattice, so

@@ -299,6 +299,14 @@ cudaError_t SLBC_FN(launch_setvel)(Lattice &L, const double *stage, long long x0
   return cudaGetLastError();
 }
 
+cudaError_t SLBC_FN(launch_vacf_sums)(Lattice &L, double *p, const double *p2, const double *psi, double pmean,
+                                      int axis, double *partials, int nblocks) {
+  k_vacf_sums<T_><<<nblocks, kReduceThreads, 0, L.stream>>>(pop_args(L), L.layout, L.mp_rho64, p, p2, psi, pmean,
+                                                             axis, partials);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t SLBC_FN(launch_move_sphere)(Lattice &L, const MoveArgs &m, int with_uw) {
   const long long nbox = (long long)m.len[0] * m.len[1] * m.len[2];
   const int blocks = (int)std::max<long long>(1, std::min<long long>((nbox + 255) / 256, 152LL * 8));

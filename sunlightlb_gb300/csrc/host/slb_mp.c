@@ -359,6 +359,201 @@ void mplist(MPSys mp, char *file, LBReal pval) {
   mptrace(mp, "mplist");
 }
 
+/* ---- tracer velocity autocorrelation: reference src/mpvacf.c ------------ */
+/* Two tracer fields: P (mp) carries the start-direction velocity of the
+ * tagged tracer, P2 (mp2) counts the tracer.  The initialisations run on
+ * the host on the mirrors (once per measurement, in the reference's order
+ * of summation, so P and P2 equal the reference's bit for bit); every
+ * mpvacf call runs on the GPU (FP64 tracers).  The reference's arithmetic
+ * is kept as it is in three places that look unintended but that a
+ * driver's numbers depend on: the rest-population term of P2 goes to the
+ * +x neighbour (src/mpvacf.c:120-121), the bounce-back term of link 10
+ * misses its velocity factor (:211-213), and the zero-time normalisation
+ * adds both sum psi P2 and sum psi^2 rho (:277-280).  State is
+ * process-wide, as in the reference. */
+static int vacf_l1, vacf_l2, vacf_n, vacf_max;
+static LBReal *vacf_arr;
+
+static int vacf_axis(char ch) {
+  switch (ch) {
+    case 'x': case 'i': return 0;
+    case 'y': case 'j': return 1;
+    case 'z': case 'k': return 2;
+  }
+  return -1;
+}
+
+static const int VX[15] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+static const int VY[15] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+static const int VZ[15] = {0, 0, 0, 0, 0, 1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
+static const int VOPP[15] = {0, 2, 1, 4, 3, 6, 5, 14, 13, 12, 11, 10, 9, 8, 7};
+
+static long vnbr(LBSys lb, int i, int j, int k, int q) {
+  int ii = i + VX[q], jj = j + VY[q], kk = k + VZ[q];
+  if (ii < 0) ii = lb->esi - 1; else if (ii >= lb->esi) ii = 0;
+  if (jj < 0) jj = lb->esj - 1; else if (jj >= lb->esj) jj = 0;
+  if (kk < 0) kk = lb->esk - 1; else if (kk >= lb->esk) kk = 0;
+  return slb_node(lb, ii, jj, kk);
+}
+
+static void vacf_mirrors(MPSys mp, MPSys mp2) {
+  if (mp->lb != mp2->lb) error("mpvacf: the two tracer fields belong to different lattices");
+  lbpull(mp->lb);
+  slb_pull_rho(mp->lb);
+  if (mp->lb->rho == NULL) error("mpvacf: no density snapshot (call mpinit first)");
+  mppull(mp);
+  mppull(mp2);
+}
+
+/* reference src/mpvacf.c:39-293 */
+void mpvacfinit(MPSys mp, MPSys mp2, char *vacfdir, int reqnvacf) {
+  LBSys lb = mp->lb;
+  int i, j, k, q, m;
+  LBReal *a, *p = mp->p, *p2 = mp2->p, *rho, *psi = lb->psi;
+  LBReal rho0 = lb->rho0, alpha = mp->alpha, wfac = 1.0, vacftot = 0.0, ntracers = 0.0;
+  const LBReal onebyb = 1.0 / 72.0, eightbyb = 8.0 / 72.0, css = 1.0 / 3.0;
+  long x;
+  free(vacf_arr);
+  vacf_arr = (LBReal *)malloc((reqnvacf + 1) * sizeof(LBReal));
+  if (vacf_arr == NULL) { fprintf(stderr, "Not enought room at the inn for %i reals\n", reqnvacf + 1); return; }
+  vacf_max = reqnvacf;
+  if (vacfdir[0] == '\0') error("mpvacfinit: please supply initial direction");
+  if ((vacf_l1 = vacf_axis(vacfdir[0])) < 0) error("mpvacfinit: unrecognised initial direction");
+  if (vacfdir[1] == '\0') error("mpvacfinit: please supply final direction");
+  if ((vacf_l2 = vacf_axis(vacfdir[1])) < 0) error("mpvacfinit: unrecognised final direction");
+  if (lb->status != POST_COLLIDE) {
+    fprintf(stderr, "vacf initialisation apparently out of position\n");
+    wrstatus(lb, stdout);
+  }
+  vacf_mirrors(mp, mp2);
+  a = lb->a; rho = lb->rho;
+  for (i = 0; i < lb->esi; i++) for (j = 0; j < lb->esj; j++) for (k = 0; k < lb->esk; k++) {
+    x = slb_node(lb, i, j, k);
+    if (lb->obj[x] == NULL) {
+      LBReal piece = onebyb * (rho0 - alpha * rho[x]), piece8 = 8.0 * piece;
+      if (psi != NULL) wfac = psi[x];
+      for (q = 1; q < 15; q++)
+        p[vnbr(lb, i, j, k, q)] += wfac * lb->c[3 * q + vacf_l1] * (a[q + 15 * x] + (q < 7 ? piece8 : piece));
+      p2[vnbr(lb, i, j, k, 1)] += wfac * (a[15 * x] + 16.0 * piece + alpha * rho[x]);
+      for (q = 1; q < 15; q++) p2[vnbr(lb, i, j, k, q)] += wfac * (a[q + 15 * x] + (q < 7 ? piece8 : piece));
+    } else if ((m = lb->mask[x]) && !(m & ADSORB)) {
+      for (q = 1; q < 15; q++) {
+        long y;
+        LBReal pc, term;
+        if (!(m & (1 << (q - 1)))) continue;
+        y = vnbr(lb, i, j, k, q);
+        pc = (q < 7 ? eightbyb : onebyb) * (rho0 - alpha * rho[y]);
+        if (psi != NULL) wfac = psi[y];
+        term = a[VOPP[q] + 15 * y] + pc;
+        p[y] += q == 10 ? wfac * term : wfac * lb->c[3 * VOPP[q] + vacf_l1] * term;
+        p2[y] += wfac * term;
+      }
+    }
+  }
+  for (x = 0; x < lb->nnodes; x++)
+    if (lb->obj[x] != NULL) p[x] = p2[x] = 0.0;
+  wfac = 1.0;
+  for (x = 0; x < lb->nnodes; x++) {
+    const LBReal *t = a + 15 * x;
+    LBReal t1p2, t3p4, t5p6, lo_sum, hi_sum, lo_x, hi_x, lo_y, hi_y, lo_xy, hi_xy, t0p6, sd, st[6], piece;
+    if (lb->obj[x] != NULL) continue;
+    t1p2 = t[1] + t[2]; t3p4 = t[3] + t[4]; t5p6 = t[5] + t[6];
+    lo_sum = t[7] + t[8] + t[9] + t[10]; hi_sum = t[11] + t[12] + t[13] + t[14];
+    lo_x = t[7] - t[8] + t[9] - t[10]; hi_x = t[11] - t[12] + t[13] - t[14];
+    lo_y = t[7] + t[8] - t[9] - t[10]; hi_y = t[11] + t[12] - t[13] - t[14];
+    lo_xy = t[7] - t[8] - t[9] + t[10]; hi_xy = t[11] - t[12] - t[13] + t[14];
+    t0p6 = t[0] + t1p2 + t3p4 + t5p6;
+    sd = 2.0 * (t0p6 + (lo_sum + hi_sum)) / 3.0 - t0p6;
+    st[0] = sd + t1p2; st[1] = sd + t3p4; st[2] = sd + t5p6;
+    st[3] = lo_xy + hi_xy; st[4] = lo_x - hi_x; st[5] = lo_y - hi_y;
+    if (psi != NULL) wfac = psi[x];
+    ntracers += wfac * p2[x];
+    wfac = wfac * wfac;
+    ntracers += wfac * rho[x];
+    piece = rho[x] * css * (1.0 - alpha);
+    if (vacf_l1 == vacf_l2) vacftot += wfac * (piece + st[vacf_l1]);
+    else vacftot += wfac * st[vacf_l1 + vacf_l2 + 2];  /* xy, xz, yz */
+  }
+  mppush(mp);
+  mppush(mp2);
+  vacf_arr[0] = vacftot / ntracers;
+  vacf_n = 1;
+  printf("MP '%s' %i : Initialised for vacf, init drn %c, final drn %c\n", mp->name, mp->step, vacfdir[0], vacfdir[1]);
+  printf("MP '%s' %i : Initialised storage for %i vacf values\n", mp->name, mp->step, vacf_max);
+  printf("MP '%s' %i : ntracers = %f\n", mp->name, mp->step, ntracers);
+  printf("MP '%s' %i : vacf(0) = %f\n", mp->name, mp->step, vacf_arr[0]);
+  mptrace(mp, "mpvacfinit");
+}
+
+/* reference src/mpvacf.c:298-335 */
+void mpvacfinit2(MPSys mp, MPSys mp2) {
+  LBSys lb = mp->lb;
+  long x;
+  LBReal wfac = 1.0;
+  vacf_mirrors(mp, mp2);
+  for (x = 0; x < lb->nnodes; x++) {
+    const LBReal *t = lb->a + 15 * x;
+    LBReal u, r;
+    if (lb->obj[x] != NULL) continue;
+    r = lb->rho[x];
+    u = vacf_l1 == 0 ? (t[1] - t[2] + t[7] - t[8] + t[9] - t[10] + t[11] - t[12] + t[13] - t[14]) / r
+      : vacf_l1 == 1 ? (t[3] - t[4] + t[7] + t[8] - t[9] - t[10] + t[11] + t[12] - t[13] - t[14]) / r
+                     : (t[5] - t[6] + t[7] + t[8] + t[9] + t[10] - t[11] - t[12] - t[13] - t[14]) / r;
+    if (lb->psi != NULL) wfac = lb->psi[x];
+    mp->p[x] = wfac * u;
+    mp2->p[x] = wfac;
+  }
+  mppush(mp);
+  mppush(mp2);
+  vacf_n = 0;
+  printf("MP '%s' %i : Re-initialised vacf calculation\n", mp->name, mp->step);
+  mptrace(mp, "mpvacfinit2");
+}
+
+/* reference src/mpvacf.c:337-389, on the GPU */
+void mpvacf(MPSys mp, MPSys mp2) {
+  double out[2];
+  slbc_tracer *t, *t2;
+  if (vacf_arr == NULL) { fprintf(stderr, "mpvacf: call mpvacfinit first\n"); return; }
+  if (vacf_n > vacf_max) { fprintf(stderr, "Ran out of storage after %i vacf values\n", vacf_max); return; }
+  if (mp->lb != mp2->lb) error("mpvacf: the two tracer fields belong to different lattices");
+  t = tracer(mp);
+  t2 = tracer(mp2);
+  slb_check(slbc_mp_vacf(t, t2, vacf_l2, mp->lb->psi, out), "tracer velocity autocorrelation");
+  p_changed(mp);
+  vacf_arr[vacf_n++] = out[0] / out[1];
+  mptrace(mp, "mpvacf");
+}
+
+/* reference src/mpvacf.c:391-428: the diffusion coefficient
+ * 0.5 vacf(0) + sum_{i>0} vacf(i); the file (not "null") gets every
+ * (nvacf / nvals)-th value.  The reference divides by zero when
+ * nvals > nvacf and closes a null file for "null": both guarded here. */
+LBReal mpvacfwr(MPSys mp, MPSys mp2, char *vacffile, int nvals) {
+  int i, ntrck;
+  LBReal diffcon;
+  FILE *fp = NULL;
+  (void)mp2;
+  if (vacf_arr == NULL) return 0.0;
+  if (!myscmp("null", vacffile)) {
+    if ((fp = fopen(vacffile, "w")) == NULL) { fprintf(stderr, "%s could not be opened\n", vacffile); return 0.0; }
+    printf("MP '%s' %i : Writing vacf data to %s\n", mp->name, mp->step, vacffile);
+  } else {
+    printf("MP '%s' %i : Analyzing vacf data\n", mp->name, mp->step);
+  }
+  ntrck = nvals > 0 ? vacf_n / nvals : 0;
+  if (ntrck < 1) ntrck = 1;
+  diffcon = 0.5 * vacf_arr[0];
+  for (i = 1; i < vacf_n; i++) {
+    diffcon += vacf_arr[i];
+    if (fp != NULL && i % ntrck == 0) fprintf(fp, "%6i %g %g\n", i, vacf_arr[i], diffcon);
+    if (i > vacf_n - 4) printf("MP '%s' %i : step, d = %8i %g %g\n", mp->name, mp->step, i, vacf_arr[i], diffcon);
+  }
+  if (fp != NULL) fclose(fp);
+  mptrace(mp, "mpvacfwr");
+  return diffcon;
+}
+
 /* ---- adsorption sites: reference src/mpads.c ------------------------------ */
 
 void adall(MPSys mp) {
