@@ -3,8 +3,9 @@
 // population array as one aligned float4.  Included by slbc_launch.cuh.
 //
 // The update rule is the one of step_node (slbc_kernels.cuh), node by node,
-// with the same arithmetic, so results equal the scalar kernel bit for bit;
-// only the memory accesses are regrouped:
+// with the same arithmetic (to FP32 rounding: the compiler may contract
+// multiply-adds differently in the two kernels); only the memory accesses
+// are regrouped:
 //
 //  * local step (C1 -> C0): 15 float4 loads of slots q at x0..x0+3, 15
 //    float4 stores to slots opp(q): no neighbour involved.

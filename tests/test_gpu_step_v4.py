@@ -2,8 +2,12 @@
 per thread, warp shuffles for the +-1 k shifts, scalar accesses at warp and
 row edges and across bounce-back links) against the scalar form.
 
-Both forms apply the same per-node arithmetic, so the populations must be
-equal bit for bit after any number of steps, on lattices chosen to hit the
+Both forms apply the same per-node arithmetic; the compiler may still
+contract multiply-adds differently in the two kernels (FP32 arithmetic is
+built with FMA), so the populations must agree to FP32 rounding -- 2e-6 of
+their largest magnitude, a few units in the last place, where a misplaced
+value would show as O(1) of it -- after any number of steps, on lattices
+chosen to hit the
 edge cases: rows of 8, 12, 20, 64 and 132 nodes along k (blocks of 2, 3, 5,
 16 and 32+1 lanes along k, so warps span several rows or end inside one),
 spheres across the periodic boundary, moving walls, Navier-Stokes,
@@ -21,6 +25,7 @@ from scenarios import two_spheres
 pytestmark = pytest.mark.gpu
 
 VEC4 = -4
+TOL = 2e-6
 
 
 def run(gpu, cfg, shape, steps):
@@ -51,10 +56,10 @@ def test_vec4_equals_scalar(gpu, name, steps):
     a = run(gpu, cfg, (VEC4, 128, VEC4, 128), steps)
     b = run(gpu, cfg, (1, 64, 1, 64), steps)
     pa, pb = a.pops(), b.pops()
-    assert np.array_equal(pa, pb), f"max |diff| = {np.abs(pa - pb).max():.3e}"
+    assert np.abs(pa - pb).max() <= TOL * np.abs(pb).max(), f"max |diff| = {np.abs(pa - pb).max():.3e}"
     gpu.measure(a)
     gpu.measure(b)
-    assert a.vmeanx == b.vmeanx
+    assert abs(a.vmeanx - b.vmeanx) <= TOL * abs(b.vmeanx)
 
 
 def test_vec4_nonuniform_body_force(gpu):
@@ -69,7 +74,7 @@ def test_vec4_nonuniform_body_force(gpu):
         for _ in range(9):
             gpu.lbstep(lb)
         out.append(lb.pops())
-    assert np.array_equal(out[0], out[1])
+    assert np.abs(out[0] - out[1]).max() <= TOL * np.abs(out[1]).max()
 
 
 def test_vec4_rejected_where_it_does_not_apply(gpu):

@@ -21,14 +21,17 @@ def oracle():
     return orc_unet
 
 
-@pytest.mark.parametrize("nch", [3, 4])
-def test_unet_gradients_match_cpu_oracle(gpu, nch):
-    """nch label channels: the velocity, and with 4 the density deviation."""
+@pytest.mark.parametrize("nch,widths,B", [(3, (32, 32, 32, 32), 2), (4, (32, 32, 32, 32), 2),
+                                          (4, (32, 64, 128, 256), 1)])
+def test_unet_gradients_match_cpu_oracle(gpu, nch, widths, B):
+    """nch label channels: the velocity, and with 4 the density deviation;
+    the network's own widths 32 -> 64 -> 128 -> 256 as well as a narrow
+    form."""
     torch = pytest.importorskip("torch")
     from sunlightlb_gb300 import warmstart as WS
     orc = oracle()
-    B, D, H, W = 2, 32, 32, 64
-    net = WS.UNet(gpu, D, H, W, batch=B, widths=(32, 32, 32, 32), seed=3, features=0)
+    D, H, W = 32, 32, 64
+    net = WS.UNet(gpu, D, H, W, batch=B, widths=widths, seed=3, features=0)
     rng = np.random.default_rng(5)
     solid = (rng.random((B, D, H, W)) > 0.7).astype(np.uint8)
     zz, yy, xx = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
