@@ -161,11 +161,11 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(prec_name, n=HEAD_N):
+def profile_traffic(prec_name, n=None):
     """DRAM bytes per launch of the fused step (mean of the odd and even
     step) at an n^3 lattice from the committed ncu summary
     profiles/lb_step_<n>.md, line 'traffic_per_launch_<precision>: <bytes>'."""
-    p = os.path.join(ROOT, "profiles", f"lb_step_{n}.md")
+    p = os.path.join(ROOT, "profiles", f"lb_step_{n or HEAD_N}.md")
     try:
         with open(p) as f:
             for line in f:
@@ -1088,6 +1088,7 @@ def warm_leg(torch, L, args):
 
 
 def main():
+    global HEAD_N
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -1096,6 +1097,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16dev"])
     ap.add_argument("--e2e-intervals", type=int, default=20)
     ap.add_argument("--e2e-fp64-intervals", type=int, default=2)
+    ap.add_argument("--head-side", type=int, default=HEAD_N,
+                    help="side of the headline packed bed (smaller sides for profiling runs only)")
     ap.add_argument("--no-legs", action="store_true", help="default workload: skip the batch, tracer and "
                                                          "warm-start legs")
     ap.add_argument("--leg-domains", type=int, default=64)
@@ -1134,6 +1137,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    HEAD_N = args.head_side
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "tracer":
