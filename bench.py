@@ -754,6 +754,7 @@ def build_domain(L, side, rad, centre, vel, precision=1):
     for c in W.images((side, side, side), rad, centre):
         L.insertsph(lb, rad, c[0], c[1], c[2])
     obj = L.flattenobj(lb)
+    obj.posx, obj.posy, obj.posz = centre  # flattenobj leaves the centroid of the (wrapped) nodes
     obj.velx, obj.vely, obj.velz = vel
     L.syncobjs(lb)
     L.vspread(lb)
@@ -774,12 +775,41 @@ def _oracle_domain(spec, steps, out, slot):
     out[slot] = drag(lb)
 
 
-def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=True):
+def translate_all(L, lbs, specs, every):
+    """Move every domain's sphere on by its velocity times `every` steps
+    (lbtranslate: the node set re-rasterised on the GPU)."""
+    for lb, (side, rad, centre, vel) in zip(lbs, specs):
+        obj = lb.objects()[0]
+        c = [(getattr(obj, a) + v * every) % side for a, v in zip(("posx", "posy", "posz"), vel)]
+        L.lbtranslate(lb, obj, rad, *c)
+
+
+def advance(L, lbs, specs, steps, every, batch=None):
+    """steps update steps of the domains (one batch, or one domain at a
+    time), the spheres translated every `every` steps (0: fixed nodes)."""
+    import torch
+    done = 0
+    while done < steps:
+        n = steps - done if every <= 0 else min(every, steps - done)
+        if batch is not None:
+            L.batchsteps(batch, n)
+        else:
+            for lb in lbs:
+                L.lbsteps(lb, n)
+                torch.cuda.synchronize()  # one domain at a time
+        done += n
+        if every > 0 and n == every:
+            translate_all(L, lbs, specs, every)
+
+
+def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=True, translate_every=0):
     """Many independent moving-sphere domains advanced together (batchsteps,
     packed tiles, one launch per step from a CUDA graph) against the same
     domains one at a time (lbsteps per domain), per-domain drag compared;
     optionally the other batch mode and a seeded subset against the CPU
-    oracle (FP64)."""
+    oracle (FP64).  With translate_every > 0 the spheres really move: every
+    that many steps each is re-rasterised at its new centre (lbtranslate),
+    in both arms (the CPU subset keeps fixed nodes)."""
     local = dist_env()[2]
     specs = batch_domains(ndom)
     nodes = sum(s[0] ** 3 for s in specs)
@@ -802,16 +832,15 @@ def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=Tr
     if clk:
         clk.__enter__()
     t0 = time.perf_counter()
-    L.batchsteps(b, steps)
+    advance(L, batch, specs, steps, translate_every, batch=b)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     if clk:
         clk.__exit__(None, None, None)
     launches = L.lbkernelcount() - k0
     t0 = time.perf_counter()
-    for lb in alone:
-        L.lbsteps(lb, steps)
-        torch.cuda.synchronize()  # one domain at a time
+    advance(L, alone, specs, steps, translate_every)
+    torch.cuda.synchronize()
     t_alone = time.perf_counter() - t0
     worst = 0.0
     drags = []
@@ -827,7 +856,9 @@ def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=Tr
         "config": {"domains": ndom, "sides": list(BATCH_SIDES), "cells": nodes, "steps": steps,
                    "radii": [BATCH_RMIN, BATCH_RMAX], "speed": BATCH_SPEED, "seed": BATCH_SEED, "tau": 1.0,
                    "flow": "Stokes", "populations": "fp32",
-                   "boundary": "moving-wall link bounce-back on the fixed node map (vspread)"},
+                   "boundary": "moving-wall link bounce-back (vspread)" +
+                               (f", spheres re-rasterised at their new centres every {translate_every} steps "
+                                "(lbtranslate)" if translate_every > 0 else " on the fixed node map")},
         "build_s": round(t_build, 1),
         "batched": {"mode": "packed tiles, one launch per step, CUDA graph", "wall_s": round(t_batch, 3),
                     "MLUPS": round(nodes * steps / t_batch / 1e6, 1), "hbm_gbs": round(gbs, 1),
@@ -851,7 +882,7 @@ def batch_result(torch, L, ndom, steps, cpu_subset=0, persistent=True, clocks=Tr
         t_pers = time.perf_counter() - t0
         out["batched_persistent_mode"] = {"steps": psteps, "wall_s": round(t_pers, 3),
                                           "MLUPS": round(nodes * psteps / t_pers / 1e6, 1)}
-    if cpu_subset > 0:
+    if cpu_subset > 0 and translate_every <= 0:
         # the smallest domains, FP64 on the CPU oracle, one thread each
         sub = sorted(range(len(specs)), key=lambda d: (specs[d][0], d))[:cpu_subset]
         res = [None] * len(sub)
@@ -886,7 +917,8 @@ def run_batch(args):
         return
     torch.cuda.set_device(local)
     L = sunlightlb_gb300.library()
-    out = batch_result(torch, L, args.domains, args.batch_steps, cpu_subset=args.cpu_subset)
+    out = batch_result(torch, L, args.domains, args.batch_steps, cpu_subset=args.cpu_subset,
+                       translate_every=args.translate_every)
     line = {"workload": f"batched ensemble: {args.domains} periodic moving-sphere domains, sides {list(BATCH_SIDES)}",
             "metric": "MLUPS of all domains together, batched vs one domain at a time"}
     line.update(out)
@@ -1118,6 +1150,9 @@ def main():
     ap.add_argument("--domains", type=int, default=512, help="batch workload: number of domains")
     ap.add_argument("--batch-steps", type=int, default=20000)
     ap.add_argument("--cpu-subset", type=int, default=8, help="batch workload: domains checked on the CPU oracle")
+    ap.add_argument("--translate-every", type=int, default=0,
+                    help="batch workload: move the spheres (re-rasterise them) every this many steps; 0 keeps "
+                         "the node map fixed")
     ap.add_argument("--train", type=int, default=2000, help="warmstart workload: training packings")
     ap.add_argument("--eval", type=int, default=100, help="warmstart workload: held-out packings")
     ap.add_argument("--epochs", type=int, default=10)

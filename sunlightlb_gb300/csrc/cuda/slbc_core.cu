@@ -786,7 +786,7 @@ void slbc_destroy(slbc_lattice *h) {
   void *bufs[] = {L.pop, L.scratch, L.flags, L.bnd_node, L.bnd_obj, L.bnd_f, L.piece_obj,
                   L.piece_lo, L.piece_hi, L.piece_sum, L.obj_pos, L.obj_ft, L.ads, L.objidx,
                   L.bf, L.uw, L.partials, L.staging, L.mp_rho64, L.mp_rho32, L.mom[0], L.mom[1],
-                  L.ads_links, L.mp_rinv32, L.mp_coef};
+                  L.ads_links, L.mp_rinv32, L.mp_coef, L.move_buf};
   for (void *b : bufs) if (b) cudaFree(b);
   if (L.host_out) cudaFreeHost(L.host_out);
   if (L.graph) cudaGraphExecDestroy(L.graph);
@@ -1019,8 +1019,12 @@ int slbc_move_sphere(slbc_lattice *h, int obj, double rad, const double oldc[3],
   m.layout = L.layout;
   m.objidx = L.objidx;
   m.cap = (int)std::min<long>(cap, 1L << 30);
-  int *dev_list = nullptr;
-  CK(cudaMalloc(&dev_list, (size_t)(2 * (long)m.cap + 1) * sizeof(int)));
+  if (L.move_cap < m.cap) {  // kept with the lattice: moves are repeated
+    if (L.move_buf) { CK(cudaStreamSynchronize(L.stream)); cudaFree(L.move_buf); L.move_buf = nullptr; }
+    CK(cudaMalloc(&L.move_buf, (size_t)(2 * (long)m.cap + 1) * sizeof(int)));
+    L.move_cap = m.cap;
+  }
+  int *dev_list = L.move_buf;
   m.nchanged = dev_list;
   m.changed = dev_list + 1;
   cudaError_t e = cudaMemsetAsync(dev_list, 0, sizeof(int), L.stream);
@@ -1029,8 +1033,9 @@ int slbc_move_sphere(slbc_lattice *h, int obj, double rad, const double oldc[3],
   if (e == cudaSuccess) e = cudaMemcpyAsync(&count, dev_list, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
   if (e == cudaSuccess && count > 0)
-    e = cudaMemcpy(changed, dev_list + 1, (size_t)2 * std::min(count, m.cap) * sizeof(int), cudaMemcpyDeviceToHost);
-  cudaFree(dev_list);
+    e = cudaMemcpyAsync(changed, dev_list + 1, (size_t)2 * std::min(count, m.cap) * sizeof(int),
+                        cudaMemcpyDeviceToHost, L.stream);
+  if (e == cudaSuccess && count > 0) e = cudaStreamSynchronize(L.stream);
   if (e != cudaSuccess) return fail("slbc_move_sphere", e);
   *nchanged = count;
   if (count > m.cap) return fail_msg("slbc_move_sphere: more changed nodes than the list holds");

@@ -82,6 +82,8 @@ struct Lattice {
   uint16_t *ads_links = nullptr;
   long ads_version = 0, ads_links_version = -1;
   int *objidx = nullptr;        // object index per node (-1 fluid)
+  int *move_buf = nullptr;      // changed-node list of slbc_move_sphere (count, then pairs)
+  long move_cap = 0;
   // parameters
   slbc_params par{};
   int bf_uniform = 1;
