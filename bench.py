@@ -419,11 +419,15 @@ def run_e2e(L, precision, solid, intervals):
     L.lbpush(lb)
     h2d = 15 * 8 * n + 4 * n + 3 * 8 * n  # populations (FP64), object map, body force arrays
     d2h = 0
-    for _ in range(intervals):
+    t_first = None
+    for it in range(intervals):
         L.lbsteps(lb, CHECK - 2)
         L.measure(lb)
         _ = (lb.vmeanx, lb.step)
+        if it == 0:
+            t_first = time.perf_counter() - t0  # upload + the first interval
         d2h += 5 * 8 * 3 + 6 * 8  # three mean-flow sums and the object force/torque
+    t_steps = time.perf_counter() - t0
     L.lbpull(lb)  # populations into the host buffer lb->a (FP64, reference order)
     pops = lb.array("a")
     d2h += pops.nbytes
@@ -433,6 +437,9 @@ def run_e2e(L, precision, solid, intervals):
     return {"value": round(n * steps / dt / 1e6, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps),
             "steps": steps, "populations": PREC_NAMES[precision], "wall_s": round(dt, 3),
+            "wall_breakdown_s": {"upload_and_first_interval": round(t_first, 3),
+                                 "other_intervals": round(t_steps - t_first, 3),
+                                 "download": round(dt - t_steps, 3)},
             "note": "public C API: lbpush, lbsteps + measure per 100 steps, lbpull"}
 
 
