@@ -605,13 +605,16 @@ constexpr int kWgTileA = 128 * 128;  // 128 rows x 64 K x 2 B
 constexpr int kWgTileB = 256 * 128;  // up to 256 rows
 constexpr int kWgSmem = kStages * (kWgTileA + kWgTileB) + 1024;
 
-__global__ void __launch_bounds__(128, 1)
+// B stages hold ntile rows of 128 bytes (the dynamic shared memory is sized
+// by ntile), so layers with up to 64 input channels fit two blocks per SM.
+__global__ void __launch_bounds__(128, 2)
 k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap a1,
         const __grid_constant__ CUtensorMap a2, const __grid_constant__ CUtensorMap tb, WgradArgs w, int *err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
   uint8_t *tA = smem_raw + pad;
   uint8_t *tB = tA + kStages * kWgTileA;
+  const int tile_b = w.ntile * 128;  // bytes of one B stage (a multiple of 2048)
   __shared__ uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -656,7 +659,7 @@ k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensor
         const CUtensorMap *am = dx == 0 ? &a0 : (dx == 1 ? &a1 : &a2);
         tc::tma_load_2d(tA + s * kWgTileA + tl * w.co_rows * 128, am, &full[s], x, co0);
       }
-      tc::tma_load_2d(tB + s * kWgTileB, &tb, &full[s], k0, ci0);
+      tc::tma_load_2d(tB + s * tile_b, &tb, &full[s], k0, ci0);
       issued = kt + 1;
     }
   } else if (threadIdx.x == 32) {
@@ -669,7 +672,7 @@ k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensor
       }
       tc::fence_after_sync();
       const uint64_t ad = tc::smem_desc(tA + s * kWgTileA, tc::kSwizzle128, 128);
-      const uint64_t bd = tc::smem_desc(tB + s * kWgTileB, tc::kSwizzle128, 128);
+      const uint64_t bd = tc::smem_desc(tB + s * tile_b, tc::kSwizzle128, 128);
 #pragma unroll
       for (int kk = 0; kk < 4; kk++) tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, idesc, (kt | kk) != 0);
       tc::mma_commit(&empty[s]);
@@ -966,7 +969,8 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
   const dim3 grid((unsigned)(((27 + w.taps_per_tile - 1) / w.taps_per_tile) * w.co_tiles), (unsigned)(cin / w.ntile),
                   (unsigned)splits);
-  k_wgrad<<<grid, 128, kWgSmem, (cudaStream_t)stream>>>(m0, m1, m2, mb, w, err);
+  const int smem = kStages * (kWgTileA + w.ntile * 128) + 1024;
+  k_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, w, err);
   slbc::count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
