@@ -1016,6 +1016,7 @@ def run_warmstart(args):
                                     "warm_wall_s": round(hitw[1] + t_inf, 4) if hitw else None}
             if check == 100:
                 row["warm_k_error_first_check"] = abs(trajw[0][1] - k_conv) / abs(k_conv)
+                row["warm_k_signed_error_checks"] = [(st, (kk - k_conv) / k_conv) for st, kk, _ in trajw[:6]]
                 row["plain_k_error_first_check"] = abs(traj[0][1] - k_conv) / abs(k_conv)
         # the same network set without its density (rho = rho0, u - F / rho0,
         # the best shift without a density) and with its density but the
