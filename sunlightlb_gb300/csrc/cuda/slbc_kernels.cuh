@@ -219,11 +219,10 @@ __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, 
     t[0] = P[x];
 #pragma unroll
     for (int q = 1; q < 15; q++) {
-      // select between two addresses whose slot offsets are fixed by q
-      // (no per-load wide multiply of a selected slot by the stride)
-      const T *own = P + q * S + x;
-      const T *up = P + OPP(q) * S + nb.at(-CX(q), -CY(q), -CZ(q));
-      t[q] = *(((fl >> q) & 1) ? own : up);
+      const bool bnd = (fl >> q) & 1;
+      const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+      const int slot = bnd ? q : OPP(q);
+      t[q] = P[slot * S + src];
     }
   }
 }
@@ -250,9 +249,10 @@ __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb,
     P[x] = t[0];
 #pragma unroll
     for (int q = 1; q < 15; q++) {
-      T *own = P + OPP(q) * S + x;
-      T *down = P + q * S + nb.at(CX(q), CY(q), CZ(q));
-      *(((fl >> OPP(q)) & 1) ? own : down) = t[q];
+      const bool bnd = (fl >> OPP(q)) & 1;
+      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+      const int slot = bnd ? OPP(q) : q;
+      P[slot * S + dst] = t[q];
     }
   }
 }
