@@ -962,29 +962,47 @@ def run_warmstart(args):
     torch.cuda.set_device(local)
     L = sunlightlb_gb300.library()
     side, ev_side, force = args.warm_side, args.eval_side, WARM_FORCE
-    specs = WS.packing_specs(args.train + args.eval, WARM_SEED)
-    tr_specs, ev_specs = specs[:args.train], specs[args.train:]
+    # held-out packings: the ones after the training set, or from --eval-offset
+    # (to evaluate networks trained on different sets on the same packings)
+    ev_off = args.train if args.eval_offset is None else args.eval_offset
+    if ev_off < args.train:
+        raise SystemExit("--eval-offset must not reach into the training packings")
+    specs = WS.packing_specs(ev_off + args.eval, WARM_SEED)
+    tr_specs, ev_specs = specs[:args.train], specs[ev_off:ev_off + args.eval]
+    train_now = args.epochs > 0 or not args.init_weights
     t0 = time.perf_counter()
-    solids = [WS.packing(side, phi, sd) for phi, sd in tr_specs]
+    solids = [WS.packing(side, phi, sd) for phi, sd in tr_specs] if train_now else []
     t_pack = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    fields, lsteps = WS.converged_flows(L, solids, force=force, tol=args.label_tol, maxsteps=args.label_maxsteps,
-                                        density=True)
+    lsteps = [0]
+    if train_now:
+        fields, lsteps = WS.converged_flows(L, solids, force=force, tol=args.label_tol, maxsteps=args.label_maxsteps,
+                                            density=True)
     torch.cuda.synchronize()
     t_labels = time.perf_counter() - t0
-    masks = torch.as_tensor(np.stack(solids).astype(np.uint8), device="cuda")
-    labels = torch.stack([WS.to_labels(f, (side, side, side)) for f in fields])
-    del fields
-    net = WS.UNet(L, side, side, side, batch=args.batch, seed=1, features=args.features)
-    iters = max(1, args.epochs * args.train // args.batch)
+    if train_now:
+        masks = torch.as_tensor(np.stack(solids).astype(np.uint8), device="cuda")
+        labels = torch.stack([WS.to_labels(f, (side, side, side)) for f in fields])
+        del fields
+    init_meta = None
+    if args.init_weights:  # fine-tune a saved network (same widths and input encoding)
+        params, widths, features, init_meta = WS.load_weights(args.init_weights)
+        net = WS.UNet(L, side, side, side, batch=args.batch, widths=widths, features=features,
+                      params=WS.with_adam_state(params))
+        args.features = features
+    else:
+        net = WS.UNet(L, side, side, side, batch=args.batch, seed=1, features=args.features)
+    iters = max(1, args.epochs * args.train // args.batch) if train_now else 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    # each sample's loss relative to its own label energy (labels span more
-    # than an order of magnitude with the solid fraction)
-    sample_w = 1.0 / labels.pow(2).mean(dim=(1, 2, 3, 4)).clamp_min(1e-12)
-    hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20), sample_w=sample_w,
-                    lr_min=args.lr * 0.01)
+    hist = []
+    if train_now:
+        # each sample's loss relative to its own label energy (labels span more
+        # than an order of magnitude with the solid fraction)
+        sample_w = 1.0 / labels.pow(2).mean(dim=(1, 2, 3, 4)).clamp_min(1e-12)
+        hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20),
+                        sample_w=sample_w, lr_min=args.lr * 0.01, warmup=100 if not args.init_weights else 20)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     tc_status = net.status()
@@ -1060,7 +1078,7 @@ def run_warmstart(args):
                    "precision": "BF16 weights/activations, FP32 accumulation (tcgen05)"},
         "packing_s": round(t_pack, 1), "labels_s": round(t_labels, 1),
         "label_steps": {"mean": float(np.mean(lsteps)), "max": int(np.max(lsteps))},
-        "train_s": round(t_train, 1), "train_ms_per_iteration": round(1e3 * t_train / iters, 2),
+        "train_s": round(t_train, 1), "train_ms_per_iteration": round(1e3 * t_train / iters, 2) if iters else None,
         "loss": hist, "tc_status": tc_status,
         "eval": rows,
         "summary": summary(WARM_CHECKS[-1]),
@@ -1077,7 +1095,8 @@ def run_warmstart(args):
         WS.save_weights(net, args.save_weights,
                         meta={"train_samples": args.train, "train_side": side, "epochs": args.epochs,
                               "iterations": iters, "seed": WARM_SEED, "label_tol": args.label_tol,
-                              "final_loss": hist[-1] if hist else None})
+                              "final_loss": hist[-1] if hist else None, "lr": args.lr,
+                              "fine_tuned_from": init_meta})
 
 
 def warm_leg(torch, L, args):
@@ -1171,6 +1190,10 @@ def main():
     ap.add_argument("--label-tol", type=float, default=1e-7)
     ap.add_argument("--label-maxsteps", type=int, default=20000)
     ap.add_argument("--save-weights", default="")
+    ap.add_argument("--init-weights", default="", help="warmstart workload: start from a saved network (fine-tune; "
+                                                         "with --epochs 0 only evaluate it)")
+    ap.add_argument("--eval-offset", type=int, default=None,
+                    help="warmstart workload: index of the first held-out packing (default: after the training set)")
     ap.add_argument("--features", type=int, default=1, choices=[0, 1, 2],
                     help="warmstart workload: input encoding (wall distance searched to 5 or 12)")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")

@@ -425,6 +425,17 @@ def load_weights(path=WEIGHTS):
     return params, tuple(int(v) for v in z["widths"]), int(z["features"][0]), meta
 
 
+def with_adam_state(params):
+    """params of load_weights with zero Adam moments, ready for training
+    (fine-tuning a saved network)."""
+    import torch
+    for p in params.values():
+        for key in ("w", "b"):
+            p["m" + key] = torch.zeros_like(p[key])
+            p["v" + key] = torch.zeros_like(p[key])
+    return params
+
+
 def packing_specs(n, seed, phi_range=(0.1, 0.5), r_range=(3.0, 8.0)):
     """Seeded (phi, packing seed) pairs; spheres may overlap (a Boolean model),
     since non-overlapping random addition stalls near phi = 0.38."""
