@@ -217,19 +217,12 @@ __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, 
     for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
   } else {
     t[0] = P[x];
-    if (!(fl & FLAG_LINKS)) {
-      // no bounce-back link (most nodes): every population comes from its
-      // upstream neighbour, each slot fixed by q
 #pragma unroll
-      for (int q = 1; q < 15; q++) t[q] = P[OPP(q) * S + nb.at(-CX(q), -CY(q), -CZ(q))];
-    } else {
-#pragma unroll
-      for (int q = 1; q < 15; q++) {
-        const bool bnd = (fl >> q) & 1;
-        const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
-        const int slot = bnd ? q : OPP(q);
-        t[q] = P[slot * S + src];
-      }
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> q) & 1;
+      const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
+      const int slot = bnd ? q : OPP(q);
+      t[q] = P[slot * S + src];
     }
   }
 }
@@ -254,17 +247,12 @@ __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb,
     for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
   } else {
     P[x] = t[0];
-    if (!(fl & FLAG_LINKS)) {
 #pragma unroll
-      for (int q = 1; q < 15; q++) P[q * S + nb.at(CX(q), CY(q), CZ(q))] = t[q];
-    } else {
-#pragma unroll
-      for (int q = 1; q < 15; q++) {
-        const bool bnd = (fl >> OPP(q)) & 1;
-        const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
-        const int slot = bnd ? OPP(q) : q;
-        P[slot * S + dst] = t[q];
-      }
+    for (int q = 1; q < 15; q++) {
+      const bool bnd = (fl >> OPP(q)) & 1;
+      const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
+      const int slot = bnd ? OPP(q) : q;
+      P[slot * S + dst] = t[q];
     }
   }
 }
