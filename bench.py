@@ -948,8 +948,6 @@ def batch_leg(torch, L, args):
 # ---- learned warm start ------------------------------------------------------
 
 WARM_SEED, WARM_FORCE = 3, 1e-6
-WARM_CHECKS = (100, 50)  # permeability check intervals of the time-to-accuracy comparison
-WARM_VARIANTS = ("velocity_only", "state_whole_force_shift")
 
 
 def run_warmstart(args):
@@ -1007,16 +1005,21 @@ def run_warmstart(args):
         # than an order of magnitude with the solid fraction)
         sample_w = 1.0 / labels.pow(2).mean(dim=(1, 2, 3, 4)).clamp_min(1e-12)
         hist = WS.train(net, masks, labels, iters, lr=args.lr, seed=2, log_every=max(1, iters // 20),
-                        sample_w=sample_w, lr_min=args.lr * 0.01, warmup=100 if not args.init_weights else 20)
+                        sample_w=sample_w, lr_min=args.lr * 0.01, warmup=100 if not args.init_weights else 20,
+                        proj_weight=args.proj_weight)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     tc_status = net.status()
     # held-out packings at the evaluation size
     inf = WS.UNet(L, ev_side, ev_side, ev_side, batch=1, params=net.params, features=args.features)
     rows = []
+    checks = tuple(int(c) for c in args.warm_checks.split(",") if c)
+    variants = tuple(v for v in args.warm_variants.split(",") if v)
+    corrections = tuple(int(c) for c in args.warm_correct.split(",") if c)
     for phi, sd in ev_specs:
         solid = WS.packing(ev_side, phi, sd)
-        traj = WS.permeability_run(L, solid, force)
+        pstats = {}
+        traj = WS.permeability_run(L, solid, force, stats=pstats)
         k_conv = traj[-1][1]
         sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
         torch.cuda.synchronize()
@@ -1024,11 +1027,15 @@ def run_warmstart(args):
         u, drho = WS.predict_state(inf, sdev, force, WS.ETA_TAU1)
         torch.cuda.synchronize()
         t_inf = time.perf_counter() - t0
-        row = {"phi": round(phi, 4), "k": k_conv, "plain_converged_steps": traj[-1][0], "inference_s": round(t_inf, 4)}
+        row = {"phi": round(phi, 4), "k": k_conv, "plain_converged_steps": traj[-1][0], "inference_s": round(t_inf, 4),
+               "plain_final_force_imbalance": pstats["imbalance_final"]}
+        if args.warm_probe:
+            row["warm_probe"] = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho,
+                                                    probe=args.warm_probe)
         # time to k within 1e-4, the permeability measured every `check` steps
         # in both arms (the plain arm from rest, the warm arm from the
         # prediction, inference included)
-        for check in WARM_CHECKS:
+        for check in checks:
             tp = traj if check == 100 else WS.permeability_run(L, solid, force, k_ref=k_conv, check=check)
             plain = WS.first_within(tp, k_conv, 1e-4)
             trajw = WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho, check=check)
@@ -1044,7 +1051,12 @@ def run_warmstart(args):
         # the same network set without its density (rho = rho0, u - F / rho0,
         # the best shift without a density) and with its density but the
         # whole-force shift (the warm start sets u - F / (2 rho0) and rho)
-        for name in WARM_VARIANTS:
+        for n in corrections:  # the force-balance correction `n` steps after the warm state
+            hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho, check=50,
+                                                     correct=n), k_conv, 1e-4)
+            row[f"check50_correct{n}"] = {"warm_steps": hs[0] if hs else None,
+                                          "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
+        for name in variants:
             if name == "velocity_only":
                 vs, ds = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0), None
             else:
@@ -1075,6 +1087,8 @@ def run_warmstart(args):
                    "phi": [0.1, 0.5], "radii": [3.0, 8.0], "spheres_overlap": True, "force": force, "tau": 1.0,
                    "widths": list(net.widths), "batch": args.batch, "iterations": iters,
                    "lr": f"{args.lr:g} -> {args.lr * 0.01:g} (half cosine)",
+                   "loss": "relative MSE per sample" + (f" + {args.proj_weight:g} x (projection of the velocity error "
+                                                        "on the label)^2" if args.proj_weight > 0 else ""),
                    "input": {0: "solid mask", 1: "solid mask + periodic wall distance d/5 and (d/5)^2 (d capped at 5)",
                              2: "solid mask + periodic wall distance d/12, (d/12)^2 (capped at 12) and min(d,5)/5"}[
                                  args.features],
@@ -1086,14 +1100,18 @@ def run_warmstart(args):
         "train_s": round(t_train, 1), "train_ms_per_iteration": round(1e3 * t_train / iters, 2) if iters else None,
         "loss": hist, "tc_status": tc_status,
         "eval": rows,
-        "summary": summary(WARM_CHECKS[-1]),
-        "summary_by_check": [summary(c) for c in WARM_CHECKS],
+        "summary": summary(checks[-1]),
+        "summary_by_check": [summary(c) for c in checks],
         "variants_at_check50": {
             name: {"wall_speedup_mean": float(np.mean([r["check50"]["plain_wall_s"] / r[f"check50_{name}"]["warm_wall_s"]
                                                        for r in rows if r[f"check50_{name}"]["warm_wall_s"]])),
                    "steps_ratio_mean": float(np.mean([r["check50"]["plain_steps"] / r[f"check50_{name}"]["warm_steps"]
-                                                      for r in rows if r[f"check50_{name}"]["warm_steps"]]))}
-            for name in WARM_VARIANTS},
+                                                      for r in rows if r[f"check50_{name}"]["warm_steps"]])),
+                   "plain_wall_total_s": round(float(sum(r["check50"]["plain_wall_s"] for r in rows
+                                                         if r[f"check50_{name}"]["warm_wall_s"])), 3),
+                   "warm_wall_total_s": round(float(sum(r[f"check50_{name}"]["warm_wall_s"] for r in rows
+                                                        if r[f"check50_{name}"]["warm_wall_s"])), 3)}
+            for name in variants + tuple(f"correct{n}" for n in corrections)} if 50 in checks else None,
     }
     print(json.dumps(line), flush=True)
     if args.save_weights:
@@ -1101,6 +1119,7 @@ def run_warmstart(args):
                         meta={"train_samples": args.train, "train_side": side, "epochs": args.epochs,
                               "iterations": iters, "seed": WARM_SEED, "label_tol": args.label_tol,
                               "final_loss": hist[-1] if hist else None, "lr": args.lr,
+                              "proj_weight": args.proj_weight,
                               "fine_tuned_from": init_meta})
 
 
@@ -1199,6 +1218,17 @@ def main():
                                                          "with --epochs 0 only evaluate it)")
     ap.add_argument("--eval-offset", type=int, default=None,
                     help="warmstart workload: index of the first held-out packing (default: after the training set)")
+    ap.add_argument("--proj-weight", type=float, default=0.0,
+                    help="warmstart workload: weight of the squared projection of the velocity error on the label")
+    ap.add_argument("--warm-checks", default="100,50",
+                    help="warmstart workload: permeability check intervals of the time-to-accuracy comparison")
+    ap.add_argument("--warm-variants", default="velocity_only,state_whole_force_shift",
+                    help="warmstart workload: other ways of setting the prediction, timed at 50-step checks")
+    ap.add_argument("--warm-correct", default="",
+                    help="warmstart workload: force-balance corrections of the mean flow, after these steps")
+    ap.add_argument("--warm-probe", type=int, default=0,
+                    help="warmstart workload: record the force imbalance and permeability error of this many "
+                         "measures in a row after the warm state")
     ap.add_argument("--features", type=int, default=1, choices=[0, 1, 2],
                     help="warmstart workload: input encoding (wall distance searched to 5 or 12)")
     ap.add_argument("--side", type=int, default=512, help="tracer workload: lattice side")

@@ -310,10 +310,20 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
  * dy0, dy1, dy2 = dY with its periodic halo at shift -1, 0, 1 (shift =
  * dx - 1 for the taps of dx = 0, 1, 2), xt = X with a zero halo at shift 0.  K is split over `splits`
  * blocks into partial (splits * 27 * cout * cin floats) summed in order.
- * cout 32, 64, 128 or a multiple of 128; cin a multiple of 16. */
+ * cout 32, 64, 128 or a multiple of 128; cin a multiple of 16.  For cout
+ * <= 128 the taps' y/z offsets move to the input (27 taps in one block per
+ * K range: dx along M, (dy, dz) taps x input channels along N). */
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream);
+/* The same, added to dw when accumulate is set (batches taken a sample at a
+ * time, so that the channel-major copies of one sample stay in L2). */
+int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
+                      int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats,
+                      int splits, float *dw, int accumulate, void *stream);
+/* K splits for slbc_tc_wgrad that fill the current device once (at most
+ * k_tiles / 8 and max_splits; k_tiles = B * pstride / 64). */
+int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_splits);
 
 /* Network glue of the learned warm start (same buffers; channel slices
  * [coff, coff + C) with C, coff, ctot multiples of 8; D, H, W the fine grid).
@@ -350,6 +360,13 @@ int slbc_nn_adam(float *p, const float *g, float *m, float *v, long long n, floa
                  int t, void *stream);
 int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int nch, const float *sample_w, int B, int D, int H,
                 int W, void *grad, int gctot, double *loss, void *stream);
+/* Projection term of the loss, after slbc_nn_mse on the same buffers: per
+ * sample s_n = <label_n, pred_n - label_n> / lab_sq[n] (labels
+ * [n][D][H][W][lch], channels [0, nch) taken, lab_sq[n] = <label_n,
+ * label_n> over them, device doubles), loss += (weight / B) sum_n s_n^2 and
+ * its derivative added to grad; dot: B device doubles of scratch. */
+int slbc_nn_proj(const float *pred, int ctot_p, const float *label, int lch, int nch, const double *lab_sq, int B,
+                 int D, int H, int W, float weight, void *grad, int gctot, double *dot, double *loss, void *stream);
 /* Gradient-norm clipping against a running norm, without a host round
  * trip: slbc_nn_sqsum adds the sum of squares of one gradient tensor to
  * state[0] (call it for every tensor), slbc_nn_clip turns the total into

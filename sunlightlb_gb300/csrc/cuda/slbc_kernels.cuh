@@ -205,16 +205,29 @@ __device__ __forceinline__ void apply_wall(T (&t)[15], uint16_t fl, bool solid, 
   }
 }
 
+// Element index of population `slot` of node `node`.  I32: the whole
+// population array (15 x S elements) is indexable in 32 unsigned bits, so
+// the index is formed and scaled in 32-bit arithmetic (one multiply-add and
+// one widening address multiply per access instead of 64-bit products).
+template <bool I32>
+__device__ __forceinline__ auto pop_index(int slot, long long S, int node) {
+  if constexpr (I32) {
+    return (unsigned)slot * (unsigned)S + (unsigned)node;
+  } else {
+    return slot * S + node;
+  }
+}
+
 // Populations of node x entering a fused update.  ODD = false (C1 -> C0):
 // the node's own slots; ODD = true (C0 -> C1): pulled from the upstream
 // neighbours x - c_q, or from the node's own slot q across a bounce-back
 // link (bit q of fl).
-template <typename T, bool ODD>
+template <typename T, bool ODD, bool I32 = false>
 __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, const Nbr &nb, int x,
                                           uint16_t fl, T (&t)[15]) {
   if (!ODD) {
 #pragma unroll
-    for (int q = 0; q < 15; q++) t[q] = P[q * S + x];
+    for (int q = 0; q < 15; q++) t[q] = P[pop_index<I32>(q, S, x)];
   } else {
     t[0] = P[x];
 #pragma unroll
@@ -222,7 +235,7 @@ __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, 
       const bool bnd = (fl >> q) & 1;
       const int src = bnd ? x : nb.at(-CX(q), -CY(q), -CZ(q));
       const int slot = bnd ? q : OPP(q);
-      t[q] = P[slot * S + src];
+      t[q] = P[pop_index<I32>(slot, S, src)];
     }
   }
 }
@@ -230,7 +243,7 @@ __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, 
 // Wall terms, collision and the write-back of node x (the slots load_pops
 // read: locally reversed for the even step, pushed to the neighbours, or to
 // the node's own opposite slot across a bounce-back link, for the odd one).
-template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU>
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, bool I32 = false>
 __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb, int x, uint16_t fl,
                                             T (&t)[15]) {
   T *__restrict__ P = a.p.pop;
@@ -244,7 +257,7 @@ __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb,
   }
   if (!ODD) {
 #pragma unroll
-    for (int q = 0; q < 15; q++) P[OPP(q) * S + x] = t[q];
+    for (int q = 0; q < 15; q++) P[pop_index<I32>(OPP(q), S, x)] = t[q];
   } else {
     P[x] = t[0];
 #pragma unroll
@@ -252,7 +265,7 @@ __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb,
       const bool bnd = (fl >> OPP(q)) & 1;
       const int dst = bnd ? x : nb.at(CX(q), CY(q), CZ(q));
       const int slot = bnd ? OPP(q) : q;
-      P[slot * S + dst] = t[q];
+      P[pop_index<I32>(slot, S, dst)] = t[q];
     }
   }
 }
@@ -279,8 +292,9 @@ __device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, in
 // nodes' slot sets meet; it keeps about two rows of loads in flight per
 // thread and removes the flag-then-populations round trip of the odd step
 // from every row but the first.
-// Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).
-template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT>
+// Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).  I32: 15 x npad
+// elements fit 32 unsigned bits (pop_index).
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT, bool I32 = false>
 __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.z;
@@ -295,7 +309,7 @@ __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
     if (r < nrow) fl[r] = __ldg(a.p.flags + ((i * a.p.esj + j0 + r) * a.p.esk + k));
   Nbr nb = make_nbr(i, j0, k, a.p.esi, a.p.esj, a.p.esk);
   T cur[15];
-  load_pops<T, ODD>(P, S, nb, nb.at(0, 0, 0), fl[0], cur);
+  load_pops<T, ODD, I32>(P, S, nb, nb.at(0, 0, 0), fl[0], cur);
 #pragma unroll
   for (int r = 0; r < NPT; r++) {
     if (r >= nrow) break;
@@ -304,9 +318,9 @@ __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
     const bool more = r + 1 < nrow;
     if (more) {
       nbn = make_nbr(i, j0 + r + 1, k, a.p.esi, a.p.esj, a.p.esk);
-      load_pops<T, ODD>(P, S, nbn, nbn.at(0, 0, 0), fl[r + 1 < NPT ? r + 1 : r], nxt);
+      load_pops<T, ODD, I32>(P, S, nbn, nbn.at(0, 0, 0), fl[r + 1 < NPT ? r + 1 : r], nxt);
     }
-    finish_node<T, ODD, EXACT, MOVING, BFU>(a, nb, nb.at(0, 0, 0), fl[r], cur);
+    finish_node<T, ODD, EXACT, MOVING, BFU, I32>(a, nb, nb.at(0, 0, 0), fl[r], cur);
     if (more) {
 #pragma unroll
       for (int q = 0; q < 15; q++) cur[q] = nxt[q];

@@ -68,9 +68,17 @@ static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
     return;
   }
   const dim3 grid((unsigned)((L.esk + bx - 1) / bx), (unsigned)((L.esj + npt - 1) / npt), (unsigned)L.esi);
-  if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4><<<grid, bx, 0, L.stream>>>(a);
-  else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2><<<grid, bx, 0, L.stream>>>(a);
-  else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1><<<grid, bx, 0, L.stream>>>(a);
+  // 32-bit population indices whenever all 15 arrays fit (lattices up to
+  // about 286 M nodes)
+  if (15LL * L.npad <= 0xFFFFFFFFLL) {
+    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, true><<<grid, bx, 0, L.stream>>>(a);
+    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, true><<<grid, bx, 0, L.stream>>>(a);
+    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, true><<<grid, bx, 0, L.stream>>>(a);
+  } else {
+    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, false><<<grid, bx, 0, L.stream>>>(a);
+    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, false><<<grid, bx, 0, L.stream>>>(a);
+    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, false><<<grid, bx, 0, L.stream>>>(a);
+  }
 }
 
 template <bool ODD>

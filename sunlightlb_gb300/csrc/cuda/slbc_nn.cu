@@ -302,6 +302,54 @@ __global__ void k_mse(const float *pred, int ctot_p, const float *label, int nch
   if (threadIdx.x == 0) atomicAdd(loss, sh[0] * inv);
 }
 
+// Projection of the prediction error on the label, per sample n:
+// s_n = <label_n, pred_n - label_n> / <label_n, label_n> over the interior
+// voxels and channels [0, nch) (labels [n][D][H][W][lch]).  k_proj_dot adds <label_n, pred_n> into
+// dot[n] (grid.y = sample); k_proj_grad adds the derivative of
+// (weight / B) * sum_n s_n^2 to the BF16 gradient and the term to the loss.
+__global__ void k_proj_dot(const float *pred, int ctot_p, const float *label, int lch, int nch, int D, int H, int W,
+                           double *dot) {
+  __shared__ double sh[256];
+  const int n = blockIdx.y;
+  const long long per = (long long)D * H * W;
+  double acc = 0.0;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < per; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H);
+    const int z = (int)(r / H);
+    const long long v = vox(n, z, y, x, D, H, W);
+    const float *lb = label + ((long long)n * per + e) * lch;
+    for (int c = 0; c < nch; c++) acc += (double)pred[v * ctot_p + c] * (double)lb[c];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(dot + n, sh[0]);
+}
+
+__global__ void k_proj_grad(const float *label, int lch, int nch, const double *lab_sq, const double *dot, int B, int D,
+                            int H, int W, float weight, bf16 *grad, int gctot, double *loss) {
+  const long long per = (long long)D * H * W, total = (long long)B * per;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    const int x = (int)(r % W); r /= W;
+    const int y = (int)(r % H); r /= H;
+    const int z = (int)(r % D);
+    const int n = (int)(r / D);
+    const double q = lab_sq[n];
+    if (!(q > 0.0)) continue;
+    const double sn = (dot[n] - q) / q;
+    const float coef = (float)(2.0 * weight * sn / (q * B));
+    bf16 *gp = grad + vox(n, z, y, x, D, H, W) * gctot;
+    for (int c = 0; c < nch; c++) gp[c] = __float2bfloat16(__bfloat162float(gp[c]) + coef * label[e * lch + c]);
+    if (e % per == 0) atomicAdd(loss, (double)weight * sn * sn / B);
+  }
+}
+
 // input encoding: channel 0 = 1 on solid nodes, 0 on fluid; with
 // features = 1, channel 1 = d / R and channel 2 = (d / R)^2 where d is the
 // periodic distance from a fluid node to the nearest solid node, searched
@@ -507,6 +555,21 @@ int slbc_nn_mse(const float *pred, int ctot_p, const float *label, int nch, cons
   k_mse<<<std::min(grid_for((long long)B * D * H * W), 152 * 4), 256, 0, (cudaStream_t)stream>>>(
       pred, ctot_p, label, nch, sample_w, B, D, H, W, (bf16 *)grad, gctot, loss);
   return launched("slbc_nn_mse");
+}
+
+int slbc_nn_proj(const float *pred, int ctot_p, const float *label, int lch, int nch, const double *lab_sq, int B, int D,
+                 int H, int W, float weight, void *grad, int gctot, double *dot, double *loss, void *stream) {
+  if (nch < 1 || lch < nch || ctot_p < nch || gctot % 8 || gctot < nch || B < 1 || B > 65535)
+    return bad("slbc_nn_proj: bad arguments");
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(dot, 0, sizeof(double) * B, st) != cudaSuccess) return bad("slbc_nn_proj: memset");
+  const long long per = (long long)D * H * W;
+  const dim3 g1((unsigned)std::min<long long>((per + 255) / 256, 152), (unsigned)B);
+  k_proj_dot<<<g1, 256, 0, st>>>(pred, ctot_p, label, lch, nch, D, H, W, dot);
+  if (launched("slbc_nn_proj")) return 1;
+  k_proj_grad<<<std::min(grid_for((long long)B * per), 152 * 4), 256, 0, st>>>(label, lch, nch, lab_sq, dot, B, D, H,
+                                                                                W, weight, (bf16 *)grad, gctot, loss);
+  return launched("slbc_nn_proj");
 }
 
 int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void *out, int ctot, int features,

@@ -710,10 +710,199 @@ k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensor
   if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)w.tmem_cols);
 }
 
-// dw[i] = sum over splits of partial[s][i], in split order
-__global__ void k_sum_splits(const float *partial, long long n, int splits, float *dw) {
+// ---- weight gradients, taps stacked along N ----------------------------------
+// The same sum with the y/z part of the tap offset moved to the input:
+// dW[tap][co][ci] = sum_v S_dx[v][co] * X[v + s][ci], s = (dy - 1) * Wp +
+// (dz - 1) * plane (v = u - s; X is zero outside its interior and TMA fills
+// zeros outside the array, so the terms are the same).  Per K tile of 64
+// flat positions a block then loads the three dY copies once (M: dx blocks
+// of cout rows, 128 rows = up to 3 copies, a 4th block of 32 rows for cout =
+// 32 is never loaded and its accumulator rows are dropped) and the input
+// window at nt shifts s (N: nt taps x cc input channels, up to 288 rows in
+// two MMAs), instead of 27 shifted dY tiles against one input tile: the
+// operand bytes staged per FLOP drop 2.7x for 32 channels, and every MMA
+// is 128 x 144 instead of 128 x 32.
+struct WgradNArgs {
+  int cin, cout;
+  int dpm;        // dx copies per M tile
+  int nt;         // (dy, dz) taps per block
+  int groups;     // tap groups: ceil(9 / nt)
+  int cc;         // input channels per block (cin, or a divisor of it)
+  int ci_chunks;  // cin / cc
+  int n_rows;     // nt * cc: accumulator columns
+  int n_mma;      // columns per MMA (n_rows split into equal parts of <= 256)
+  int Wp, plane;
+  long long k_tiles;
+  int splits;
+  int tmem_cols;
+  float *partial;  // [splits][27][cout][cin]
+};
+
+constexpr int kWgnMaxRows = 288;
+constexpr int kWgnSmem = kStages * (kWgTileA + kWgnMaxRows * 128) + 1024;
+
+// Block decomposition of k_wgrad_n for (cin, cout); false when it does not
+// apply (cout not 32, 64 or 128).
+bool wgrad_n_plan(int cin, int cout, WgradNArgs &w) {
+  if (!(cout == 32 || cout == 64 || cout == 128) || cin < 16 || cin % 16) return false;
+  w.cin = cin;
+  w.cout = cout;
+  w.dpm = std::min(128 / cout, 3);
+  int cc = cin;
+  if (cc > 256) {
+    cc = 0;
+    for (int c = 256; c >= 16; c -= 16)
+      if (cin % c == 0) { cc = c; break; }
+    if (!cc) return false;
+  }
+  int groups = (9 * cc + kWgnMaxRows - 1) / kWgnMaxRows, nt = (9 + groups - 1) / groups;
+  while (nt * cc > kWgnMaxRows) {
+    groups++;
+    nt = (9 + groups - 1) / groups;
+  }
+  w.cc = cc;
+  w.ci_chunks = cin / cc;
+  w.nt = nt;
+  w.groups = groups;
+  w.n_rows = nt * cc;
+  const int parts = (w.n_rows + 255) / 256;
+  if (w.n_rows % (16 * parts)) return false;
+  w.n_mma = w.n_rows / parts;
+  w.tmem_cols = 32;
+  while (w.tmem_cols < w.n_rows) w.tmem_cols *= 2;
+  return true;
+}
+
+int wgrad_n_ctas(const WgradNArgs &w) { return ((3 + w.dpm - 1) / w.dpm) * w.groups * w.ci_chunks; }
+
+__global__ void __launch_bounds__(128, 1)
+k_wgrad_n(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap a1,
+          const __grid_constant__ CUtensorMap a2, const __grid_constant__ CUtensorMap tb, WgradNArgs w, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
+  uint8_t *tA = smem_raw + pad;
+  uint8_t *tB = tA + kStages * kWgTileA;
+  const int tile_b = w.n_rows * 128;  // bytes of one B stage (a multiple of 2048)
+  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint32_t tmem_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int chunk = blockIdx.x % w.ci_chunks;
+  const int g = (blockIdx.x / w.ci_chunks) % w.groups;
+  const int mt = blockIdx.x / (w.ci_chunks * w.groups);
+  const int ci0 = chunk * w.cc;
+  const long long per = (w.k_tiles + w.splits - 1) / w.splits;
+  const long long k_lo = (long long)blockIdx.z * per;
+  const long long k_hi = k_lo + per < w.k_tiles ? k_lo + per : w.k_tiles;
+  const int nk = k_hi > k_lo ? (int)(k_hi - k_lo) : 0;
+  // bytes landing per stage: the dY copies and input windows actually loaded
+  int a_blocks = 0, b_taps = 0;
+  for (int d = 0; d < w.dpm; d++) a_blocks += mt * w.dpm + d < 3;
+  for (int t = 0; t < w.nt; t++) b_taps += g * w.nt + t < 9;
+  const uint32_t bytes = (uint32_t)(a_blocks * w.cout * 128 + b_taps * w.cc * 128);
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, (uint32_t)w.tmem_cols);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < kStages; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  int issued = 0;
+  if (threadIdx.x == 0) {
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (kt >= kStages && !tc::mbar_wait(&empty[s], ((kt / kStages) - 1) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      const int k0 = (int)((k_lo + kt) * 64);
+      tc::mbar_expect_tx(&full[s], bytes);
+      for (int d = 0; d < w.dpm; d++) {
+        const int dx = mt * w.dpm + d;
+        if (dx >= 3) break;
+        const CUtensorMap *am = dx == 0 ? &a0 : (dx == 1 ? &a1 : &a2);
+        tc::tma_load_2d(tA + s * kWgTileA + d * w.cout * 128, am, &full[s], k0, 0);
+      }
+      for (int t = 0; t < w.nt; t++) {
+        const int yz = g * w.nt + t;
+        if (yz >= 9) break;
+        const int dy = yz % 3, dz = yz / 3;
+        // may start before 0 or end past the array: TMA fills zeros there
+        const int x = k0 + (dy - 1) * w.Wp + (dz - 1) * w.plane;
+        tc::tma_load_2d(tB + s * tile_b + t * w.cc * 128, &tb, &full[s], x, ci0);
+      }
+      issued = kt + 1;
+    }
+  } else if (threadIdx.x == 32) {
+    const uint32_t idesc = tc::idesc_bf16(128, w.n_mma);
+    const int parts = w.n_rows / w.n_mma;
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (!tc::mbar_wait(&full[s], (kt / kStages) & 1, kWaitLimit)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const uint64_t ad = tc::smem_desc(tA + s * kWgTileA, tc::kSwizzle128, 128);
+      for (int j = 0; j < parts; j++) {
+        const uint64_t bd = tc::smem_desc(tB + s * tile_b + j * w.n_mma * 128, tc::kSwizzle128, 128);
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+          tc::mma_bf16(tmem + (uint32_t)(j * w.n_mma), ad + 2 * kk, bd + 2 * kk, idesc, (kt | kk) != 0);
+      }
+      tc::mma_commit(&empty[s]);
+    }
+    tc::mma_commit(&done);
+  }
+  __syncwarp();
+  const bool okd = __all_sync(0xffffffffu, tc::mbar_wait(&done, 0, kWaitLimit));
+  tc::fence_after_sync();
+  if (okd) {
+    const int r = warp * 32 + lane;
+    const int d = r / w.cout, co = r % w.cout;
+    const int dx = mt * w.dpm + d;
+    const bool row_ok = d < w.dpm && dx < 3;
+#pragma unroll 1
+    for (int c = 0; c < w.n_rows; c += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);  // whole warp
+      if (nk == 0) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = 0.0f;
+      }
+      const int t = c / w.cc, yz = g * w.nt + t;
+      if (row_ok && yz < 9) {
+        const int tap = (yz / 3) * 9 + (yz % 3) * 3 + dx;
+        float *dst = w.partial + (((long long)blockIdx.z * 27 + tap) * w.cout + co) * w.cin + ci0 + c % w.cc;
+        ((float4 *)dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
+        ((float4 *)dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
+      }
+    }
+  }
+  if (!ok || !okd) atomicExch(err, 1);
+  if (threadIdx.x == 0) {
+    for (int kt = issued > kStages ? issued - kStages : 0; kt < issued; kt++)
+      if (!tc::mbar_wait(&full[kt % kStages], (kt / kStages) & 1, kWaitLimit)) atomicExch(err, 2);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)w.tmem_cols);
+}
+
+// dw[i] = sum over splits of partial[s][i], in split order (added to dw[i]
+// when accumulate is set)
+__global__ void k_sum_splits(const float *partial, long long n, int splits, float *dw, int accumulate) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    float v = 0.0f;
+    float v = accumulate ? dw[i] : 0.0f;
     for (int s = 0; s < splits; s++) v += partial[(long long)s * n + i];
     dw[i] = v;
   }
@@ -930,14 +1119,78 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
   return 0;
 }
 
+int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_splits) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 152;
+  WgradNArgs wn;
+  long long want;
+  if (wgrad_n_plan(cin, cout, wn)) {
+    const int ctas = wgrad_n_ctas(wn);  // one block per SM
+    want = (sms + ctas - 1) / ctas;
+  } else {  // two blocks per SM
+    const int co_rows = cout < 128 ? cout : 128;
+    int ntile = cin;
+    while (ntile > 256) ntile /= 2;
+    const int blocks = ((27 + 128 / co_rows - 1) / (128 / co_rows)) * (cout / co_rows) * (cin / ntile);
+    want = 2 * sms / blocks + 1;
+  }
+  want = std::min(want, std::max(1LL, k_tiles / 8));
+  want = std::min(want, max_splits);
+  return (int)std::max(1LL, want);
+}
+
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream) {
+  return slbc_tc_wgrad_acc(dy0, dy1, dy2, xt, B, D, H, W, Wp, pstride, cin, cout, partial, partial_floats, splits, dw,
+                           0, stream);
+}
+
+int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
+                      int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats,
+                      int splits, float *dw, int accumulate, void *stream) {
   WgradArgs w;
   if (cout < 32 || (cout > 128 && cout % 128) || (cout <= 128 && 128 % cout) || cin < 16 || cin % 16)
     return slbc::set_error("slbc_tc_wgrad: cout must be 32, 64, 128 or a multiple of 128; cin a multiple of 16"), 1;
   if (Wp < W + 2 || Wp % 8 || pstride % 64 || pstride < (long long)(D + 2) * (H + 2) * Wp || splits < 1)
     return slbc::set_error("slbc_tc_wgrad: bad geometry"), 1;
+  if (partial_floats < (long long)splits * 27 * cout * cin)
+    return slbc::set_error("slbc_tc_wgrad: partial buffer too small"), 1;
+  if (!aligned16(dy0) || !aligned16(dy1) || !aligned16(dy2) || !aligned16(xt) || !aligned16(partial) ||
+      !aligned16(dw))
+    return slbc::set_error("slbc_tc_wgrad: buffers must be 16-byte aligned"), 1;
+  const long long cols = (long long)B * pstride;
+  WgradNArgs wn;
+  if (wgrad_n_plan(cin, cout, wn)) {  // taps stacked along N
+    wn.Wp = Wp;
+    wn.plane = (H + 2) * Wp;
+    wn.k_tiles = cols / 64;
+    wn.splits = splits;
+    wn.partial = partial;
+    int *err = tc_err_flag();
+    if (!err) return slbc::set_error("slbc_tc_wgrad: no device error flag"), 1;
+    CUtensorMap m0, m1, m2, mb;
+    if (!make_map_k64(&m0, dy0, cout, cols, cout) || !make_map_k64(&m1, dy1, cout, cols, cout) ||
+        !make_map_k64(&m2, dy2, cout, cols, cout) || !make_map_k64(&mb, xt, cin, cols, wn.cc))
+      return slbc::set_error("slbc_tc_wgrad: tensor map encoding failed"), 1;
+    static unsigned long long attr_n_done = 0;
+    cudaError_t e = smem_opt_in((const void *)k_wgrad_n, kWgnSmem, attr_n_done);
+    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
+    const dim3 grid((unsigned)wgrad_n_ctas(wn), 1, (unsigned)splits);
+    const int smem = kStages * (kWgTileA + wn.n_rows * 128) + 1024;
+    k_wgrad_n<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, wn, err);
+    slbc::count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
+    const long long n = 27LL * cout * cin;
+    k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
+        partial, n, splits, dw, accumulate);
+    slbc::count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
+    return 0;
+  }
   w.cin = cin; w.cout = cout;
   w.co_rows = cout < 128 ? cout : 128;
   w.taps_per_tile = 128 / w.co_rows;
@@ -952,14 +1205,8 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
   w.tmem_cols = 32;
   while (w.tmem_cols < w.ntile) w.tmem_cols *= 2;
   w.partial = partial;
-  if (partial_floats < (long long)splits * 27 * cout * cin)
-    return slbc::set_error("slbc_tc_wgrad: partial buffer too small"), 1;
-  if (!aligned16(dy0) || !aligned16(dy1) || !aligned16(dy2) || !aligned16(xt) || !aligned16(partial) ||
-      !aligned16(dw))
-    return slbc::set_error("slbc_tc_wgrad: buffers must be 16-byte aligned"), 1;
   int *err = tc_err_flag();
   if (!err) return slbc::set_error("slbc_tc_wgrad: no device error flag"), 1;
-  const long long cols = (long long)B * pstride;
   CUtensorMap m0, m1, m2, mb;
   if (!make_map_k64(&m0, dy0, cout, cols, w.co_rows) || !make_map_k64(&m1, dy1, cout, cols, w.co_rows) ||
       !make_map_k64(&m2, dy2, cout, cols, w.co_rows) || !make_map_k64(&mb, xt, cin, cols, w.ntile))
@@ -975,8 +1222,8 @@ int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void 
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
   const long long n = 27LL * cout * cin;
-  k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(partial, n,
-                                                                                                        splits, dw);
+  k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
+      partial, n, splits, dw, accumulate);
   slbc::count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;

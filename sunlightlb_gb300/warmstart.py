@@ -49,6 +49,7 @@ class Kernels:
             "slbc_tc_halo": [p] + [i] * 7 + [p],
             "slbc_tc_cmajor": [p] + [i] * 8 + [ll, i, i, p, p],
             "slbc_tc_wgrad": [p] * 4 + [i] * 5 + [ll, i, i, p, ll, i, p, p],
+            "slbc_tc_wgrad_acc": [p] * 4 + [i] * 5 + [ll, i, i, p, ll, i, p, i, p],
             "slbc_nn_pool": [p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_pool_bwd": [p, i, i, p, i, i, p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_up": [p, i, i, p, i, i] + [i] * 5 + [p],
@@ -58,6 +59,7 @@ class Kernels:
             "slbc_nn_wdgrad": [p, i, i, i, i, p, p],
             "slbc_nn_adam": [p, p, p, p, ll, f, f, f, f, i, p],
             "slbc_nn_mse": [p, i, p, i, p, i, i, i, i, p, i, p, p],
+            "slbc_nn_proj": [p, i, p, i, i, p, i, i, i, i, f, p, i, p, p, p],
             "slbc_nn_sqsum": [p, ll, p, p],
             "slbc_nn_clip": [p, f, f, p],
             "slbc_nn_scale": [p, ll, p, p],
@@ -72,6 +74,10 @@ class Kernels:
             fn.restype = C.c_int
             setattr(self, name[5:], self._checked(name, fn))
         dll.slbc_last_error.restype = C.c_char_p
+        # a count, not a status
+        self.tc_wgrad_splits = dll.slbc_tc_wgrad_splits
+        self.tc_wgrad_splits.argtypes = [i, i, ll, ll]
+        self.tc_wgrad_splits.restype = C.c_int
 
     def _checked(self, name, fn):
         def call(*a):
@@ -240,13 +246,16 @@ class UNet:
             "gB3": (3, w3), "gA3": (3, w3), "gP3": (3, w2),
         }
         self.grad = {n: self._act(lv, c) for n, (lv, c) in self.grad_spec.items()}
+        # channel-major copies of one sample (the weight gradients take a
+        # batch a sample at a time, so the copies just written are still in L2)
         Wp, ps = flat_geometry(self.D, self.H, self.W)
         maxc = max(c for _, c in self.buf_spec.values())
-        self.cm_x = torch.empty(maxc * self.B * ps, device=self.dev, dtype=torch.bfloat16)
-        self.cm_g = [torch.empty(w3 * self.B * ps, device=self.dev, dtype=torch.bfloat16) for _ in range(3)]
+        self.cm_x = torch.empty(maxc * ps, device=self.dev, dtype=torch.bfloat16)
+        self.cm_g = [torch.empty(max(w0, w3) * ps, device=self.dev, dtype=torch.bfloat16) for _ in range(3)]
         self.ws_floats = 1 << 26
         self.ws = torch.empty(self.ws_floats, device=self.dev, dtype=torch.float32)
         self.loss_acc = torch.zeros(1, device=self.dev, dtype=torch.float64)
+        self.proj_dot = torch.zeros(self.B, device=self.dev, dtype=torch.float64)
         for name, *_ in self.layers:
             p = self.params[name]
             p["gw"] = torch.zeros_like(p["w"])
@@ -261,23 +270,18 @@ class UNet:
         Wp, ps = flat_geometry(d, h, w)
         g = self.grad[g_name]
         x = self.buf[x_name]
-        for c, shift in zip(self.cm_g, (-1, 0, 1)):
-            k.tc_cmajor(g.data_ptr(), self.B, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0, c.data_ptr(),
-                        self.stream)
-        k.tc_cmajor(x.data_ptr(), self.B, d, h, w, x.shape[-1], x_coff, cin, Wp, ps, 0, 1, self.cm_x.data_ptr(),
-                    self.stream)
-        co_rows = min(cout, 128)
-        mtiles = ((27 + 128 // co_rows - 1) // (128 // co_rows)) * (cout // co_rows)
-        ntile = cin
-        while ntile > 256:
-            ntile //= 2
-        blocks = mtiles * (cin // ntile)
-        k_tiles = self.B * ps // 64
-        splits = max(1, min(2 * 152 // blocks + 1, k_tiles // 8, self.ws_floats // (27 * cout * cin)))
+        vol = (d + 2) * (h + 2) * (w + 2)
+        splits = k.tc_wgrad_splits(cin, cout, ps // 64, self.ws_floats // (27 * cout * cin))
         p = self.params[name]
-        k.tc_wgrad(self.cm_g[0].data_ptr(), self.cm_g[1].data_ptr(), self.cm_g[2].data_ptr(), self.cm_x.data_ptr(),
-                   self.B, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats, splits,
-                   p["gw"].data_ptr(), self.stream)
+        for n in range(self.B):
+            gp = g.data_ptr() + 2 * n * vol * g.shape[-1]
+            xp = x.data_ptr() + 2 * n * vol * x.shape[-1]
+            for c, shift in zip(self.cm_g, (-1, 0, 1)):
+                k.tc_cmajor(gp, 1, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0, c.data_ptr(), self.stream)
+            k.tc_cmajor(xp, 1, d, h, w, x.shape[-1], x_coff, cin, Wp, ps, 0, 1, self.cm_x.data_ptr(), self.stream)
+            k.tc_wgrad_acc(self.cm_g[0].data_ptr(), self.cm_g[1].data_ptr(), self.cm_g[2].data_ptr(),
+                           self.cm_x.data_ptr(), 1, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats,
+                           splits, p["gw"].data_ptr(), int(n > 0), self.stream)
         p["gb"].zero_()
         k.nn_bias_grad(g.data_ptr(), g.shape[-1], 0, self.B, d, h, w, cout, p["gb"].data_ptr(), self.stream)
 
@@ -294,9 +298,12 @@ class UNet:
                         o.data_ptr(), o.shape[-1], c0, 0, m.data_ptr() if m is not None else None, self.stream)
         self._halo(out_name)
 
-    def loss_and_backward(self, labels, sample_w=None):
-        """labels: device FP32 (B, D, H, W, 3); sample_w: optional device
-        FP32 (B,) loss weights.  Returns the loss (device scalar, FP64)."""
+    def loss_and_backward(self, labels, sample_w=None, proj=None):
+        """labels: device FP32 (B, D, H, W, 3 or 4); sample_w: optional device
+        FP32 (B,) loss weights; proj: optional (weight, lab_sq) adding weight
+        times the mean squared projection of the velocity error on the
+        label (lab_sq: device FP64 (B,) label energies over the 3 velocity
+        channels, slbc_nn_proj).  Returns the loss (device scalar, FP64)."""
         if self.grad is None:
             self._alloc_grads()
         k, G, X = self.k, self.grad, self.buf
@@ -305,6 +312,10 @@ class UNet:
         k.nn_mse(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), labels.shape[-1],
                  sample_w.data_ptr() if sample_w is not None else None, B, self.D, self.H, self.W, G["gOUT"].data_ptr(),
                  OUT_CH, self.loss_acc.data_ptr(), self.stream)
+        if proj is not None and proj[0] > 0:
+            k.nn_proj(X["OUT"].data_ptr(), OUT_CH, labels.data_ptr(), labels.shape[-1], 3, proj[1].data_ptr(), B,
+                      self.D, self.H, self.W, float(proj[0]), G["gOUT"].data_ptr(), OUT_CH, self.proj_dot.data_ptr(),
+                      self.loss_acc.data_ptr(), self.stream)
         self._halo("gOUT")
         # level 0 decoder
         self._wgrad("out", "gOUT", "D0")
@@ -551,33 +562,81 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5):
     return u, drho
 
 
+def set_warm(L, lb, warm_u, warm_drho, scale=1.0):
+    """Warm state through lbsetstatedev (velocity and density deviation) or
+    lbsetveldev (velocity only), both fields multiplied by `scale`."""
+    if scale != 1.0:
+        warm_u = warm_u * scale
+        warm_drho = warm_drho * scale if warm_drho is not None else None
+    if warm_drho is not None:
+        L.lbsetstatedev(lb, warm_u.data_ptr(), warm_drho.data_ptr())
+    else:
+        L.lbsetveldev(lb, warm_u.data_ptr())
+
+
+def wall_force_balance(L, lb, obj, body):
+    """Relative imbalance F_wall / F_body - 1 along x after one measure (two
+    steps): F_wall the momentum exchanged over the bounce-back links of the
+    bed's object, F_body = body = force * (fluid nodes), equal at steady
+    state."""
+    L.measure(lb)
+    return obj.frcx / body - 1.0
+
+
 def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-4, check=100, maxsteps=60000,
-                     warm_drho=None):
+                     warm_drho=None, correct=0, probe=0, stats=None):
     """Packed bed (device uint8 or numpy mask) until the relative change of
     the mean flow between checks is below tol (plain) or, given k_ref, until
     the permeability is within `rel` of k_ref; warm_u (device velocities,
     lbsetveldev layout) warm-starts the lattice, with warm_drho (device
     density deviations) through lbsetstatedev.  Returns the trajectory
     [(steps, k, wall seconds)] measured every `check` steps; the wall clock
-    starts before the warm start."""
+    starts before the warm start.
+
+    correct > 0 adds a force-balance correction of the warm start's mean
+    flow: `correct` steps after the warm state, one measure compares the
+    wall force with the body force.  In Stokes flow the wall force is linear
+    in the flow, so a prediction of the right shape but a mean flow (1 +
+    eps) times the converged one feels (1 + eps) times the body force; the
+    warm state is set again scaled by 1 / (1 + eps) and the steps and time
+    spent count towards the run.  probe > 0 (with k_ref) instead records,
+    for `probe` measures in a row after the warm state, the force imbalance
+    beside the permeability error: returns [(steps, imbalance, k error)].
+    A dict `stats` receives the force imbalance of the final state
+    ("imbalance_final")."""
     import torch
     mask = solid.cpu().numpy() if hasattr(solid, "cpu") else solid
     lb = L.newlb(mask.shape[0], mask.shape[1], mask.shape[2], "null")
     lb.precision = 1
     lb.tau = 1.0
     lb.stokes_flow = 1
-    W.insert_solid(L, lb, mask)
+    obj = W.insert_solid(L, lb, mask)
     L.syncobjs(lb)
     L.addbf(lb, force, 0.0, 0.0)
+    body = force * L.countfluid(lb)
     L.lbsteps(lb, 2)  # upload and tuning outside the timed region
     torch.cuda.synchronize()
     eta = lb.rho0 * (lb.tau - 0.5) / 3.0
     t0 = time.perf_counter()
-    if warm_u is not None and warm_drho is not None:
-        L.lbsetstatedev(lb, warm_u.data_ptr(), warm_drho.data_ptr())
-    elif warm_u is not None:
-        L.lbsetveldev(lb, warm_u.data_ptr())
     steps, prev, traj = 0, None, []
+    if warm_u is not None:
+        set_warm(L, lb, warm_u, warm_drho)
+        if probe > 0:
+            rows = []
+            for n in range(probe):
+                imb = wall_force_balance(L, lb, obj, body)
+                rows.append((2 * (n + 1), imb, (lb.vmeanx * eta / force - k_ref) / k_ref))
+            L.freelb(lb)
+            return rows
+        if correct > 0:
+            if correct > 2:
+                L.lbsteps(lb, correct - 2)
+            eps = wall_force_balance(L, lb, obj, body)
+            steps += max(correct, 2)
+            set_warm(L, lb, warm_u, warm_drho, 1.0 / (1.0 + eps))
+    elif probe > 0:
+        L.freelb(lb)
+        return []
     while steps < maxsteps:
         L.lbsteps(lb, check - 2)
         L.measure(lb)
@@ -590,6 +649,8 @@ def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-
         elif prev is not None and abs(lb.vmeanx - prev) <= tol * abs(lb.vmeanx):
             break
         prev = lb.vmeanx
+    if stats is not None:
+        stats["imbalance_final"] = obj.frcx / body - 1.0
     L.freelb(lb)
     return traj
 
@@ -626,6 +687,66 @@ def conv_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         out.append((lv, cin, cout, ms, 2.0 * 27 * cin * cout * batch * d ** 3 / (ms * 1e-3) / 1e12))
+    return out
+
+
+def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20, per_sample=False):
+    """Weight-gradient time of every layer shape of the network on `batch`
+    grids of side^3, CUDA events over `reps` calls on random BF16 data:
+    [(level, cin, cout, splits, ms, TFLOP/s)], FLOPs 2 * 27 * cin * cout *
+    interior voxels.  Default: slbc_tc_wgrad alone (the split sum included)
+    on ready channel-major copies of the whole batch.  per_sample: the
+    training step's path, per sample the four channel-major copies from
+    channels-last buffers and slbc_tc_wgrad_acc on them."""
+    import torch
+    k = Kernels(lib.dll)
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    w0, w1, w2, w3 = widths
+    shapes = [(0, IN_CH, w0), (0, w1 + w0, w0), (0, w0, w0), (1, w0, w1), (1, w1, w1), (1, w2 + w1, w1),
+              (2, w1, w2), (2, w2, w2), (2, w3 + w2, w2), (3, w2, w3), (3, w3, w3)]
+    ws_floats = 1 << 26
+    ws = torch.empty(ws_floats, device=dev, dtype=torch.float32)
+    out = []
+    for lv, cin, cout in shapes:
+        d = side >> lv
+        Wp, ps = flat_geometry(d, d, d)
+        nb = 1 if per_sample else batch
+        xt = torch.randn(cin, nb * ps, device=dev).to(torch.bfloat16)
+        dys = [torch.randn(cout, nb * ps, device=dev).to(torch.bfloat16) for _ in range(3)]
+        dw = torch.empty(27 * cout * cin, device=dev, dtype=torch.float32)
+        splits = k.tc_wgrad_splits(cin, cout, nb * ps // 64, ws_floats // (27 * cout * cin))
+        if per_sample:
+            x = torch.randn(batch, d + 2, d + 2, d + 2, cin, device=dev).to(torch.bfloat16)
+            g = torch.randn(batch, d + 2, d + 2, d + 2, cout, device=dev).to(torch.bfloat16)
+            vol = (d + 2) ** 3
+
+            def run():
+                for n in range(batch):
+                    for c, shift in zip(dys, (-1, 0, 1)):
+                        k.tc_cmajor(g.data_ptr() + 2 * n * vol * cout, 1, d, d, d, cout, 0, cout, Wp, ps, shift, 0,
+                                    c.data_ptr(), stream)
+                    k.tc_cmajor(x.data_ptr() + 2 * n * vol * cin, 1, d, d, d, cin, 0, cin, Wp, ps, 0, 1,
+                                xt.data_ptr(), stream)
+                    k.tc_wgrad_acc(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), 1, d, d,
+                                   d, Wp, ps, cin, cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), int(n > 0),
+                                   stream)
+        else:
+            def run():
+                k.tc_wgrad(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), batch, d, d, d,
+                           Wp, ps, cin, cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), stream)
+        for _ in range(3):
+            run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out.append((lv, cin, cout, splits, ms, 2.0 * 27 * cin * cout * batch * d ** 3 / (ms * 1e-3) / 1e12))
+    if k.tc_status() != 0:
+        raise RuntimeError("wgrad_layer_times: a tensor-core pipeline wait gave up")
     return out
 
 
@@ -670,7 +791,7 @@ def symmetry(mask, label, flip_x, flip_y, flip_z, swap_yz):
 
 
 def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None, lr_min=None, warmup=100, clip=3.0,
-          augment=False):
+          augment=False, proj_weight=0.0):
     """Adam on mini-batches of net.B samples drawn (seeded) from masks
     (device uint8 (N, D, H, W)) and labels (device FP32 (N, D, H, W, 3)),
     optional per-sample loss weights (device FP32 (N,)); with lr_min the
@@ -679,23 +800,28 @@ def train(net, masks, labels, iters, lr=1e-3, seed=0, log_every=0, sample_w=None
     are clipped to `clip` times their running norm (0: off): without these,
     some seeds of the 1e-3 rate fell into a plateau near loss 0.25 early on.
     With augment, every drawn sample goes through a random one of the 16
-    symmetries of the problem (cubic grids only).
+    symmetries of the problem (cubic grids only).  proj_weight > 0 adds the
+    squared projection of each sample's velocity error on its label
+    (slbc_nn_proj): the component of the error along the converged flow,
+    which the lattice removes slowest after a warm start.
     Returns the loss every log_every iterations (and the last)."""
     import torch
     rng = np.random.default_rng(seed)
     n = masks.shape[0]
     hist = []
+    lab_sq = labels[..., :3].double().pow(2).sum(dim=(1, 2, 3, 4)) if proj_weight > 0 else None
     for it in range(1, iters + 1):
         idx = torch.as_tensor(rng.choice(n, size=net.B, replace=n < net.B), device=masks.device)
         mb = masks.index_select(0, idx).contiguous()
         lab = labels.index_select(0, idx).contiguous()
         sw = sample_w.index_select(0, idx).contiguous() if sample_w is not None else None
+        proj = (proj_weight, lab_sq.index_select(0, idx).contiguous()) if lab_sq is not None else None
         if augment and mb.shape[1] == mb.shape[2] == mb.shape[3]:
             for b, bits in enumerate(rng.integers(0, 2, size=(net.B, 4))):
                 mb[b], lab[b] = symmetry(mb[b], lab[b], *bits)
         net.encode(mb)
         net.forward()
-        loss = net.loss_and_backward(lab, sw)
+        loss = net.loss_and_backward(lab, sw, proj)
         if clip:
             net.clip_grads(clip)
         rate = lr if lr_min is None else lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * (it - 1) / iters))

@@ -174,6 +174,42 @@ def test_training_lowers_the_loss(gpu):
     assert last < 0.7 * first, (first, last)
 
 
+def test_projection_loss_term(gpu):
+    """slbc_nn_proj: loss += (w / B) sum_n s_n^2 and grad += 2 w s_n
+    label_n / (q_n B) with s_n = <label_n, pred_n - label_n> / q_n, q_n =
+    <label_n, label_n> over the 3 velocity channels of 4-channel labels,
+    against float64 torch on the same data (BF16 gradient rounding)."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    k = WS.Kernels(gpu.dll)
+    B, D, H, W, ctot, lch, w = 3, 8, 8, 16, 32, 4, 7.5
+    g = torch.Generator(device="cuda").manual_seed(12)
+    lab = torch.randn(B, D, H, W, lch, device="cuda", generator=g)
+    pred = torch.zeros(B, D + 2, H + 2, W + 2, ctot, device="cuda")
+    pred[:, 1:-1, 1:-1, 1:-1, :lch] = lab * (1.0 + 0.05 * torch.arange(1, B + 1, device="cuda").view(B, 1, 1, 1, 1))
+    pred[:, 1:-1, 1:-1, 1:-1, :lch] += 0.1 * torch.randn(B, D, H, W, lch, device="cuda", generator=g)
+    base = 0.01 * torch.randn(B, D + 2, H + 2, W + 2, ctot, device="cuda", generator=g)
+    grad = base.to(torch.bfloat16)
+    q = lab[..., :3].double().pow(2).sum(dim=(1, 2, 3, 4))
+    dot = torch.zeros(B, device="cuda", dtype=torch.float64)
+    loss = torch.full((1,), 0.25, device="cuda", dtype=torch.float64)
+    st = torch.cuda.current_stream().cuda_stream
+    k.nn_proj(pred.data_ptr(), ctot, lab.data_ptr(), lch, 3, q.data_ptr(), B, D, H, W, w, grad.data_ptr(), ctot,
+              dot.data_ptr(), loss.data_ptr(), st)
+    torch.cuda.synchronize()
+    p = pred[:, 1:-1, 1:-1, 1:-1, :3].double()
+    s = ((p - lab[..., :3].double()) * lab[..., :3].double()).sum(dim=(1, 2, 3, 4)) / q
+    assert abs(float(loss) - (0.25 + w / B * float((s * s).sum()))) <= 1e-9 * (1.0 + float(loss))
+    want = base.to(torch.bfloat16).double()
+    want[:, 1:-1, 1:-1, 1:-1, :3] += (2.0 * w * s / (q * B)).view(B, 1, 1, 1, 1) * lab[..., :3].double()
+    got = grad.double()
+    # channels 3.. and the halo untouched; channels 0..2 within BF16 rounding
+    assert torch.equal(got[..., 3:], base.to(torch.bfloat16).double()[..., 3:])
+    assert torch.equal(got[:, 0], want[:, 0])
+    err = (got - want).abs().max().item()
+    assert err <= 2 ** -7 * want.abs().max().item(), err
+
+
 def test_gradient_clipping(gpu):
     """Device-side clipping against the running gradient norm: the first
     call sets the running norm, a 10x spike is scaled to 3x the running
