@@ -316,11 +316,6 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream);
-/* The same, added to dw when accumulate is set (batches taken a sample at a
- * time, so that the channel-major copies of one sample stay in L2). */
-int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
-                      int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats,
-                      int splits, float *dw, int accumulate, void *stream);
 /* K splits for slbc_tc_wgrad that fill the current device once (at most
  * k_tiles / 8 and max_splits; k_tiles = B * pstride / 64). */
 int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_splits);

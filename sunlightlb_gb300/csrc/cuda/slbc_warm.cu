@@ -898,11 +898,10 @@ k_wgrad_n(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtens
   if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)w.tmem_cols);
 }
 
-// dw[i] = sum over splits of partial[s][i], in split order (added to dw[i]
-// when accumulate is set)
-__global__ void k_sum_splits(const float *partial, long long n, int splits, float *dw, int accumulate) {
+// dw[i] = sum over splits of partial[s][i], in split order
+__global__ void k_sum_splits(const float *partial, long long n, int splits, float *dw) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    float v = accumulate ? dw[i] : 0.0f;
+    float v = 0.0f;
     for (int s = 0; s < splits; s++) v += partial[(long long)s * n + i];
     dw[i] = v;
   }
@@ -1143,13 +1142,6 @@ int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_spl
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream) {
-  return slbc_tc_wgrad_acc(dy0, dy1, dy2, xt, B, D, H, W, Wp, pstride, cin, cout, partial, partial_floats, splits, dw,
-                           0, stream);
-}
-
-int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
-                      int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats,
-                      int splits, float *dw, int accumulate, void *stream) {
   WgradArgs w;
   if (cout < 32 || (cout > 128 && cout % 128) || (cout <= 128 && 128 % cout) || cin < 16 || cin % 16)
     return slbc::set_error("slbc_tc_wgrad: cout must be 32, 64, 128 or a multiple of 128; cin a multiple of 16"), 1;
@@ -1185,7 +1177,7 @@ int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const v
     if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
     const long long n = 27LL * cout * cin;
     k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
-        partial, n, splits, dw, accumulate);
+        partial, n, splits, dw);
     slbc::count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
@@ -1223,7 +1215,7 @@ int slbc_tc_wgrad_acc(const void *dy0, const void *dy1, const void *dy2, const v
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
   const long long n = 27LL * cout * cin;
   k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
-      partial, n, splits, dw, accumulate);
+      partial, n, splits, dw);
   slbc::count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;

@@ -49,7 +49,6 @@ class Kernels:
             "slbc_tc_halo": [p] + [i] * 7 + [p],
             "slbc_tc_cmajor": [p] + [i] * 8 + [ll, i, i, p, p],
             "slbc_tc_wgrad": [p] * 4 + [i] * 5 + [ll, i, i, p, ll, i, p, p],
-            "slbc_tc_wgrad_acc": [p] * 4 + [i] * 5 + [ll, i, i, p, ll, i, p, i, p],
             "slbc_nn_pool": [p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_pool_bwd": [p, i, i, p, i, i, p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_up": [p, i, i, p, i, i] + [i] * 5 + [p],
@@ -246,12 +245,10 @@ class UNet:
             "gB3": (3, w3), "gA3": (3, w3), "gP3": (3, w2),
         }
         self.grad = {n: self._act(lv, c) for n, (lv, c) in self.grad_spec.items()}
-        # channel-major copies of one sample (the weight gradients take a
-        # batch a sample at a time, so the copies just written are still in L2)
         Wp, ps = flat_geometry(self.D, self.H, self.W)
         maxc = max(c for _, c in self.buf_spec.values())
-        self.cm_x = torch.empty(maxc * ps, device=self.dev, dtype=torch.bfloat16)
-        self.cm_g = [torch.empty(max(w0, w3) * ps, device=self.dev, dtype=torch.bfloat16) for _ in range(3)]
+        self.cm_x = torch.empty(maxc * self.B * ps, device=self.dev, dtype=torch.bfloat16)
+        self.cm_g = [torch.empty(w3 * self.B * ps, device=self.dev, dtype=torch.bfloat16) for _ in range(3)]
         self.ws_floats = 1 << 26
         self.ws = torch.empty(self.ws_floats, device=self.dev, dtype=torch.float32)
         self.loss_acc = torch.zeros(1, device=self.dev, dtype=torch.float64)
@@ -270,18 +267,16 @@ class UNet:
         Wp, ps = flat_geometry(d, h, w)
         g = self.grad[g_name]
         x = self.buf[x_name]
-        vol = (d + 2) * (h + 2) * (w + 2)
-        splits = k.tc_wgrad_splits(cin, cout, ps // 64, self.ws_floats // (27 * cout * cin))
+        for c, shift in zip(self.cm_g, (-1, 0, 1)):
+            k.tc_cmajor(g.data_ptr(), self.B, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0, c.data_ptr(),
+                        self.stream)
+        k.tc_cmajor(x.data_ptr(), self.B, d, h, w, x.shape[-1], x_coff, cin, Wp, ps, 0, 1, self.cm_x.data_ptr(),
+                    self.stream)
+        splits = k.tc_wgrad_splits(cin, cout, self.B * ps // 64, self.ws_floats // (27 * cout * cin))
         p = self.params[name]
-        for n in range(self.B):
-            gp = g.data_ptr() + 2 * n * vol * g.shape[-1]
-            xp = x.data_ptr() + 2 * n * vol * x.shape[-1]
-            for c, shift in zip(self.cm_g, (-1, 0, 1)):
-                k.tc_cmajor(gp, 1, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0, c.data_ptr(), self.stream)
-            k.tc_cmajor(xp, 1, d, h, w, x.shape[-1], x_coff, cin, Wp, ps, 0, 1, self.cm_x.data_ptr(), self.stream)
-            k.tc_wgrad_acc(self.cm_g[0].data_ptr(), self.cm_g[1].data_ptr(), self.cm_g[2].data_ptr(),
-                           self.cm_x.data_ptr(), 1, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats,
-                           splits, p["gw"].data_ptr(), int(n > 0), self.stream)
+        k.tc_wgrad(self.cm_g[0].data_ptr(), self.cm_g[1].data_ptr(), self.cm_g[2].data_ptr(), self.cm_x.data_ptr(),
+                   self.B, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats, splits,
+                   p["gw"].data_ptr(), self.stream)
         p["gb"].zero_()
         k.nn_bias_grad(g.data_ptr(), g.shape[-1], 0, self.B, d, h, w, cout, p["gb"].data_ptr(), self.stream)
 
@@ -690,14 +685,12 @@ def conv_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
     return out
 
 
-def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20, per_sample=False):
-    """Weight-gradient time of every layer shape of the network on `batch`
-    grids of side^3, CUDA events over `reps` calls on random BF16 data:
-    [(level, cin, cout, splits, ms, TFLOP/s)], FLOPs 2 * 27 * cin * cout *
-    interior voxels.  Default: slbc_tc_wgrad alone (the split sum included)
-    on ready channel-major copies of the whole batch.  per_sample: the
-    training step's path, per sample the four channel-major copies from
-    channels-last buffers and slbc_tc_wgrad_acc on them."""
+def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
+    """Weight-gradient time (slbc_tc_wgrad alone, from ready channel-major
+    copies; the split sum included) of every layer shape of the network on
+    `batch` grids of side^3, CUDA events over `reps` calls on random BF16
+    data: [(level, cin, cout, splits, ms, TFLOP/s)], FLOPs 2 * 27 * cin *
+    cout * interior voxels."""
     import torch
     k = Kernels(lib.dll)
     dev = torch.device("cuda")
@@ -711,36 +704,18 @@ def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20, per_
     for lv, cin, cout in shapes:
         d = side >> lv
         Wp, ps = flat_geometry(d, d, d)
-        nb = 1 if per_sample else batch
-        xt = torch.randn(cin, nb * ps, device=dev).to(torch.bfloat16)
-        dys = [torch.randn(cout, nb * ps, device=dev).to(torch.bfloat16) for _ in range(3)]
+        xt = torch.randn(cin, batch * ps, device=dev).to(torch.bfloat16)
+        dys = [torch.randn(cout, batch * ps, device=dev).to(torch.bfloat16) for _ in range(3)]
         dw = torch.empty(27 * cout * cin, device=dev, dtype=torch.float32)
-        splits = k.tc_wgrad_splits(cin, cout, nb * ps // 64, ws_floats // (27 * cout * cin))
-        if per_sample:
-            x = torch.randn(batch, d + 2, d + 2, d + 2, cin, device=dev).to(torch.bfloat16)
-            g = torch.randn(batch, d + 2, d + 2, d + 2, cout, device=dev).to(torch.bfloat16)
-            vol = (d + 2) ** 3
-
-            def run():
-                for n in range(batch):
-                    for c, shift in zip(dys, (-1, 0, 1)):
-                        k.tc_cmajor(g.data_ptr() + 2 * n * vol * cout, 1, d, d, d, cout, 0, cout, Wp, ps, shift, 0,
-                                    c.data_ptr(), stream)
-                    k.tc_cmajor(x.data_ptr() + 2 * n * vol * cin, 1, d, d, d, cin, 0, cin, Wp, ps, 0, 1,
-                                xt.data_ptr(), stream)
-                    k.tc_wgrad_acc(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), 1, d, d,
-                                   d, Wp, ps, cin, cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), int(n > 0),
-                                   stream)
-        else:
-            def run():
-                k.tc_wgrad(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), batch, d, d, d,
-                           Wp, ps, cin, cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), stream)
+        splits = k.tc_wgrad_splits(cin, cout, batch * ps // 64, ws_floats // (27 * cout * cin))
+        args = (dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), batch, d, d, d, Wp, ps, cin,
+                cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), stream)
         for _ in range(3):
-            run()
+            k.tc_wgrad(*args)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            run()
+            k.tc_wgrad(*args)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps

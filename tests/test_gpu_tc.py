@@ -195,50 +195,3 @@ def test_wgrad_matches_torch(gpu, case):
     ref = ref.permute(2, 3, 4, 0, 1).reshape(27, cout, cin)
     assert (dw - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
 
-
-def test_wgrad_per_sample_accumulates(gpu):
-    """slbc_tc_wgrad_acc a sample at a time (one-sample channel-major copies,
-    accumulate after the first) equals the whole-batch weight gradient up to
-    the FP32 summation order."""
-    torch = pytest.importorskip("torch")
-    _, halo = conv_fns(gpu)
-    cm, wg = wgrad_fns(gpu)
-    acc = gpu.dll.slbc_tc_wgrad_acc
-    acc.restype = C.c_int
-    acc.argtypes = [C.c_void_p] * 4 + [C.c_int] * 5 + [C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
-                                                      C.c_int, C.c_void_p, C.c_int, C.c_void_p]
-    B, D, H, W, cin, cout, splits = 3, 8, 8, 16, 96, 32, 6
-    g = torch.Generator(device="cuda").manual_seed(21)
-    x = torch.randn(B, cin, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
-    dy = torch.randn(B, cout, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
-    st = torch.cuda.current_stream().cuda_stream
-    xb = to_padded(torch, x, cin, 0)
-    yb = to_padded(torch, dy, cout, 0)
-    assert halo(xb.data_ptr(), B, D, H, W, cin, 0, cin, st) == 0
-    assert halo(yb.data_ptr(), B, D, H, W, cout, 0, cout, st) == 0
-    Wp, pstride = flat_geometry(D, H, W)
-    partial = torch.empty(splits * 27 * cout * cin, device="cuda")
-
-    def copies(n_samples, x_ptr, y_ptr):
-        xt = torch.empty(cin, n_samples * pstride, device="cuda", dtype=torch.bfloat16)
-        assert cm(x_ptr, n_samples, D, H, W, cin, 0, cin, Wp, pstride, 0, 1, xt.data_ptr(), st) == 0
-        dys = []
-        for shift in (-1, 0, 1):
-            t = torch.empty(cout, n_samples * pstride, device="cuda", dtype=torch.bfloat16)
-            assert cm(y_ptr, n_samples, D, H, W, cout, 0, cout, Wp, pstride, shift, 0, t.data_ptr(), st) == 0
-            dys.append(t)
-        return xt, dys
-
-    xt, dys = copies(B, xb.data_ptr(), yb.data_ptr())
-    whole = torch.empty(27, cout, cin, device="cuda")
-    assert wg(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), B, D, H, W, Wp, pstride, cin,
-              cout, partial.data_ptr(), partial.numel(), splits, whole.data_ptr(), st) == 0
-    per = torch.full((27, cout, cin), 5.0, device="cuda")  # overwritten by the first call
-    vol = (D + 2) * (H + 2) * (W + 2)
-    for n in range(B):
-        xt1, dys1 = copies(1, xb.data_ptr() + 2 * n * vol * cin, yb.data_ptr() + 2 * n * vol * cout)
-        rc = acc(dys1[0].data_ptr(), dys1[1].data_ptr(), dys1[2].data_ptr(), xt1.data_ptr(), 1, D, H, W, Wp, pstride,
-                 cin, cout, partial.data_ptr(), partial.numel(), splits, per.data_ptr(), int(n > 0), st)
-        assert rc == 0, gpu.dll.slbc_last_error
-    assert gpu.dll.slbc_tc_status() == 0
-    assert (per - whole).abs().max().item() <= 1e-5 * whole.abs().max().item()
