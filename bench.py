@@ -947,7 +947,6 @@ def batch_leg(torch, L, args):
 
 # ---- learned warm start ------------------------------------------------------
 
-WARM_SEED, WARM_FORCE = 3, 1e-6
 
 
 def run_warmstart(args):
@@ -964,13 +963,13 @@ def run_warmstart(args):
         return
     torch.cuda.set_device(local)
     L = sunlightlb_gb300.library()
-    side, ev_side, force = args.warm_side, args.eval_side, WARM_FORCE
+    side, ev_side, force = args.warm_side, args.eval_side, WS.PACKING_FORCE
     # held-out packings: the ones after the training set, or from --eval-offset
     # (to evaluate networks trained on different sets on the same packings)
     ev_off = args.train if args.eval_offset is None else args.eval_offset
     if ev_off < args.train:
         raise SystemExit("--eval-offset must not reach into the training packings")
-    specs = WS.packing_specs(ev_off + args.eval, WARM_SEED)
+    specs = WS.packing_specs(ev_off + args.eval, WS.PACKING_SEED)
     tr_specs, ev_specs = specs[:args.train], specs[ev_off:ev_off + args.eval]
     train_now = args.epochs > 0 or not args.init_weights
     t0 = time.perf_counter()
@@ -1057,14 +1056,22 @@ def run_warmstart(args):
             row[f"check50_correct{n}"] = {"warm_steps": hs[0] if hs else None,
                                           "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
         for name in variants:
+            t_extra = 0.0
             if name == "velocity_only":
                 vs, ds = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0), None
+            elif name == "plane_flux":  # the default state with uniform plane fluxes (timed with inference)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1)
+                row["plane_flux_spread"] = WS.uniform_plane_flux(vs, ds, sdev, force)
+                torch.cuda.synchronize()
+                t_extra = max(0.0, time.perf_counter() - t0 - t_inf)
             else:
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0)
             hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=vs, warm_drho=ds, check=50),
                                  k_conv, 1e-4)
             row[f"check50_{name}"] = {"warm_steps": hs[0] if hs else None,
-                                      "warm_wall_s": round(hs[1] + t_inf, 4) if hs else None}
+                                      "warm_wall_s": round(hs[1] + t_inf + t_extra, 4) if hs else None}
         rows.append(row)
 
     def summary(check):
@@ -1117,7 +1124,7 @@ def run_warmstart(args):
     if args.save_weights:
         WS.save_weights(net, args.save_weights,
                         meta={"train_samples": args.train, "train_side": side, "epochs": args.epochs,
-                              "iterations": iters, "seed": WARM_SEED, "label_tol": args.label_tol,
+                              "iterations": iters, "seed": WS.PACKING_SEED, "label_tol": args.label_tol,
                               "final_loss": hist[-1] if hist else None, "lr": args.lr,
                               "proj_weight": args.proj_weight,
                               "fine_tuned_from": init_meta})
@@ -1129,38 +1136,18 @@ def warm_leg(torch, L, args):
     --save-weights on the GPU) against the plain start on the first
     `--leg-warm-eval` held-out 128^3 packings of the warmstart workload;
     steps and wall time to permeability within 1e-4 of the plain converged
-    value, checks every 50 steps in both arms, inference timed."""
+    value, checks every 50 steps in both arms, inference timed
+    (warmstart.held_out_comparison)."""
     import numpy as np
     from sunlightlb_gb300 import warmstart as WS
     if not os.path.exists(WS.WEIGHTS):
         return {"skipped": "no trained weights in sunlightlb_gb300/data/warm_unet.npz"}
-    params, widths, features, meta = WS.load_weights()
-    force, side = WARM_FORCE, args.eval_side
-    ntrain = int(meta.get("train_samples", args.train))
-    specs = WS.packing_specs(ntrain + args.eval, WARM_SEED)[ntrain:ntrain + args.leg_warm_eval]
-    inf = WS.UNet(L, side, side, side, batch=1, widths=widths, params=params, features=features)
-    rows = []
-    for phi, sd in specs:
-        solid = WS.packing(side, phi, sd)
-        traj = WS.permeability_run(L, solid, force)
-        k_conv = traj[-1][1]
-        sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
-        plain = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, check=50), k_conv, 1e-4)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        u, drho = WS.predict_state(inf, sdev, force, WS.ETA_TAU1)
-        torch.cuda.synchronize()
-        t_inf = time.perf_counter() - t0
-        warm = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=u, warm_drho=drho,
-                                                   check=50), k_conv, 1e-4)
-        rows.append({"phi": round(phi, 4), "k": k_conv, "plain_steps": plain[0] if plain else None,
-                     "plain_wall_s": round(plain[1], 4) if plain else None,
-                     "warm_steps": warm[0] if warm else None,
-                     "warm_wall_s": round(warm[1] + t_inf, 4) if warm else None, "inference_s": round(t_inf, 4)})
+    rows, meta = WS.held_out_comparison(L, args.leg_warm_eval, side=args.eval_side, check=50)
+    _, widths, _, _ = WS.load_weights()
     ok = [r for r in rows if r["plain_wall_s"] and r["warm_wall_s"]]
     tot_p = sum(r["plain_wall_s"] for r in ok)
     tot_w = sum(r["warm_wall_s"] for r in ok)
-    return {"workload": f"learned warm start, {len(rows)} held-out {side}^3 packings",
+    return {"workload": f"learned warm start, {len(rows)} held-out {args.eval_side}^3 packings",
             "network": {"widths": list(widths), "trained": meta},
             "criterion": "permeability within 1e-4 of the plain converged value, checks every 50 steps",
             "samples": len(ok), "plain_wall_total_s": round(tot_p, 3), "warm_wall_total_s": round(tot_w, 3),

@@ -240,13 +240,19 @@ __device__ __forceinline__ void load_pops(const T *__restrict__ P, long long S, 
   }
 }
 
-// Wall terms, collision and the write-back of node x (the slots load_pops
-// read: locally reversed for the even step, pushed to the neighbours, or to
-// the node's own opposite slot across a bounce-back link, for the odd one).
-template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, bool I32 = false>
-__device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb, int x, uint16_t fl,
-                                            T (&t)[15]) {
-  T *__restrict__ P = a.p.pop;
+// Element offsets of the pull-and-push update for nodes away from the
+// lattice's faces (no periodic wrap): population q arrives from element
+// x + pull_nbr[q] (slot opp(q) of x - c_q) or, over a bounce-back link, from
+// x + pull_self[q] (slot q of x); it leaves to x + push_nbr[q] (slot q of
+// x + c_q) or x + push_self[q] (slot opp(q) of x).  Unsigned 32-bit: only
+// used when 15 x npad elements fit (I32).
+struct OddOffsets {
+  unsigned pull_self[15], pull_nbr[15], push_self[15], push_nbr[15];
+};
+
+// Wall terms and collision of node x.
+template <typename T, bool EXACT, bool MOVING, bool BFU>
+__device__ __forceinline__ void relax_node(const StepArgs<T> &a, const Nbr &nb, int x, uint16_t fl, T (&t)[15]) {
   const long long S = a.p.npad;
   const bool solid = (fl & FLAG_SOLID) != 0;
   if (MOVING && (fl & FLAG_LINKS)) apply_wall<T>(t, fl, solid, nb, x, a.uw, S);
@@ -255,6 +261,35 @@ __device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb,
     if (!BFU) { bx = a.bf[x]; by = a.bf[S + x]; bz = a.bf[2 * S + x]; }
     collide<T, EXACT>(t, a.omega, a.comega, a.rho0, a.stokes, !solid, bx, by, bz);
   }
+}
+
+// The pull and push of a node away from the faces through OddOffsets: one
+// select between two uniform offsets per access, no neighbour indexing.
+template <typename T>
+__device__ __forceinline__ void load_pops_inner(const T *__restrict__ P, const OddOffsets &o, int x, uint16_t fl,
+                                                T (&t)[15]) {
+  t[0] = P[x];
+#pragma unroll
+  for (int q = 1; q < 15; q++) t[q] = P[(unsigned)x + (((fl >> q) & 1) ? o.pull_self[q] : o.pull_nbr[q])];
+}
+
+template <typename T>
+__device__ __forceinline__ void store_pops_inner(T *__restrict__ P, const OddOffsets &o, int x, uint16_t fl,
+                                                 const T (&t)[15]) {
+  P[x] = t[0];
+#pragma unroll
+  for (int q = 1; q < 15; q++) P[(unsigned)x + (((fl >> OPP(q)) & 1) ? o.push_self[q] : o.push_nbr[q])] = t[q];
+}
+
+// Wall terms, collision and the write-back of node x (the slots load_pops
+// read: locally reversed for the even step, pushed to the neighbours, or to
+// the node's own opposite slot across a bounce-back link, for the odd one).
+template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, bool I32 = false>
+__device__ __forceinline__ void finish_node(const StepArgs<T> &a, const Nbr &nb, int x, uint16_t fl,
+                                            T (&t)[15]) {
+  T *__restrict__ P = a.p.pop;
+  const long long S = a.p.npad;
+  relax_node<T, EXACT, MOVING, BFU>(a, nb, x, fl, t);
   if (!ODD) {
 #pragma unroll
     for (int q = 0; q < 15; q++) P[pop_index<I32>(OPP(q), S, x)] = t[q];
@@ -293,23 +328,33 @@ __device__ __forceinline__ void step_node(const StepArgs<T> &a, int i, int j, in
 // thread and removes the flag-then-populations round trip of the odd step
 // from every row but the first.
 // Grid: (ceil(esk/blockDim.x), ceil(esj/NPT), esi).  I32: 15 x npad
-// elements fit 32 unsigned bits (pop_index).
+// elements fit 32 unsigned bits (pop_index); then, in the pull-and-push
+// update, a row whose nodes in the whole warp lie away from the lattice's
+// faces takes the OddOffsets addressing (a warp-uniform choice, so no warp
+// runs both forms).
 template <typename T, bool ODD, bool EXACT, bool MOVING, bool BFU, int NPT, bool I32 = false>
-__global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
+__global__ void __launch_bounds__(256) k_step(StepArgs<T> a, OddOffsets off) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.z;
   if (k >= a.p.esk) return;
   const int j0 = blockIdx.y * NPT;
   const int nrow = min(NPT, a.p.esj - j0);
-  const T *P = a.p.pop;
+  T *P = a.p.pop;
   const long long S = a.p.npad;
   uint16_t fl[NPT];
+  bool inner[NPT];
+  const unsigned warp_mask = __activemask();
+  const bool ik_inner = i > 0 && i < a.p.esi - 1 && k > 0 && k < a.p.esk - 1;
 #pragma unroll
-  for (int r = 0; r < NPT; r++)
+  for (int r = 0; r < NPT; r++) {
     if (r < nrow) fl[r] = __ldg(a.p.flags + ((i * a.p.esj + j0 + r) * a.p.esk + k));
+    const int j = j0 + r;
+    inner[r] = ODD && I32 && __all_sync(warp_mask, ik_inner && j > 0 && j < a.p.esj - 1);
+  }
   Nbr nb = make_nbr(i, j0, k, a.p.esi, a.p.esj, a.p.esk);
   T cur[15];
-  load_pops<T, ODD, I32>(P, S, nb, nb.at(0, 0, 0), fl[0], cur);
+  if (inner[0]) load_pops_inner<T>(P, off, nb.at(0, 0, 0), fl[0], cur);
+  else load_pops<T, ODD, I32>(P, S, nb, nb.at(0, 0, 0), fl[0], cur);
 #pragma unroll
   for (int r = 0; r < NPT; r++) {
     if (r >= nrow) break;
@@ -318,9 +363,16 @@ __global__ void __launch_bounds__(256) k_step(StepArgs<T> a) {
     const bool more = r + 1 < nrow;
     if (more) {
       nbn = make_nbr(i, j0 + r + 1, k, a.p.esi, a.p.esj, a.p.esk);
-      load_pops<T, ODD, I32>(P, S, nbn, nbn.at(0, 0, 0), fl[r + 1 < NPT ? r + 1 : r], nxt);
+      const int rn = r + 1 < NPT ? r + 1 : r;
+      if (inner[rn]) load_pops_inner<T>(P, off, nbn.at(0, 0, 0), fl[rn], nxt);
+      else load_pops<T, ODD, I32>(P, S, nbn, nbn.at(0, 0, 0), fl[rn], nxt);
     }
-    finish_node<T, ODD, EXACT, MOVING, BFU, I32>(a, nb, nb.at(0, 0, 0), fl[r], cur);
+    if (inner[r]) {
+      relax_node<T, EXACT, MOVING, BFU>(a, nb, nb.at(0, 0, 0), fl[r], cur);
+      store_pops_inner<T>(P, off, nb.at(0, 0, 0), fl[r], cur);
+    } else {
+      finish_node<T, ODD, EXACT, MOVING, BFU, I32>(a, nb, nb.at(0, 0, 0), fl[r], cur);
+    }
     if (more) {
 #pragma unroll
       for (int q = 0; q < 15; q++) cur[q] = nxt[q];

@@ -53,6 +53,21 @@ static dim3 row_grid(const Lattice &L, int bx) {
 
 static int flat_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// Element offsets of the pull-and-push update away from the faces (k_step):
+// the neighbour x + c_q is x + c_q . (esj esk, esk, 1) there.
+static OddOffsets odd_offsets(const Lattice &L) {
+  OddOffsets o;
+  const unsigned S = (unsigned)L.npad;
+  for (int q = 0; q < 15; q++) {
+    const int d = CX(q) * L.esj * L.esk + CY(q) * L.esk + CZ(q);
+    o.pull_self[q] = (unsigned)q * S;
+    o.pull_nbr[q] = (unsigned)OPP(q) * S - (unsigned)d;
+    o.push_self[q] = (unsigned)OPP(q) * S;
+    o.push_nbr[q] = (unsigned)q * S + (unsigned)d;
+  }
+  return o;
+}
+
 template <bool ODD, bool MOVING, bool BFU>
 static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
   if (npt == kStepVec4) {  // 128-bit form: 4 nodes along k per thread, bx threads per block
@@ -71,13 +86,15 @@ static void step_variant(Lattice &L, const StepArgs<T_> &a, int npt, int bx) {
   // 32-bit population indices whenever all 15 arrays fit (lattices up to
   // about 286 M nodes)
   if (15LL * L.npad <= 0xFFFFFFFFLL) {
-    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, true><<<grid, bx, 0, L.stream>>>(a);
-    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, true><<<grid, bx, 0, L.stream>>>(a);
-    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, true><<<grid, bx, 0, L.stream>>>(a);
+    const OddOffsets off = odd_offsets(L);
+    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, true><<<grid, bx, 0, L.stream>>>(a, off);
+    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, true><<<grid, bx, 0, L.stream>>>(a, off);
+    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, true><<<grid, bx, 0, L.stream>>>(a, off);
   } else {
-    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, false><<<grid, bx, 0, L.stream>>>(a);
-    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, false><<<grid, bx, 0, L.stream>>>(a);
-    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, false><<<grid, bx, 0, L.stream>>>(a);
+    const OddOffsets off{};
+    if (npt == 4) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 4, false><<<grid, bx, 0, L.stream>>>(a, off);
+    else if (npt == 2) k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 2, false><<<grid, bx, 0, L.stream>>>(a, off);
+    else k_step<T_, ODD, SLBC_EXACT, MOVING, BFU, 1, false><<<grid, bx, 0, L.stream>>>(a, off);
   }
 }
 

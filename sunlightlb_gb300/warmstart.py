@@ -557,6 +557,38 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5):
     return u, drho
 
 
+def uniform_plane_flux(u, drho, solid_u8, force):
+    """Make the x flux of a predicted state the same through every x plane,
+    as mass conservation requires of the converged flow (the mass flux
+    through any plane normal to x is the same in a periodic steady state).
+    A network that sees only part of the bed predicts each slab as if the
+    whole body force drove it, Q(i) = c(i) F; slabs in series carry the
+    harmonic mean Q_h = n / sum 1/Q(i), with the pressure taking up the
+    difference, dp/dx = F (1 - Q_h / Q(i)).  So every plane's velocity is
+    scaled by Q_h / Q(i) and its fluid nodes' density deviation gets 3 p(i)
+    (p = rho / 3), p accumulated over the planes (midpoint rule, zero mean).
+    u: (3 x N) device FP32 in lbsetveldev layout (x = the slowest index),
+    drho: (N) or None; both changed in place.  Returns the relative spread
+    (max - min) / mean of the plane fluxes before."""
+    import torch
+    D, H, W = solid_u8.shape
+    ux = u[:D * H * W].view(D, H, W)
+    q = ux.double().sum(dim=(1, 2))
+    if not bool((q > 0).all()):
+        return None
+    qh = D / (1.0 / q).sum()
+    spread = float((q.max() - q.min()) / q.mean())
+    scale = (qh / q).float()
+    u.view(3, D, H, W).mul_(scale.view(1, D, 1, 1))
+    if drho is not None:
+        g = force * (1.0 - qh / q)
+        p = torch.cumsum(g, 0) - 0.5 * g
+        p -= p.mean()
+        fluid = (solid_u8 == 0).float()
+        drho.view(D, H, W).add_((3.0 * p).float().view(D, 1, 1) * fluid)
+    return spread
+
+
 def set_warm(L, lb, warm_u, warm_drho, scale=1.0):
     """Warm state through lbsetstatedev (velocity and density deviation) or
     lbsetveldev (velocity only), both fields multiplied by `scale`."""
@@ -723,6 +755,43 @@ def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
     if k.tc_status() != 0:
         raise RuntimeError("wgrad_layer_times: a tensor-core pipeline wait gave up")
     return out
+
+
+PACKING_SEED, PACKING_FORCE = 3, 1e-6  # the packings and body force the committed network was trained on
+
+
+def held_out_comparison(L, count, side=128, check=50, rel=1e-4, weights=WEIGHTS):
+    """The saved network (weights) against the plain start on the first
+    `count` held-out side^3 packings of its training distribution (those
+    after its training set, seed PACKING_SEED): per packing the steps and
+    wall time to permeability within `rel` of the plain converged value,
+    checks every `check` steps in both arms, inference timed in the warm
+    arm.  Returns (rows, meta) with rows of dicts."""
+    import torch
+    params, widths, features, meta = load_weights(weights)
+    ntrain = int(meta.get("train_samples", 0))
+    specs = packing_specs(ntrain + count, PACKING_SEED)[ntrain:ntrain + count]
+    inf = UNet(L, side, side, side, batch=1, widths=widths, params=params, features=features)
+    rows = []
+    for phi, sd in specs:
+        solid = packing(side, phi, sd)
+        traj = permeability_run(L, solid, PACKING_FORCE)
+        k_conv = traj[-1][1]
+        sdev = torch.as_tensor(solid.astype(np.uint8), device="cuda")
+        plain = first_within(permeability_run(L, solid, PACKING_FORCE, k_ref=k_conv, check=check, rel=rel), k_conv,
+                             rel)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u, drho = predict_state(inf, sdev, PACKING_FORCE, ETA_TAU1)
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t0
+        warm = first_within(permeability_run(L, solid, PACKING_FORCE, k_ref=k_conv, warm_u=u, warm_drho=drho,
+                                             check=check, rel=rel), k_conv, rel)
+        rows.append({"phi": round(phi, 4), "k": k_conv, "plain_steps": plain[0] if plain else None,
+                     "plain_wall_s": round(plain[1], 4) if plain else None,
+                     "warm_steps": warm[0] if warm else None,
+                     "warm_wall_s": round(warm[1] + t_inf, 4) if warm else None, "inference_s": round(t_inf, 4)})
+    return rows, meta
 
 
 def first_within(traj, k_ref, rel):

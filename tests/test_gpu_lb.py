@@ -36,6 +36,10 @@ CASES = {
     "thin_xy": dict(dims=(1, 2, 13), moving=1),
     "small": dict(dims=(3, 3, 3), steps=7),
     "ragged": dict(dims=(7, 13, 33), steps=12),
+    # rows long enough for whole warps away from the lattice's faces (the
+    # offset-table addressing of the pull-and-push update)
+    "long_rows": dict(dims=(5, 7, 100), steps=9),
+    "long_rows_moving_ns": dict(dims=(4, 6, 160), moving=1, stokes=0, tau=0.7, steps=10),
 }
 
 
