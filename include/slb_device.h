@@ -376,6 +376,18 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
                    void *stream);
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,
                    float shift_x, float *u, float drho_scale, float *drho, void *stream);
+/* Uniform plane flux of a decoded state (u: 3 x D*H*W FP32, x = the slowest
+ * index; drho: D*H*W or null; solid: D*H*W bytes): the x flux q[i] through
+ * every x plane becomes the harmonic mean qh of the planes' fluxes (u of
+ * plane i times qh / q[i]), and the fluid nodes of plane i get the density
+ * deviation 3 p[i], p the pressure that carries the body force `force`
+ * through slabs in series (dp/dx = force (1 - qh / q[i]), zero mean).  A
+ * converged periodic flow has the same mass flux through every plane.
+ * work: 3 D + 1 device doubles (q, scale, p, then the relative spread
+ * (max - min) / mean of the fluxes before, -1 when some flux is <= 0 and
+ * nothing was changed). */
+int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D, int H, int W, float force,
+                       double *work, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

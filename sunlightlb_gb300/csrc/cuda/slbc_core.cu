@@ -13,6 +13,7 @@
 #include <atomic>
 #include <algorithm>
 #include <cmath>
+#include <thread>
 
 #include "slbc_internal.cuh"
 #include "slbc_kernels.cuh"
@@ -729,6 +730,22 @@ int reduction_blocks(const Lattice &L) {
 }  // namespace slbc
 
 // ============================================================================
+// Host loop over [0, n) in contiguous ranges on up to 32 threads (one per
+// core), fn(lo, hi) per range; inline below two ranges of `grain`.
+template <typename F>
+static void host_par_for(long long n, long long grain, F fn) {
+  long long t = std::min<long long>(std::max(1u, std::thread::hardware_concurrency()), 32);
+  t = std::min(t, grain > 0 ? n / grain : t);
+  if (t <= 1) {
+    fn(0LL, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (long long i = 1; i < t; i++) th.emplace_back(fn, n * i / t, n * (i + 1) / t);
+  fn(0LL, n / t);
+  for (auto &x : th) x.join();
+}
+
 extern "C" {
 
 const char *slbc_last_error(void) { return g_err.c_str(); }
@@ -846,7 +863,10 @@ int slbc_set_tuning(slbc_lattice *h, const int cfg[4]) {
 static int geometry_flags(Lattice &L, slbc_lattice *h, const int *objidx) {
   L.ads_version++;  // the boundary links change
   const long long n = L.nnodes;
-  for (long long x = 0; x < n; x++) h->solid_host[x] = objidx[x] >= 0;
+  unsigned char *solid = h->solid_host.data();
+  host_par_for(n, 1LL << 20, [&](long long lo, long long hi) {
+    for (long long x = lo; x < hi; x++) solid[x] = objidx[x] >= 0;
+  });
   CK(cudaMemcpyAsync(L.objidx, objidx, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, L.stream));
   const int bx = L.esk >= 128 ? 128 : 32;
   dim3 grid((L.esk + bx - 1) / bx, L.esj, L.esi);
@@ -869,7 +889,9 @@ static int geometry_boundary(Lattice &L, int nobj, const long *bnd_node, const i
   L.nbnd = nbnd; L.nobj = nobj; L.npiece = 0;
   if (nbnd > 0) {
     std::vector<int> nodes((size_t)nbnd);
-    for (long e = 0; e < nbnd; e++) nodes[e] = (int)bnd_node[e];
+    host_par_for(nbnd, 1LL << 20, [&](long long lo, long long hi) {
+      for (long long e = lo; e < hi; e++) nodes[e] = (int)bnd_node[e];
+    });
     CK(cudaMalloc(&L.bnd_node, nbnd * sizeof(int)));
     CK(cudaMalloc(&L.bnd_obj, nbnd * sizeof(int)));
     CK(cudaMalloc(&L.bnd_f, 3 * nbnd * sizeof(double)));
@@ -963,19 +985,42 @@ static int boundary_from_flags(Lattice &L, const int *objidx, int nobj, long **b
   cudaFree(counts);
   if (list) cudaFree(list);
   if (e != cudaSuccess) return fail("slbc_set_geometry_auto", e);
-  // grouped by object, node order kept (a counting sort over the list)
+  // grouped by object, node order kept: a stable counting sort over the
+  // list, in parallel ranges (per-range counts, offsets in (object, range)
+  // order, each range scattered in its own order)
   long *bn = (long *)malloc((size_t)(total > 0 ? total : 1) * sizeof(long));
   int *bo = (int *)malloc((size_t)(total > 0 ? total : 1) * sizeof(int));
   if (!bn || !bo) { free(bn); free(bo); return fail_msg("slbc_set_geometry_auto: no host memory"); }
-  std::vector<long> start((size_t)nobj + 1, 0);
-  for (long t = 0; t < total; t++) start[(size_t)objidx[nodes[t]] + 1]++;
-  for (int o = 0; o < nobj; o++) start[(size_t)o + 1] += start[o];
-  for (long t = 0; t < total; t++) {
-    const int o = objidx[nodes[t]];
-    const long slot = start[o]++;
-    bn[slot] = nodes[t];
-    bo[slot] = o;
-  }
+  const long long grain = 1LL << 18;
+  const int ranges = (int)std::max<long long>(1, std::min<long long>(
+      std::min<long long>(std::max(1u, std::thread::hardware_concurrency()), 32), total / grain));
+  std::vector<long> start((size_t)ranges * nobj, 0);
+  auto range_lo = [&](int r) { return total * r / ranges; };
+  host_par_for(ranges, 1, [&](long long r0, long long r1) {
+    for (long long r = r0; r < r1; r++) {
+      long *cnt = start.data() + (size_t)r * nobj;
+      for (long t = range_lo((int)r); t < range_lo((int)r + 1); t++) cnt[objidx[nodes[t]]]++;
+    }
+  });
+  long run = 0;
+  for (int o = 0; o < nobj; o++)
+    for (int r = 0; r < ranges; r++) {
+      long &c = start[(size_t)r * nobj + o];
+      const long v = c;
+      c = run;
+      run += v;
+    }
+  host_par_for(ranges, 1, [&](long long r0, long long r1) {
+    for (long long r = r0; r < r1; r++) {
+      long *at = start.data() + (size_t)r * nobj;
+      for (long t = range_lo((int)r); t < range_lo((int)r + 1); t++) {
+        const int o = objidx[nodes[t]];
+        const long slot = at[o]++;
+        bn[slot] = nodes[t];
+        bo[slot] = o;
+      }
+    }
+  });
   if (geometry_boundary(L, nobj, bn, bo, total)) { free(bn); free(bo); return 1; }
   *bnd_node_out = bn; *bnd_obj_out = bo; *nbnd_out = total;
   return 0;
@@ -1076,13 +1121,28 @@ int slbc_set_params(slbc_lattice *h, const slbc_params *p) {
 int slbc_set_bodyforce(slbc_lattice *h, const double *bx, const double *by, const double *bz) {
   Lattice &L = h->L;
   const long long n = L.nnodes;
-  bool uniform = true, found = false;
+  bool uniform = true;
   double c[3] = {0.0, 0.0, 0.0};
   if (bx && by && bz) {
-    for (long long x = 0; x < n && uniform; x++) {
-      if (h->solid_host[x]) continue;
-      if (!found) { c[0] = bx[x]; c[1] = by[x]; c[2] = bz[x]; found = true; }
-      else if (bx[x] != c[0] || by[x] != c[1] || bz[x] != c[2]) uniform = false;
+    // the first fluid node's force, then every fluid node against it (in
+    // parallel ranges)
+    const unsigned char *solid = h->solid_host.data();
+    long long first = 0;
+    while (first < n && solid[first]) first++;
+    if (first < n) {
+      c[0] = bx[first]; c[1] = by[first]; c[2] = bz[first];
+      std::atomic<bool> same(true);
+      host_par_for(n - first, 1LL << 20, [&](long long lo, long long hi) {
+        for (long long x = first + lo; x < first + hi; x++) {
+          if (solid[x]) continue;
+          if (bx[x] != c[0] || by[x] != c[1] || bz[x] != c[2]) {
+            same.store(false, std::memory_order_relaxed);
+            return;
+          }
+          if (((x - first) & 0xFFFF) == 0 && !same.load(std::memory_order_relaxed)) return;
+        }
+      });
+      uniform = same.load();
     }
   }
   if (L.bf) { cudaStreamSynchronize(L.stream); cudaFree(L.bf); L.bf = nullptr; }
@@ -1128,9 +1188,29 @@ int slbc_set_wallvel(slbc_lattice *h, const double *ux, const double *uy, const 
   return 0;
 }
 
+// Device address of a page-locked host array the device can reach (so a
+// kernel reads or writes it over the host link), else null: pageable
+// memory goes through the staging buffer.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int slbc_put_pops(slbc_lattice *h, const double *a) {
   Lattice &L = h->L;
   L.state_version++;
+  if (L.precision != 2) {
+    if (const double *dev_a = (const double *)mapped_host(a)) {
+      CK(DISPATCH(L, launch_put_host, L, dev_a));
+      CK(cudaStreamSynchronize(L.stream));
+      L.layout = SLBC_LAYOUT_N;
+      return 0;
+    }
+  }
   if (ensure_staging(L, L.nnodes, 15)) return 1;
   if (L.precision == 2) {  // count of unpaired nodes
     if (ensure_partials(L, 1)) return 1;
@@ -1164,6 +1244,13 @@ int slbc_put_pops(slbc_lattice *h, const double *a) {
 
 int slbc_get_pops(slbc_lattice *h, double *a) {
   Lattice &L = h->L;
+  if (L.precision != 2) {
+    if (double *dev_a = (double *)mapped_host(a)) {
+      CK(DISPATCH(L, launch_get_host, L, dev_a));
+      CK(cudaStreamSynchronize(L.stream));
+      return 0;
+    }
+  }
   if (ensure_staging(L, L.nnodes, 15)) return 1;
   const long long chunk = L.staging_nodes / 15;
   for (long long x0 = 0; x0 < L.nnodes; x0 += chunk) {

@@ -203,6 +203,8 @@ struct BatchState {
                                   long long x0, long long n);                   \
   cudaError_t launch_get_##SUFFIX(Lattice &L, double *stage, long long x0,      \
                                   long long n);                                 \
+  cudaError_t launch_put_host_##SUFFIX(Lattice &L, const double *host);         \
+  cudaError_t launch_get_host_##SUFFIX(Lattice &L, double *host);               \
   cudaError_t launch_swap_##SUFFIX(Lattice &L);                                 \
   cudaError_t launch_to_natural_##SUFFIX(Lattice &L);                           \
   cudaError_t launch_bbl_##SUFFIX(Lattice &L, int with_force);                  \

@@ -658,6 +658,50 @@ __global__ void k_get(PopArgs<T> p, int layout, double *stage, long long x0, lon
   for (int q = 0; q < 15; q++) stage[15 * e + q] = (double)post_value<T>(p.pop, p.npad, layout, q, x, fl, nb);
 }
 
+// The same two conversions straight from / to a page-locked host array
+// the device can address (zero-copy over the host link): a block moves
+// kHostTile nodes through shared memory, so that its reads (put) or writes
+// (get) of the host array are whole contiguous runs of 15 * kHostTile
+// doubles rather than 15 strided 8-byte accesses per node.
+constexpr int kHostTile = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kHostTile) k_put_host(PopArgs<T> p, const double *host, long long n) {
+  __shared__ double buf[15 * kHostTile];
+  for (long long x0 = (long long)blockIdx.x * kHostTile; x0 < n; x0 += (long long)gridDim.x * kHostTile) {
+    const int cnt = (int)(n - x0 < kHostTile ? n - x0 : kHostTile);
+    for (int e = threadIdx.x; e < 15 * cnt; e += kHostTile) buf[e] = host[15 * x0 + e];
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const long long x = x0 + threadIdx.x;
+#pragma unroll
+      for (int q = 0; q < 15; q++) p.pop[q * p.npad + x] = (T)buf[15 * threadIdx.x + q];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kHostTile) k_get_host(PopArgs<T> p, int layout, double *host, long long n) {
+  __shared__ double buf[15 * kHostTile];
+  for (long long x0 = (long long)blockIdx.x * kHostTile; x0 < n; x0 += (long long)gridDim.x * kHostTile) {
+    const int cnt = (int)(n - x0 < kHostTile ? n - x0 : kHostTile);
+    if (threadIdx.x < cnt) {
+      const int x = (int)(x0 + threadIdx.x);
+      int i, j, k;
+      decode(x, p.esj, p.esk, i, j, k);
+      const Nbr nb = make_nbr(i, j, k, p.esi, p.esj, p.esk);
+      const uint16_t fl = p.flags[x];
+#pragma unroll
+      for (int q = 0; q < 15; q++)
+        buf[15 * threadIdx.x + q] = (double)post_value<T>(p.pop, p.npad, layout, q, x, fl, nb);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 15 * cnt; e += kHostTile) host[15 * x0 + e] = buf[e];
+    __syncthreads();
+  }
+}
+
 // N <-> C0: swap the slots of opposite populations at every node.
 template <typename T>
 __global__ void k_swap(PopArgs<T> p, long long n) {

@@ -280,6 +280,20 @@ cudaError_t SLBC_FN(launch_get)(Lattice &L, double *stage, long long x0, long lo
   return cudaGetLastError();
 }
 
+cudaError_t SLBC_FN(launch_put_host)(Lattice &L, const double *host) {
+  const int blocks = (int)std::min<long long>((L.nnodes + kHostTile - 1) / kHostTile, 152LL * 16);
+  k_put_host<T_><<<blocks, kHostTile, 0, L.stream>>>(pop_args(L), host, L.nnodes);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t SLBC_FN(launch_get_host)(Lattice &L, double *host) {
+  const int blocks = (int)std::min<long long>((L.nnodes + kHostTile - 1) / kHostTile, 152LL * 16);
+  k_get_host<T_><<<blocks, kHostTile, 0, L.stream>>>(pop_args(L), L.layout, host, L.nnodes);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t SLBC_FN(launch_swap)(Lattice &L) {
   k_swap<T_><<<flat_blocks(L.nnodes, 256), 256, 0, L.stream>>>(pop_args(L), L.nnodes);
   count_launch();

@@ -437,6 +437,68 @@ __global__ void k_decode(const float *pred, int ctot_p, const unsigned char *sol
   }
 }
 
+// Uniform plane flux of a decoded state (u: 3 x D*H*W, x = the slowest
+// index; the flux of x through plane i is q[i] = sum over the plane of u_x).
+// k_plane_sum: one block per plane, a fixed summation order.
+__global__ void __launch_bounds__(256) k_plane_sum(const float *u, int D, long long plane, double *q) {
+  __shared__ double sh[256];
+  const int i = blockIdx.x;
+  double acc = 0.0;
+  for (long long e = threadIdx.x; e < plane; e += blockDim.x) acc += (double)u[(long long)i * plane + e];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) q[i] = sh[0];
+}
+
+// One thread: the harmonic mean qh of the plane fluxes, the scale qh / q[i]
+// of every plane and the pressure p[i] = sum over the planes before i of
+// force (1 - qh / q) (midpoint rule, zero mean); work = [q | scale | p |
+// spread].  Any plane flux <= 0 leaves the state as it is (scale 1, p 0).
+__global__ void k_plane_fix(int D, float force, double *work) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double *q = work, *scale = work + D, *p = work + 2 * D;
+  bool ok = true;
+  double inv = 0.0, qmin = q[0], qmax = q[0], qsum = 0.0;
+  for (int i = 0; i < D; i++) {
+    ok = ok && q[i] > 0.0;
+    inv += 1.0 / q[i];
+    qmin = fmin(qmin, q[i]);
+    qmax = fmax(qmax, q[i]);
+    qsum += q[i];
+  }
+  work[3 * D] = ok ? (qmax - qmin) / (qsum / D) : -1.0;
+  const double qh = D / inv;
+  double acc = 0.0, mean = 0.0;
+  for (int i = 0; i < D; i++) {
+    const double g = ok ? (double)force * (1.0 - qh / q[i]) : 0.0;
+    scale[i] = ok ? qh / q[i] : 1.0;
+    p[i] = acc + 0.5 * g;
+    acc += g;
+    mean += p[i];
+  }
+  mean /= D;
+  for (int i = 0; i < D; i++) p[i] -= mean;
+}
+
+// u[c][x] *= scale[i]; drho[x] += 3 p[i] on fluid nodes (p = rho / 3)
+__global__ void k_plane_apply(float *u, float *drho, const unsigned char *solid, int D, long long plane,
+                              const double *work) {
+  const long long total = (long long)D * plane;
+  const double *scale = work + D, *p = work + 2 * D;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / plane);
+    const float s = (float)scale[i];
+    u[e] *= s;
+    u[total + e] *= s;
+    u[2 * total + e] *= s;
+    if (drho && !solid[e]) drho[e] += (float)(3.0 * p[i]);
+  }
+}
+
 bool ok8(int ctot, int coff, int C) { return ctot % 8 == 0 && coff % 8 == 0 && C % 8 == 0 && C > 0 && coff + C <= ctot; }
 
 int launched(const char *what) {
@@ -602,6 +664,19 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
     if (e != cudaSuccess && rc == 0) return bad((std::string("slbc_nn_encode scratch: ") + cudaGetErrorString(e)).c_str());
   }
   return rc;
+}
+
+int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D, int H, int W, float force,
+                       double *work, void *stream) {
+  if (D < 1 || H < 1 || W < 1 || D > 65535 || !u || !solid || !work) return bad("slbc_nn_plane_flux: bad arguments");
+  const cudaStream_t st = (cudaStream_t)stream;
+  const long long plane = (long long)H * W;
+  k_plane_sum<<<D, 256, 0, st>>>(u, D, plane, work);
+  if (launched("slbc_nn_plane_flux")) return 1;
+  k_plane_fix<<<1, 32, 0, st>>>(D, force, work);
+  if (launched("slbc_nn_plane_flux")) return 1;
+  k_plane_apply<<<grid_for((long long)D * plane), 256, 0, st>>>(u, drho, solid, D, plane, work);
+  return launched("slbc_nn_plane_flux");
 }
 
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,

@@ -175,46 +175,126 @@ static int objmap_get(objmap_t *m, LBObj p, int *next, LBObj **objs, int *cap) {
   return (*next)++;
 }
 
+static int objmap_find(const objmap_t *m, LBObj p) {
+  unsigned long h = ptr_hash(p) & (unsigned long)(m->cap - 1);
+  while (m->key[h] != NULL) {
+    if (m->key[h] == p) return m->val[h];
+    h = (h + 1) & (unsigned long)(m->cap - 1);
+  }
+  return -1;
+}
+
+/* distinct objects of one range of the map, in first-seen order */
+typedef struct {
+  LBObj *key;     /* open-addressing set */
+  long cap;
+  LBObj *list;    /* first-seen order */
+  long count, list_cap;
+} objseen_t;
+
+typedef struct {
+  LBSys lb;
+  long n;
+  int chunks;
+  objseen_t *seen;
+  const objmap_t *map;
+  int *objidx;
+} objscan_t;
+
+static void seen_add(objseen_t *s, LBObj p) {
+  unsigned long h;
+  if (2 * (s->count + 1) > s->cap) {  /* grow and rehash */
+    long cap = s->cap ? 4 * s->cap : 64, e;
+    LBObj *key = (LBObj *)xcalloc(cap, sizeof(LBObj));
+    for (e = 0; e < s->count; e++) {
+      h = ptr_hash(s->list[e]) & (unsigned long)(cap - 1);
+      while (key[h] != NULL) h = (h + 1) & (unsigned long)(cap - 1);
+      key[h] = s->list[e];
+    }
+    free(s->key);
+    s->key = key;
+    s->cap = cap;
+  }
+  h = ptr_hash(p) & (unsigned long)(s->cap - 1);
+  while (s->key[h] != NULL) {
+    if (s->key[h] == p) return;
+    h = (h + 1) & (unsigned long)(s->cap - 1);
+  }
+  s->key[h] = p;
+  if (s->count == s->list_cap) {
+    s->list_cap = s->list_cap ? 2 * s->list_cap : 16;
+    s->list = (LBObj *)realloc(s->list, (size_t)s->list_cap * sizeof(LBObj));
+    if (s->list == NULL) error("No room for the object scan");
+  }
+  s->list[s->count++] = p;
+}
+
+/* tasks [lo, hi) of the first pass: the distinct objects of each range */
+static void scan_seen(long lo, long hi, void *ctx) {
+  objscan_t *c = (objscan_t *)ctx;
+  long t, x;
+  for (t = lo; t < hi; t++) {
+    const long x0 = c->n * t / c->chunks, x1 = c->n * (t + 1) / c->chunks;
+    LBObj last = NULL;
+    for (x = x0; x < x1; x++) {
+      LBObj p = c->lb->obj[x];
+      if (p == NULL || p == last) continue;
+      last = p;
+      seen_add(&c->seen[t], p);
+    }
+  }
+}
+
+/* tasks of the last pass: the dense index of every node */
+static void scan_fill(long lo, long hi, void *ctx) {
+  objscan_t *c = (objscan_t *)ctx;
+  long t, x;
+  for (t = lo; t < hi; t++) {
+    const long x0 = c->n * t / c->chunks, x1 = c->n * (t + 1) / c->chunks;
+    LBObj last = NULL;
+    int idx = -1;
+    for (x = x0; x < x1; x++) {
+      LBObj p = c->lb->obj[x];
+      if (p == NULL) { c->objidx[x] = -1; continue; }
+      if (p != last) { last = p; idx = objmap_find(c->map, p); }
+      c->objidx[x] = idx;
+    }
+  }
+}
+
 static void upload_geometry(LBSys lb) {
   slb_priv *st = slb_state(lb);
-  long n = lb->nnodes, x, nb = 0;
-  int nobj = 0, cap = 16;
-  int *objidx = (int *)xcalloc(n, sizeof(int));
+  long n = lb->nnodes, nb = 0;
+  int nobj = 0, cap = 16, t;
+  int *objidx = (int *)malloc((size_t)n * sizeof(int));
   LBObj *objs = (LBObj *)xcalloc(cap, sizeof(LBObj));
   objmap_t m;
-  /* dense index of every object the map references, in first-seen order */
+  objscan_t sc;
+  if (objidx == NULL) error("No room for the object index");
+  /* dense index of every object the map references, in first-seen order:
+   * the distinct objects of contiguous ranges in parallel, merged in range
+   * order, then every node's index in parallel */
+  sc.lb = lb; sc.n = n; sc.objidx = objidx;
+  sc.chunks = slb_par_threads(n, 1L << 20);
+  sc.seen = (objseen_t *)xcalloc(sc.chunks, sizeof(objseen_t));
+  slb_parallel_for(sc.chunks, 1, scan_seen, &sc);
   m.cap = 64;
   {
-    long nobjlist = 0;
-    LBObj p;
-    for (p = lb->obj_head; p != NULL; p = p->next_obj) nobjlist++;
-    while (m.cap < 4 * (nobjlist + 16)) m.cap *= 2;
+    long distinct = 16;
+    for (t = 0; t < sc.chunks; t++) distinct += sc.seen[t].count;
+    while (m.cap < 4 * distinct) m.cap *= 2;
   }
   m.key = (LBObj *)xcalloc(m.cap, sizeof(LBObj));
   m.val = (int *)xcalloc(m.cap, sizeof(int));
-  for (x = 0; x < n; x++) {
-    LBObj p = lb->obj[x];
-    if (p == NULL) { objidx[x] = -1; continue; }
-    if (x > 0 && lb->obj[x - 1] == p) { objidx[x] = objidx[x - 1]; continue; }
-    if (2 * (nobj + 1) > m.cap) {
-      /* grow and rehash */
-      objmap_t g;
-      long e;
-      g.cap = m.cap * 4;
-      g.key = (LBObj *)xcalloc(g.cap, sizeof(LBObj));
-      g.val = (int *)xcalloc(g.cap, sizeof(int));
-      for (e = 0; e < m.cap; e++) {
-        unsigned long h;
-        if (m.key[e] == NULL) continue;
-        h = ptr_hash(m.key[e]) & (unsigned long)(g.cap - 1);
-        while (g.key[h] != NULL) h = (h + 1) & (unsigned long)(g.cap - 1);
-        g.key[h] = m.key[e]; g.val[h] = m.val[e];
-      }
-      free(m.key); free(m.val);
-      m = g;
-    }
-    objidx[x] = objmap_get(&m, p, &nobj, &objs, &cap);
+  for (t = 0; t < sc.chunks; t++) {
+    long e;
+    for (e = 0; e < sc.seen[t].count; e++) objmap_get(&m, sc.seen[t].list[e], &nobj, &objs, &cap);
+    free(sc.seen[t].key);
+    free(sc.seen[t].list);
   }
+  free(sc.seen);
+  sc.map = &m;
+  slb_parallel_for(sc.chunks, 1, scan_fill, &sc);
   free(m.key); free(m.val);
   /* flag words on the GPU, and from them the solid nodes with a fluid
    * neighbour, grouped by object, node order kept */
@@ -233,11 +313,21 @@ static void upload_geometry(LBSys lb) {
   st->host_f_valid = 0;
 }
 
+typedef struct { const int *mask; unsigned char *ads; } adsfill_t;
+
+static void fill_ads(long lo, long hi, void *ctx) {
+  adsfill_t *a = (adsfill_t *)ctx;
+  long x;
+  for (x = lo; x < hi; x++) a->ads[x] = (a->mask[x] & 0x4000) ? 1 : 0;
+}
+
 static void upload_ads(LBSys lb) {
   slb_priv *st = slb_state(lb);
-  long x;
-  unsigned char *ads = (unsigned char *)xcalloc(lb->nnodes, 1);
-  for (x = 0; x < lb->nnodes; x++) ads[x] = (lb->mask[x] & 0x4000) ? 1 : 0;
+  adsfill_t a;
+  unsigned char *ads = (unsigned char *)malloc((size_t)lb->nnodes);
+  if (ads == NULL) error("No room for the adsorption bits");
+  a.mask = lb->mask; a.ads = ads;
+  slb_parallel_for(lb->nnodes, 1L << 20, fill_ads, &a);
   slb_check(slbc_set_adsorption(st->dev, ads), "adsorption upload");
   free(ads);
   st->ads_sent = st->ads_gen;
@@ -302,6 +392,13 @@ slbc_lattice *slb_device(LBSys lb) {
 
 /* ---- appended API --------------------------------------------------------- */
 
+static void zero_forces(long lo, long hi, void *ctx) {
+  LBSys lb = (LBSys)ctx;
+  memset(lb->fx + lo, 0, (size_t)(hi - lo) * sizeof(LBReal));
+  memset(lb->fy + lo, 0, (size_t)(hi - lo) * sizeof(LBReal));
+  memset(lb->fz + lo, 0, (size_t)(hi - lo) * sizeof(LBReal));
+}
+
 void lbpull(LBSys lb) {
   slb_priv *st = slb_state(lb);
   if (st->dev == NULL) { slb_host_a(lb); return; }
@@ -313,7 +410,7 @@ void lbpull(LBSys lb) {
     long e, x;
     double *f3 = (double *)xcalloc(3 * (size_t)(st->nbnd + 1), sizeof(double));
     slb_check(slbc_get_force(st->dev, f3), "force download");
-    for (x = 0; x < lb->nnodes; x++) lb->fx[x] = lb->fy[x] = lb->fz[x] = 0.0;
+    slb_parallel_for(lb->nnodes, 1L << 20, zero_forces, lb);
     for (e = 0; e < st->nbnd; e++) {
       x = st->bnd_node[e];
       lb->fx[x] = f3[3 * e]; lb->fy[x] = f3[3 * e + 1]; lb->fz[x] = f3[3 * e + 2];

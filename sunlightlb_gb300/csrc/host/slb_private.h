@@ -57,5 +57,9 @@ void slb_trace(LBSys lb, const char *what);
 void slb_pull_rho(LBSys lb);
 void slb_need_populations(LBSys lb, const char *what);
 void slb_need_relaxed_solids(LBSys lb);
+/* parallel loop over [0, n) in contiguous ranges of at least `grain` (slb_par.c) */
+typedef void (*slb_range_fn)(long lo, long hi, void *ctx);
+void slb_parallel_for(long n, long grain, slb_range_fn fn, void *ctx);
+int slb_par_threads(long n, long grain);
 
 #endif

