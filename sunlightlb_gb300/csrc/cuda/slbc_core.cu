@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cmath>
 #include <thread>
+#include <memory>
+#include <new>
 
 #include "slbc_internal.cuh"
 #include "slbc_kernels.cuh"
@@ -1355,15 +1357,19 @@ int slbc_scale_force(slbc_lattice *h, double fac) {
 int slbc_get_force(slbc_lattice *h, double *f3) {
   Lattice &L = h->L;
   if (!L.nbnd) return 0;
-  std::vector<double> tmp(3 * (size_t)L.nbnd);
-  CK(cudaMemcpyAsync(tmp.data(), L.bnd_f, 3 * (size_t)L.nbnd * sizeof(double),
-                     cudaMemcpyDeviceToHost, L.stream));
+  std::unique_ptr<double[]> tmp(new (std::nothrow) double[3 * (size_t)L.nbnd]);
+  if (!tmp) return fail_msg("slbc_get_force: no host memory");
+  double *t = tmp.get();
+  CK(cudaMemcpyAsync(t, L.bnd_f, 3 * (size_t)L.nbnd * sizeof(double), cudaMemcpyDeviceToHost, L.stream));
   CK(cudaStreamSynchronize(L.stream));
-  for (long long e = 0; e < L.nbnd; e++) {
-    f3[3 * e] = tmp[e];
-    f3[3 * e + 1] = tmp[L.nbnd + e];
-    f3[3 * e + 2] = tmp[2 * L.nbnd + e];
-  }
+  const long long nb = L.nbnd;
+  host_par_for(nb, 1LL << 18, [&](long long lo, long long hi) {
+    for (long long e = lo; e < hi; e++) {
+      f3[3 * e] = t[e];
+      f3[3 * e + 1] = t[nb + e];
+      f3[3 * e + 2] = t[2 * nb + e];
+    }
+  });
   return 0;
 }
 

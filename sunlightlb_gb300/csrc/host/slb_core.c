@@ -399,6 +399,18 @@ static void zero_forces(long lo, long hi, void *ctx) {
   memset(lb->fz + lo, 0, (size_t)(hi - lo) * sizeof(LBReal));
 }
 
+typedef struct { LBSys lb; const long *node; const double *f3; } fscatter_t;
+
+/* node forces of the boundary list into lb->fx/fy/fz (distinct nodes) */
+static void scatter_forces(long lo, long hi, void *ctx) {
+  fscatter_t *f = (fscatter_t *)ctx;
+  long e;
+  for (e = lo; e < hi; e++) {
+    const long x = f->node[e];
+    f->lb->fx[x] = f->f3[3 * e]; f->lb->fy[x] = f->f3[3 * e + 1]; f->lb->fz[x] = f->f3[3 * e + 2];
+  }
+}
+
 void lbpull(LBSys lb) {
   slb_priv *st = slb_state(lb);
   if (st->dev == NULL) { slb_host_a(lb); return; }
@@ -407,14 +419,13 @@ void lbpull(LBSys lb) {
     st->host_a_valid = 1;
   }
   if (!st->host_f_valid) {
-    long e, x;
-    double *f3 = (double *)xcalloc(3 * (size_t)(st->nbnd + 1), sizeof(double));
+    fscatter_t fs;
+    double *f3 = (double *)malloc(3 * (size_t)(st->nbnd + 1) * sizeof(double));
+    if (f3 == NULL) error("No room for the node forces");
     slb_check(slbc_get_force(st->dev, f3), "force download");
     slb_parallel_for(lb->nnodes, 1L << 20, zero_forces, lb);
-    for (e = 0; e < st->nbnd; e++) {
-      x = st->bnd_node[e];
-      lb->fx[x] = f3[3 * e]; lb->fy[x] = f3[3 * e + 1]; lb->fz[x] = f3[3 * e + 2];
-    }
+    fs.lb = lb; fs.node = st->bnd_node; fs.f3 = f3;
+    slb_parallel_for(st->nbnd, 1L << 18, scatter_forces, &fs);
     free(f3);
     st->host_f_valid = 1;
   }
