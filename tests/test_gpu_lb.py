@@ -156,3 +156,65 @@ def test_precision_switch_keeps_state(gpu):
     pa, pb = a.pops(), b.pops()
     assert a.step == b.step == 21
     assert np.abs(pa - pb).max() < 1e-6 * np.abs(pb).max()
+
+
+def test_large_lattice_many_objects(gpu, orc):
+    """A lattice large enough for the host loops of the geometry upload to
+    run in several ranges (3.1 M nodes), with 40 spheres spread over it: the
+    dense object index keeps the first-seen order, so every object's force
+    and torque and every population equal the oracle's (FP64, bit-exact
+    populations)."""
+    rng = np.random.default_rng(31)
+    dims = (192, 128, 128)
+    spheres = [(rng.uniform(3.0, 6.0), *(rng.uniform(0, d) for d in dims)) for _ in range(40)]
+    lbs = []
+    for L in (gpu, orc):
+        lb = L.newlb(*dims, "null")
+        if L.extended:
+            lb.precision = 0
+        lb.tau = 0.8
+        for r, x, y, z in spheres:
+            assert L.insertsph(lb, r, x, y, z) is not None
+        L.addbf(lb, 1e-5, 2e-6, 0.0)
+        for _ in range(3):
+            L.lbstep(lb)
+        L.measure(lb)
+        lbs.append(lb)
+    g, o = lbs
+    assert np.array_equal(g.pops(), o.pops())
+    fg, fo = objects_ft(g), objects_ft(o)
+    assert fg.shape == fo.shape == (40, 6)
+    assert close(fg[:, :3], fo[:, :3], RED_TOL)
+    assert close(fg[:, 3:], fo[:, 3:], RED_TOL)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_population_transfer_paths(gpu, precision):
+    """Download and upload of the populations through both host paths --
+    straight to and from the page-locked mirror lb->a, and through the
+    device staging buffer for a pageable array -- give the same values."""
+    import ctypes as C
+    lb = two_spheres(gpu, dims=(20, 17, 33), steps=11, measure=False, precision=precision)
+    gpu.lbpull(lb)
+    pinned = lb.pops().copy()
+    dev_fn = gpu.dll.slb_device
+    dev_fn.argtypes = [C.c_void_p]
+    dev_fn.restype = C.c_void_p
+    get = gpu.dll.slbc_get_pops
+    get.argtypes = [C.c_void_p, C.c_void_p]
+    get.restype = C.c_int
+    put = gpu.dll.slbc_put_pops
+    put.argtypes = [C.c_void_p, C.c_void_p]
+    put.restype = C.c_int
+    dev = dev_fn(lb)
+    pageable = np.zeros(15 * lb.nnodes)
+    assert get(dev, pageable.ctypes.data) == 0
+    assert np.array_equal(pageable, pinned.ravel())
+    # a changed state uploaded from pageable memory reads back through the mirror
+    changed = pageable * (1.0 + 1e-3 * np.sin(np.arange(pageable.size)))
+    if precision == 1:
+        changed = changed.astype(np.float32).astype(np.float64)
+    assert put(dev, changed.ctypes.data) == 0
+    a = lb.array("a")
+    assert get(dev, a.ctypes.data) == 0
+    assert np.array_equal(a.ravel(), changed)
