@@ -1063,6 +1063,11 @@ def run_warmstart(args):
                 vs, ds = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0), None
             elif name == "no_plane_flux":  # the state as decoded, without the plane-flux correction
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, plane_flux=False)
+            elif name == "plane_flux_velocity":  # the plane-flux velocity scaling without its pressure
+                vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, plane_flux=False)
+                work = torch.empty(3 * ev_side + 1, device="cuda", dtype=torch.float64)
+                inf.k.nn_plane_flux(vs.data_ptr(), None, sdev.data_ptr(), ev_side, ev_side, ev_side, force,
+                                    work.data_ptr(), inf.stream)
             else:
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0)
             hs = WS.first_within(WS.permeability_run(L, solid, force, k_ref=k_conv, warm_u=vs, warm_drho=ds, check=50),
