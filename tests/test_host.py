@@ -233,3 +233,32 @@ def test_flow_symmetries_algebra():
         assert int((l2[..., 3] == 5.0 * s).sum()) == 63, bits
     m2, l2 = WS.symmetry(m, lab4, 1, 1, 1, 1)
     assert float(l2[..., 3].sum()) == -(7.0 + 63 * 5.0)
+
+
+def test_host_parallel_ranges_cover_once(gpu):
+    """slb_parallel_for (the host loops of uploads and downloads): the
+    ranges handed to the callback cover [0, n) exactly once, for sizes
+    below, at and above the split threshold, on however many host threads
+    the machine has."""
+    import ctypes as C
+    import threading
+    fn_t = C.CFUNCTYPE(None, C.c_long, C.c_long, C.c_void_p)
+    par = gpu.dll.slb_parallel_for
+    par.argtypes = [C.c_long, C.c_long, fn_t, C.c_void_p]
+    par.restype = None
+    lock = threading.Lock()
+    for n, grain in ((0, 16), (5, 16), (1000, 1), (1 << 20, 1 << 16), (3_000_001, 1 << 18)):
+        seen = []
+
+        def cb(lo, hi, ctx):
+            with lock:
+                seen.append((lo, hi))
+
+        cfun = fn_t(cb)
+        par(n, grain, cfun, None)
+        seen.sort()
+        covered = 0
+        for lo, hi in seen:
+            assert lo == covered and hi >= lo, (n, seen)
+            covered = hi
+        assert covered == n, (n, seen)
