@@ -1066,7 +1066,7 @@ def run_warmstart(args):
             elif name == "plane_flux_velocity":  # the plane-flux velocity scaling without its pressure
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, plane_flux=False)
                 work = torch.empty(3 * ev_side + 1, device="cuda", dtype=torch.float64)
-                inf.k.nn_plane_flux(vs.data_ptr(), None, sdev.data_ptr(), ev_side, ev_side, ev_side, force,
+                inf.k.nn_plane_flux(vs.data_ptr(), None, sdev.data_ptr(), ev_side, ev_side, ev_side, force, 1.0,
                                     work.data_ptr(), inf.stream)
             else:
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0)

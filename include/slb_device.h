@@ -382,12 +382,14 @@ int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, in
  * plane i times qh / q[i]), and the fluid nodes of plane i get the density
  * deviation 3 p[i], p the pressure that carries the body force `force`
  * through slabs in series (dp/dx = force (1 - qh / q[i]), zero mean).  A
- * converged periodic flow has the same mass flux through every plane.
- * work: 3 D + 1 device doubles (q, scale, p, then the relative spread
- * (max - min) / mean of the fluxes before, -1 when some flux is <= 0 and
- * nothing was changed). */
+ * converged periodic flow has the same mass flux through every plane.  The
+ * whole state (velocity, density deviation, p) is then multiplied by gain
+ * (1: none; a calibrated flux gain of the network otherwise).  work: 3 D + 1
+ * device doubles (q, scale, p, then the relative spread (max - min) / mean
+ * of the fluxes before, -1 when some flux is <= 0 and only the gain was
+ * applied). */
 int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D, int H, int W, float force,
-                       double *work, void *stream);
+                       float gain, double *work, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

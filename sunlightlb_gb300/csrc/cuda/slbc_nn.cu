@@ -456,9 +456,10 @@ __global__ void __launch_bounds__(256) k_plane_sum(const float *u, int D, long l
 
 // One thread: the harmonic mean qh of the plane fluxes, the scale qh / q[i]
 // of every plane and the pressure p[i] = sum over the planes before i of
-// force (1 - qh / q) (midpoint rule, zero mean); work = [q | scale | p |
-// spread].  Any plane flux <= 0 leaves the state as it is (scale 1, p 0).
-__global__ void k_plane_fix(int D, float force, double *work) {
+// force (1 - qh / q) (midpoint rule, zero mean), both times gain; work =
+// [q | scale | p | spread].  Any plane flux <= 0 leaves the planes as they
+// are (scale = gain, p 0).
+__global__ void k_plane_fix(int D, float force, float gain, double *work) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double *q = work, *scale = work + D, *p = work + 2 * D;
   bool ok = true;
@@ -475,18 +476,18 @@ __global__ void k_plane_fix(int D, float force, double *work) {
   double acc = 0.0, mean = 0.0;
   for (int i = 0; i < D; i++) {
     const double g = ok ? (double)force * (1.0 - qh / q[i]) : 0.0;
-    scale[i] = ok ? qh / q[i] : 1.0;
+    scale[i] = (ok ? qh / q[i] : 1.0) * gain;
     p[i] = acc + 0.5 * g;
     acc += g;
     mean += p[i];
   }
   mean /= D;
-  for (int i = 0; i < D; i++) p[i] -= mean;
+  for (int i = 0; i < D; i++) p[i] = (p[i] - mean) * gain;
 }
 
-// u[c][x] *= scale[i]; drho[x] += 3 p[i] on fluid nodes (p = rho / 3)
+// u[c][x] *= scale[i]; drho[x] = gain drho[x] + 3 p[i] on fluid nodes (p = rho / 3)
 __global__ void k_plane_apply(float *u, float *drho, const unsigned char *solid, int D, long long plane,
-                              const double *work) {
+                              float gain, const double *work) {
   const long long total = (long long)D * plane;
   const double *scale = work + D, *p = work + 2 * D;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
@@ -495,7 +496,7 @@ __global__ void k_plane_apply(float *u, float *drho, const unsigned char *solid,
     u[e] *= s;
     u[total + e] *= s;
     u[2 * total + e] *= s;
-    if (drho && !solid[e]) drho[e] += (float)(3.0 * p[i]);
+    if (drho) drho[e] = gain * drho[e] + (solid[e] ? 0.0f : (float)(3.0 * p[i]));
   }
 }
 
@@ -667,15 +668,15 @@ int slbc_nn_encode(const unsigned char *solid, int B, int D, int H, int W, void 
 }
 
 int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D, int H, int W, float force,
-                       double *work, void *stream) {
+                       float gain, double *work, void *stream) {
   if (D < 1 || H < 1 || W < 1 || D > 65535 || !u || !solid || !work) return bad("slbc_nn_plane_flux: bad arguments");
   const cudaStream_t st = (cudaStream_t)stream;
   const long long plane = (long long)H * W;
   k_plane_sum<<<D, 256, 0, st>>>(u, D, plane, work);
   if (launched("slbc_nn_plane_flux")) return 1;
-  k_plane_fix<<<1, 32, 0, st>>>(D, force, work);
+  k_plane_fix<<<1, 32, 0, st>>>(D, force, gain, work);
   if (launched("slbc_nn_plane_flux")) return 1;
-  k_plane_apply<<<grid_for((long long)D * plane), 256, 0, st>>>(u, drho, solid, D, plane, work);
+  k_plane_apply<<<grid_for((long long)D * plane), 256, 0, st>>>(u, drho, solid, D, plane, gain, work);
   return launched("slbc_nn_plane_flux");
 }
 

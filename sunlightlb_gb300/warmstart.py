@@ -64,7 +64,7 @@ class Kernels:
             "slbc_nn_scale": [p, ll, p, p],
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, f, p, p],
-            "slbc_nn_plane_flux": [p, p, p, i, i, i, f, p, p],
+            "slbc_nn_plane_flux": [p, p, p, i, i, i, f, f, p, p],
             "slbc_tc_status": [],
         }
         self.dll = dll
@@ -542,7 +542,7 @@ def predict_velocity(net, solid_u8, force, eta, rho0=72.0, force_shift=1.0):
     return u
 
 
-def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_flux=True, info=None):
+def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_flux=True, info=None, gain=1.0):
     """Velocity (3 x N) and density deviation (N) device FP32 fields from a
     network trained on labels with density (converged_flows(density=True)):
     with its own density a converged state is rebuilt exactly from
@@ -552,7 +552,11 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_f
     sees part of the bed, predicts each slab as if the whole body force
     drove it.  On 59 held-out 128^3 packings this took the total wall time
     to k within 1e-4 from 2.18x to 2.32x less than the plain start.  info
-    (a dict) receives the relative spread of the plane fluxes before."""
+    (a dict) receives the relative spread of the plane fluxes before.  gain
+    multiplies the state after the plane-flux step (plane_flux must be on
+    for it; a global gain calibrated so that warm states start with the
+    converged mean flow, 0.991 for the committed network, measured worse:
+    the fast transients of the first steps take flux with them)."""
     import torch
     net.encode(solid_u8.view(1, *solid_u8.shape))
     out = net.forward()
@@ -561,10 +565,12 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_f
     drho = torch.empty(n, device="cuda", dtype=torch.float32)
     net.k.nn_decode(out.data_ptr(), OUT_CH, solid_u8.data_ptr(), net.D, net.H, net.W, force / eta,
                     force_shift * force / rho0, u.data_ptr(), DRHO_UNIT * force, drho.data_ptr(), net.stream)
+    if not plane_flux and gain != 1.0:
+        raise ValueError("predict_state: a gain needs the plane-flux step")
     if plane_flux:
         work = torch.empty(3 * net.D + 1, device="cuda", dtype=torch.float64)
         net.k.nn_plane_flux(u.data_ptr(), drho.data_ptr(), solid_u8.data_ptr(), net.D, net.H, net.W, force,
-                            work.data_ptr(), net.stream)
+                            float(gain), work.data_ptr(), net.stream)
         if info is not None:
             info["plane_flux_spread"] = float(work[3 * net.D])
     return u, drho

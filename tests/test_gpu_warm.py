@@ -231,7 +231,7 @@ def test_plane_flux_correction(gpu):
     u = torch.as_tensor(u0.astype(np.float32).ravel(), device="cuda")
     dr = torch.as_tensor(d0.astype(np.float32).ravel(), device="cuda")
     work = torch.zeros(3 * D + 1, device="cuda", dtype=torch.float64)
-    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, work.data_ptr(), st)
+    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, 1.0, work.data_ptr(), st)
     torch.cuda.synchronize()
     u32 = u0.astype(np.float32).astype(np.float64)
     q = u32[0].sum(axis=(1, 2))
@@ -253,11 +253,20 @@ def test_plane_flux_correction(gpu):
     u1[0, 3] = 0.0
     u = torch.as_tensor(u1.astype(np.float32).ravel(), device="cuda")
     dr = torch.as_tensor(d0.astype(np.float32).ravel(), device="cuda")
-    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, work.data_ptr(), st)
+    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, 1.0, work.data_ptr(), st)
     torch.cuda.synchronize()
     assert np.array_equal(u.cpu().numpy(), u1.astype(np.float32).ravel())
     assert np.array_equal(dr.cpu().numpy(), d0.astype(np.float32).ravel())
     assert float(work[3 * D]) == -1.0
+    # a gain multiplies the corrected state: velocity, density and pressure
+    u = torch.as_tensor(u0.astype(np.float32).ravel(), device="cuda")
+    dr = torch.as_tensor(d0.astype(np.float32).ravel(), device="cuda")
+    k.nn_plane_flux(u.data_ptr(), dr.data_ptr(), sdev.data_ptr(), D, H, W, force, 0.75, work.data_ptr(), st)
+    torch.cuda.synchronize()
+    got_u = u.cpu().numpy().astype(np.float64).reshape(3, D, H, W)
+    got_d = dr.cpu().numpy().astype(np.float64).reshape(D, H, W)
+    assert np.abs(got_u - 0.75 * want_u).max() <= 1e-6 * np.abs(want_u).max()
+    assert np.abs(got_d - 0.75 * want_d).max() <= 1e-6 * np.abs(want_d).max()
 
 
 def test_gradient_clipping(gpu):
