@@ -613,7 +613,9 @@ def permeability_run(L, solid, force, k_ref=None, warm_u=None, tol=1e-8, rel=1e-
     in the flow, so a prediction of the right shape but a mean flow (1 +
     eps) times the converged one feels (1 + eps) times the body force; the
     warm state is set again scaled by 1 / (1 + eps) and the steps and time
-    spent count towards the run.  probe > 0 (with k_ref) instead records,
+    spent count towards the run (measured on held-out 128^3 packings: no
+    gain, because the wall force answers the prediction's near-wall error
+    rather than its mean-flow error).  probe > 0 (with k_ref) instead records,
     for `probe` measures in a row after the warm state, the force imbalance
     beside the permeability error: returns [(steps, imbalance, k error)].
     A dict `stats` receives the force imbalance of the final state
