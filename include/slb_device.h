@@ -316,6 +316,17 @@ int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int co
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream);
+/* slbc_tc_cmajor's copy (zero_halo 0) written as K-tile blocks for
+ * slbc_tc_wgrad_tiles: the 64-position rows of flat tile t = position / 64
+ * go to dst[t][copy][c][64] (ncopy copies side by side per tile). */
+int slbc_tc_cmajor_tiles(const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
+                         long long pstride, int shift, int copy, int ncopy, void *dst, void *stream);
+/* slbc_tc_wgrad with dY's three copies as K-tile blocks dyt[t][3][cout][64]
+ * (slbc_tc_cmajor_tiles, copy = shift + 1, ncopy 3): one tile's operand is
+ * one contiguous block of memory.  cout 32, 64 or 128. */
+int slbc_tc_wgrad_tiles(const void *dyt, const void *xt, int B, int D, int H, int W, int Wp, long long pstride,
+                        int cin, int cout, float *partial, long long partial_floats, int splits, float *dw,
+                        void *stream);
 /* K splits for slbc_tc_wgrad that fill the current device once (at most
  * k_tiles / 8 and max_splits; k_tiles = B * pstride / 64). */
 int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_splits);

@@ -620,10 +620,12 @@ k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensor
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int group = blockIdx.x / w.co_tiles, cot = blockIdx.x % w.co_tiles;
   const int tap0 = group * w.taps_per_tile, co0 = cot * w.co_rows, ci0 = blockIdx.y * w.ntile;
-  const long long per = (w.k_tiles + w.splits - 1) / w.splits;
-  const long long k_lo = (long long)blockIdx.z * per;
-  const long long k_hi = k_lo + per < w.k_tiles ? k_lo + per : w.k_tiles;
-  const int nk = k_hi > k_lo ? (int)(k_hi - k_lo) : 0;
+  // K tiles z, z + splits, z + 2 splits, ... (z = blockIdx.z): the blocks
+  // of one launch work through one run of consecutive tiles at a time, so
+  // the windows that other taps read again (up to a plane further on) are
+  // still in L2
+  const long long kz = blockIdx.z;
+  const int nk = kz < w.k_tiles ? (int)((w.k_tiles - kz + w.splits - 1) / w.splits) : 0;
   const uint32_t bytes_a = 128u * 128u, bytes_b = (uint32_t)w.ntile * 128u;
   if (warp == 0) {
     tc::tmem_alloc(&tmem_base, (uint32_t)w.tmem_cols);
@@ -650,7 +652,7 @@ k_wgrad(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensor
         ok = false;
         break;
       }
-      const int k0 = (int)((k_lo + kt) * 64);
+      const int k0 = (int)((kz + (long long)kt * w.splits) * 64);
       tc::mbar_expect_tx(&full[s], bytes_a + bytes_b);
       for (int tl = 0; tl < w.taps_per_tile; tl++) {
         const int tap = tap0 + tl < 27 ? tap0 + tl : 26;  // rows past tap 26 are discarded
@@ -736,6 +738,16 @@ struct WgradNArgs {
   int splits;
   int tmem_cols;
   float *partial;  // [splits][27][cout][cin]
+  // one TMA box per stage and operand where the layout allows it: the dpm
+  // dY copies as one 3-D box (copies equally spaced in memory), the nt
+  // input windows as one 4-D box (nt = 9: dy, dz = 0..2; nt = 3: dy =
+  // 0..2 at one dz) of a view with strides Wp and plane along dy and dz;
+  // the 4-D box is used where all its windows lie inside the array
+  int a3, b4;
+  long long b4_dim0;  // first-axis extent of the window view
+  // dY copies in K-tile blocks [tile][3][cout][64] (slbc_tc_cmajor_tiles):
+  // a0 boxes dpm * cout rows of a tile, a1 boxes cout rows
+  int a_tiles;
 };
 
 constexpr int kWgnMaxRows = 288;
@@ -777,7 +789,9 @@ int wgrad_n_ctas(const WgradNArgs &w) { return ((3 + w.dpm - 1) / w.dpm) * w.gro
 
 __global__ void __launch_bounds__(128, 1)
 k_wgrad_n(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap a1,
-          const __grid_constant__ CUtensorMap a2, const __grid_constant__ CUtensorMap tb, WgradNArgs w, int *err) {
+          const __grid_constant__ CUtensorMap a2, const __grid_constant__ CUtensorMap tb,
+          const __grid_constant__ CUtensorMap a_all, const __grid_constant__ CUtensorMap b_win, WgradNArgs w,
+          int *err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
   uint8_t *tA = smem_raw + pad;
@@ -790,10 +804,12 @@ k_wgrad_n(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtens
   const int g = (blockIdx.x / w.ci_chunks) % w.groups;
   const int mt = blockIdx.x / (w.ci_chunks * w.groups);
   const int ci0 = chunk * w.cc;
-  const long long per = (w.k_tiles + w.splits - 1) / w.splits;
-  const long long k_lo = (long long)blockIdx.z * per;
-  const long long k_hi = k_lo + per < w.k_tiles ? k_lo + per : w.k_tiles;
-  const int nk = k_hi > k_lo ? (int)(k_hi - k_lo) : 0;
+  // K tiles z, z + splits, z + 2 splits, ... (z = blockIdx.z): the blocks
+  // of one launch work through one run of consecutive tiles at a time, so
+  // the windows that other taps read again (up to a plane further on) are
+  // still in L2
+  const long long kz = blockIdx.z;
+  const int nk = kz < w.k_tiles ? (int)((w.k_tiles - kz + w.splits - 1) / w.splits) : 0;
   // bytes landing per stage: the dY copies and input windows actually loaded
   int a_blocks = 0, b_taps = 0;
   for (int d = 0; d < w.dpm; d++) a_blocks += mt * w.dpm + d < 3;
@@ -824,21 +840,38 @@ k_wgrad_n(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtens
         ok = false;
         break;
       }
-      const int k0 = (int)((k_lo + kt) * 64);
+      const int k0 = (int)((kz + (long long)kt * w.splits) * 64);
       tc::mbar_expect_tx(&full[s], bytes);
-      for (int d = 0; d < w.dpm; d++) {
-        const int dx = mt * w.dpm + d;
-        if (dx >= 3) break;
-        const CUtensorMap *am = dx == 0 ? &a0 : (dx == 1 ? &a1 : &a2);
-        tc::tma_load_2d(tA + s * kWgTileA + d * w.cout * 128, am, &full[s], k0, 0);
+      if (w.a_tiles) {
+        if (a_blocks == w.dpm) {
+          tc::tma_load_3d(tA + s * kWgTileA, &a0, &full[s], 0, mt * w.dpm * w.cout, k0 >> 6);
+        } else {
+          for (int d = 0; d < a_blocks; d++)
+            tc::tma_load_3d(tA + s * kWgTileA + d * w.cout * 128, &a1, &full[s], 0, (mt * w.dpm + d) * w.cout, k0 >> 6);
+        }
+      } else if (w.a3 && a_blocks == w.dpm) {
+        tc::tma_load_3d(tA + s * kWgTileA, &a_all, &full[s], k0, 0, mt * w.dpm);
+      } else {
+        for (int d = 0; d < w.dpm; d++) {
+          const int dx = mt * w.dpm + d;
+          if (dx >= 3) break;
+          const CUtensorMap *am = dx == 0 ? &a0 : (dx == 1 ? &a1 : &a2);
+          tc::tma_load_2d(tA + s * kWgTileA + d * w.cout * 128, am, &full[s], k0, 0);
+        }
       }
-      for (int t = 0; t < w.nt; t++) {
-        const int yz = g * w.nt + t;
-        if (yz >= 9) break;
-        const int dy = yz % 3, dz = yz / 3;
-        // may start before 0 or end past the array: TMA fills zeros there
-        const int x = k0 + (dy - 1) * w.Wp + (dz - 1) * w.plane;
-        tc::tma_load_2d(tB + s * tile_b + t * w.cc * 128, &tb, &full[s], x, ci0);
+      // first window of the group: dy = 0 at the group's first dz
+      const long long xw = (long long)k0 - w.Wp + ((g * w.nt) / 3 - 1) * (long long)w.plane;
+      if (w.b4 && b_taps == w.nt && xw >= 0 && xw + 64 <= w.b4_dim0) {
+        tc::tma_load_4d(tB + s * tile_b, &b_win, &full[s], (int)xw, ci0, 0, 0);
+      } else {
+        for (int t = 0; t < w.nt; t++) {
+          const int yz = g * w.nt + t;
+          if (yz >= 9) break;
+          const int dy = yz % 3, dz = yz / 3;
+          // may start before 0 or end past the array: TMA fills zeros there
+          const int x = k0 + (dy - 1) * w.Wp + (dz - 1) * w.plane;
+          tc::tma_load_2d(tB + s * tile_b + t * w.cc * 128, &tb, &full[s], x, ci0);
+        }
       }
       issued = kt + 1;
     }
@@ -910,13 +943,17 @@ __global__ void k_sum_splits(const float *partial, long long n, int splits, floa
 // Channel-major flat copy of channels [coff, coff + nch) of a padded
 // channels-last buffer: dst[c][n * pstride + (z * (H + 2) + y) * Wp + x] =
 // src[n][z][y][x - shift][coff + c] for 0 <= x - shift <= W + 1 (0 beyond;
-// zero_halo: interior voxels only, every halo position 0).  A block moves
+// zero_halo: interior voxels only, every halo position 0); with ncopy > 0
+// the 64-position rows go to K-tile blocks instead, dst[t][copy][c][64]
+// for t = flat position / 64 (the three x-shifted copies of an output
+// gradient side by side per tile: one contiguous 12 KB block of DRAM per
+// 32-channel tile for the weight gradient's A operand).  A block moves
 // 64 consecutive flat positions x 64 channels through shared memory, so
 // both the channel runs it reads and the position runs it writes are
 // 128-byte rows.
 __global__ void __launch_bounds__(256) k_cmajor(const __nv_bfloat16 *src, int B, int D, int H, int W, int ctot,
                                                 int coff, int nch, int Wp, long long pstride, int shift,
-                                                int zero_halo, __nv_bfloat16 *dst) {
+                                                int zero_halo, int copy, int ncopy, __nv_bfloat16 *dst) {
   __shared__ __nv_bfloat16 tile[64][64 + 8];
   const long long plane = (long long)(H + 2) * Wp;
   const long long per_sample = (long long)(D + 2) * plane;
@@ -955,7 +992,11 @@ __global__ void __launch_bounds__(256) k_cmajor(const __nv_bfloat16 *src, int B,
     // store: per channel 64 positions = 128 B, 16 B per thread access
     for (int a = threadIdx.x; a < 64 * 8; a += blockDim.x) {
       const int c = a / 8, pv = a % 8;
-      if (c < cw) *(uint4 *)(dst + (long long)(c0 + c) * total + t * 64 + pv * 8) = *(const uint4 *)&tile[c][pv * 8];
+      if (c >= cw) continue;
+      // channel-major row, or (ncopy > 0) row c of copy `copy` in the
+      // block of K tile t: [t][copy][c][64]
+      const long long o = ncopy ? ((t * ncopy + copy) * nch + c0 + c) * 64 : (long long)(c0 + c) * total + t * 64;
+      *(uint4 *)(dst + o + pv * 8) = *(const uint4 *)&tile[c][pv * 8];
     }
     __syncthreads();
   }
@@ -966,6 +1007,53 @@ bool make_map_k64(CUtensorMap *map, const void *ptr, long long rows, long long c
   return make_map_2d(map, ptr, rows, cols, box_rows);
 }
 
+// 3 equally spaced copies (copy_bytes apart) of rows x cols BF16: box of 64
+// columns x rows x ncopy copies
+bool make_map_copies(CUtensorMap *map, const void *ptr, long long rows, long long cols, long long copy_bytes,
+                     int ncopy) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)cols * 2, (cuuint64_t)copy_bytes};
+  const cuuint32_t box[3] = {64, (cuuint32_t)rows, (cuuint32_t)ncopy};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// K-tile blocks [ntiles][rows][64] BF16: box of 64 x box_rows x 1
+bool make_map_tiles(CUtensorMap *map, const void *ptr, long long rows, long long ntiles, int box_rows) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {64, (cuuint64_t)rows, (cuuint64_t)ntiles};
+  const cuuint64_t strides[2] = {128, (cuuint64_t)rows * 128};
+  const cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Shifted windows of rows x cols BF16 (row-major, channel rows): element
+// (x, c, dy, dz) = ptr[c * cols + x + dy * Wp + dz * plane]; the first axis
+// ends (ny - 1) * Wp + (nz - 1) * plane short of cols, so no window reaches
+// past its row.  Box: 64 x box_rows x ny x nz.
+bool make_map_windows(CUtensorMap *map, const void *ptr, long long rows, long long cols, int Wp, long long plane,
+                      int box_rows, int ny, int nz, long long &dim0) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return false;
+  dim0 = cols - (ny - 1) * (long long)Wp - (nz - 1) * plane;
+  if (dim0 < 64) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)dim0, (cuuint64_t)rows, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[3] = {(cuuint64_t)cols * 2, (cuuint64_t)Wp * 2, (cuuint64_t)plane * 2};
+  const cuuint32_t box[4] = {64, (cuuint32_t)box_rows, (cuuint32_t)ny, (cuuint32_t)nz};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // M tile of 128 voxels for a D x H x W grid: false when the grid does not
 // tile (sides powers of two with W * H * D >= 128 do)
 bool tile_shape(int D, int H, int W, int &wbox, int &hbox, int &dbox) {
@@ -974,6 +1062,130 @@ bool tile_shape(int D, int H, int W, int &wbox, int &hbox, int &dbox) {
   dbox = 128 / (wbox * hbox);
   return wbox * hbox * dbox == 128 && W % wbox == 0 && H % hbox == 0 && D % dbox == 0 && wbox <= 256 &&
          hbox <= 256 && dbox <= 256;
+}
+
+int cmajor_launch(const char *who, const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
+                  long long pstride, int shift, int zero_halo, int copy, int ncopy, void *dst, void *stream) {
+  if (B < 1 || nch < 1 || coff < 0 || coff + nch > ctot || Wp < W + 2 || Wp % 8 || pstride % 64 ||
+      pstride < (long long)(D + 2) * (H + 2) * Wp || shift < -1 || shift > 1)
+    return slbc::set_error(std::string(who) + ": bad geometry"), 1;
+  if (nch % 8 || coff % 8 || ctot % 8 || !aligned16(src) || !aligned16(dst))
+    return slbc::set_error(std::string(who) + ": channels in multiples of 8, 16-byte aligned buffers"), 1;
+  const long long work = (long long)B * pstride / 64 * ((nch + 63) / 64);
+  const int blocks = (int)std::min<long long>(work, 152LL * 16);
+  k_cmajor<<<blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, B, D, H, W, ctot, coff, nch, Wp,
+                                                     pstride, shift, zero_halo, copy, ncopy, (__nv_bfloat16 *)dst);
+  slbc::count_launch();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(std::string(who) + ": " + cudaGetErrorString(e)), 1;
+  return 0;
+}
+
+// Both weight-gradient entry points: dY as three channel-major copies (dy0,
+// dy1, dy2) or, with dyt, as K-tile blocks of the three copies.
+int wgrad_launch(const char *who, const void *dy0, const void *dy1, const void *dy2, const void *dyt, const void *xt,
+                 int B, int D, int H, int W, int Wp, long long pstride, int cin, int cout, float *partial,
+                 long long partial_floats, int splits, float *dw, void *stream) {
+  const std::string me(who);
+  WgradArgs w;
+  if (cout < 32 || (cout > 128 && cout % 128) || (cout <= 128 && 128 % cout) || cin < 16 || cin % 16)
+    return slbc::set_error(me + ": cout must be 32, 64, 128 or a multiple of 128; cin a multiple of 16"), 1;
+  if (Wp < W + 2 || Wp % 8 || pstride % 64 || pstride < (long long)(D + 2) * (H + 2) * Wp || splits < 1)
+    return slbc::set_error(me + ": bad geometry"), 1;
+  if (partial_floats < (long long)splits * 27 * cout * cin)
+    return slbc::set_error(me + ": partial buffer too small"), 1;
+  if (dyt) dy0 = dy1 = dy2 = dyt;
+  if (!aligned16(dy0) || !aligned16(dy1) || !aligned16(dy2) || !aligned16(xt) || !aligned16(partial) ||
+      !aligned16(dw))
+    return slbc::set_error(me + ": buffers must be 16-byte aligned"), 1;
+  const long long cols = (long long)B * pstride;
+  WgradNArgs wn;
+  const bool plan_n = wgrad_n_plan(cin, cout, wn);
+  if (dyt && !plan_n) return slbc::set_error(me + ": K-tile blocks need cout 32, 64 or 128"), 1;
+  if (plan_n) {  // taps stacked along N
+    wn.Wp = Wp;
+    wn.plane = (H + 2) * Wp;
+    wn.k_tiles = cols / 64;
+    wn.splits = splits;
+    wn.partial = partial;
+    int *err = tc_err_flag();
+    if (!err) return slbc::set_error(me + ": no device error flag"), 1;
+    CUtensorMap m0, m1, m2, mb;
+    wn.a_tiles = dyt != nullptr;
+    if (wn.a_tiles) {
+      if (!make_map_tiles(&m0, dyt, 3LL * cout, wn.k_tiles, wn.dpm * cout) ||
+          !make_map_tiles(&m1, dyt, 3LL * cout, wn.k_tiles, cout) || !make_map_k64(&mb, xt, cin, cols, wn.cc))
+        return slbc::set_error(me + ": tensor map encoding failed"), 1;
+      m2 = m0;
+    } else if (!make_map_k64(&m0, dy0, cout, cols, cout) || !make_map_k64(&m1, dy1, cout, cols, cout) ||
+               !make_map_k64(&m2, dy2, cout, cols, cout) || !make_map_k64(&mb, xt, cin, cols, wn.cc)) {
+      return slbc::set_error(me + ": tensor map encoding failed"), 1;
+    }
+    // single-box forms (each falls back to the per-copy / per-tap boxes
+    // when its map cannot be made)
+    CUtensorMap ma = m0, mw = mb;
+    const long long cstride = (const char *)dy1 - (const char *)dy0;
+    wn.a3 = !wn.a_tiles && wn.dpm > 1 && cstride >= (long long)cout * cols * 2 && cstride % 16 == 0 &&
+            (const char *)dy2 - (const char *)dy1 == cstride && make_map_copies(&ma, dy0, cout, cols, cstride, wn.dpm);
+    wn.b4_dim0 = 0;
+    wn.b4 = (wn.nt == 9 || wn.nt == 3) &&
+            make_map_windows(&mw, xt, cin, cols, Wp, wn.plane, wn.cc, 3, wn.nt / 3, wn.b4_dim0);
+    if (!wn.a3) ma = m0;
+    if (!wn.b4) mw = mb;
+    static unsigned long long attr_n_done = 0;
+    cudaError_t e = smem_opt_in((const void *)k_wgrad_n, kWgnSmem, attr_n_done);
+    if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+    const dim3 grid((unsigned)wgrad_n_ctas(wn), 1, (unsigned)splits);
+    const int smem = kStages * (kWgTileA + wn.n_rows * 128) + 1024;
+    k_wgrad_n<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, ma, mw, wn, err);
+    slbc::count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+    const long long n = 27LL * cout * cin;
+    k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
+        partial, n, splits, dw);
+    slbc::count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+    return 0;
+  }
+  w.cin = cin; w.cout = cout;
+  w.co_rows = cout < 128 ? cout : 128;
+  w.taps_per_tile = 128 / w.co_rows;
+  w.co_tiles = cout / w.co_rows;
+  w.ntile = cin;
+  while (w.ntile > 256) w.ntile /= 2;
+  if (cin % w.ntile || w.ntile % 16) return slbc::set_error(me + ": cin does not split into N tiles"), 1;
+  w.Wp = Wp;
+  w.plane = (H + 2) * Wp;
+  w.k_tiles = (long long)B * pstride / 64;
+  w.splits = splits;
+  w.tmem_cols = 32;
+  while (w.tmem_cols < w.ntile) w.tmem_cols *= 2;
+  w.partial = partial;
+  int *err = tc_err_flag();
+  if (!err) return slbc::set_error(me + ": no device error flag"), 1;
+  CUtensorMap m0, m1, m2, mb;
+  if (!make_map_k64(&m0, dy0, cout, cols, w.co_rows) || !make_map_k64(&m1, dy1, cout, cols, w.co_rows) ||
+      !make_map_k64(&m2, dy2, cout, cols, w.co_rows) || !make_map_k64(&mb, xt, cin, cols, w.ntile))
+    return slbc::set_error(me + ": tensor map encoding failed"), 1;
+  static unsigned long long attr_done = 0;
+  cudaError_t e = smem_opt_in((const void *)k_wgrad, kWgSmem, attr_done);
+  if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+  const dim3 grid((unsigned)(((27 + w.taps_per_tile - 1) / w.taps_per_tile) * w.co_tiles), (unsigned)(cin / w.ntile),
+                  (unsigned)splits);
+  const int smem = kStages * (kWgTileA + w.ntile * 128) + 1024;
+  k_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, w, err);
+  slbc::count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+  const long long n = 27LL * cout * cin;
+  k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
+      partial, n, splits, dw);
+  slbc::count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return slbc::set_error(me + ": " + cudaGetErrorString(e)), 1;
+  return 0;
 }
 
 }  // namespace
@@ -1103,19 +1315,16 @@ int slbc_tc_halo(void *buf, int B, int D, int H, int W, int ctot, int coff, int 
 
 int slbc_tc_cmajor(const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
                    long long pstride, int shift, int zero_halo, void *dst, void *stream) {
-  if (B < 1 || nch < 1 || coff < 0 || coff + nch > ctot || Wp < W + 2 || Wp % 8 || pstride % 64 ||
-      pstride < (long long)(D + 2) * (H + 2) * Wp || shift < -1 || shift > 1)
-    return slbc::set_error("slbc_tc_cmajor: bad geometry"), 1;
-  if (nch % 8 || coff % 8 || ctot % 8 || !aligned16(src) || !aligned16(dst))
-    return slbc::set_error("slbc_tc_cmajor: channels in multiples of 8, 16-byte aligned buffers"), 1;
-  const long long work = (long long)B * pstride / 64 * ((nch + 63) / 64);
-  const int blocks = (int)std::min<long long>(work, 152LL * 16);
-  k_cmajor<<<blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)src, B, D, H, W, ctot, coff, nch, Wp,
-                                                     pstride, shift, zero_halo, (__nv_bfloat16 *)dst);
-  slbc::count_launch();
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_cmajor: ") + cudaGetErrorString(e)), 1;
-  return 0;
+  return cmajor_launch("slbc_tc_cmajor", src, B, D, H, W, ctot, coff, nch, Wp, pstride, shift, zero_halo, 0, 0, dst,
+                       stream);
+}
+
+int slbc_tc_cmajor_tiles(const void *src, int B, int D, int H, int W, int ctot, int coff, int nch, int Wp,
+                         long long pstride, int shift, int copy, int ncopy, void *dst, void *stream) {
+  if (ncopy < 1 || copy < 0 || copy >= ncopy)
+    return slbc::set_error("slbc_tc_cmajor_tiles: copy must lie in [0, ncopy)"), 1;
+  return cmajor_launch("slbc_tc_cmajor_tiles", src, B, D, H, W, ctot, coff, nch, Wp, pstride, shift, 0, copy, ncopy,
+                       dst, stream);
 }
 
 int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_splits) {
@@ -1124,15 +1333,17 @@ int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_spl
     sms = 152;
   WgradNArgs wn;
   long long want;
+  // as many splits as fill the SMs in one wave: a block left over for a
+  // second wave would take as long as the whole first one
   if (wgrad_n_plan(cin, cout, wn)) {
     const int ctas = wgrad_n_ctas(wn);  // one block per SM
-    want = (sms + ctas - 1) / ctas;
+    want = sms / ctas;
   } else {  // two blocks per SM
     const int co_rows = cout < 128 ? cout : 128;
     int ntile = cin;
     while (ntile > 256) ntile /= 2;
     const int blocks = ((27 + 128 / co_rows - 1) / (128 / co_rows)) * (cout / co_rows) * (cin / ntile);
-    want = 2 * sms / blocks + 1;
+    want = 2 * sms / blocks;
   }
   want = std::min(want, std::max(1LL, k_tiles / 8));
   want = std::min(want, max_splits);
@@ -1142,84 +1353,16 @@ int slbc_tc_wgrad_splits(int cin, int cout, long long k_tiles, long long max_spl
 int slbc_tc_wgrad(const void *dy0, const void *dy1, const void *dy2, const void *xt, int B, int D, int H, int W,
                   int Wp, long long pstride, int cin, int cout, float *partial, long long partial_floats, int splits,
                   float *dw, void *stream) {
-  WgradArgs w;
-  if (cout < 32 || (cout > 128 && cout % 128) || (cout <= 128 && 128 % cout) || cin < 16 || cin % 16)
-    return slbc::set_error("slbc_tc_wgrad: cout must be 32, 64, 128 or a multiple of 128; cin a multiple of 16"), 1;
-  if (Wp < W + 2 || Wp % 8 || pstride % 64 || pstride < (long long)(D + 2) * (H + 2) * Wp || splits < 1)
-    return slbc::set_error("slbc_tc_wgrad: bad geometry"), 1;
-  if (partial_floats < (long long)splits * 27 * cout * cin)
-    return slbc::set_error("slbc_tc_wgrad: partial buffer too small"), 1;
-  if (!aligned16(dy0) || !aligned16(dy1) || !aligned16(dy2) || !aligned16(xt) || !aligned16(partial) ||
-      !aligned16(dw))
-    return slbc::set_error("slbc_tc_wgrad: buffers must be 16-byte aligned"), 1;
-  const long long cols = (long long)B * pstride;
-  WgradNArgs wn;
-  if (wgrad_n_plan(cin, cout, wn)) {  // taps stacked along N
-    wn.Wp = Wp;
-    wn.plane = (H + 2) * Wp;
-    wn.k_tiles = cols / 64;
-    wn.splits = splits;
-    wn.partial = partial;
-    int *err = tc_err_flag();
-    if (!err) return slbc::set_error("slbc_tc_wgrad: no device error flag"), 1;
-    CUtensorMap m0, m1, m2, mb;
-    if (!make_map_k64(&m0, dy0, cout, cols, cout) || !make_map_k64(&m1, dy1, cout, cols, cout) ||
-        !make_map_k64(&m2, dy2, cout, cols, cout) || !make_map_k64(&mb, xt, cin, cols, wn.cc))
-      return slbc::set_error("slbc_tc_wgrad: tensor map encoding failed"), 1;
-    static unsigned long long attr_n_done = 0;
-    cudaError_t e = smem_opt_in((const void *)k_wgrad_n, kWgnSmem, attr_n_done);
-    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-    const dim3 grid((unsigned)wgrad_n_ctas(wn), 1, (unsigned)splits);
-    const int smem = kStages * (kWgTileA + wn.n_rows * 128) + 1024;
-    k_wgrad_n<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, wn, err);
-    slbc::count_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-    const long long n = 27LL * cout * cin;
-    k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
-        partial, n, splits, dw);
-    slbc::count_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-    return 0;
-  }
-  w.cin = cin; w.cout = cout;
-  w.co_rows = cout < 128 ? cout : 128;
-  w.taps_per_tile = 128 / w.co_rows;
-  w.co_tiles = cout / w.co_rows;
-  w.ntile = cin;
-  while (w.ntile > 256) w.ntile /= 2;
-  if (cin % w.ntile || w.ntile % 16) return slbc::set_error("slbc_tc_wgrad: cin does not split into N tiles"), 1;
-  w.Wp = Wp;
-  w.plane = (H + 2) * Wp;
-  w.k_tiles = (long long)B * pstride / 64;
-  w.splits = splits;
-  w.tmem_cols = 32;
-  while (w.tmem_cols < w.ntile) w.tmem_cols *= 2;
-  w.partial = partial;
-  int *err = tc_err_flag();
-  if (!err) return slbc::set_error("slbc_tc_wgrad: no device error flag"), 1;
-  CUtensorMap m0, m1, m2, mb;
-  if (!make_map_k64(&m0, dy0, cout, cols, w.co_rows) || !make_map_k64(&m1, dy1, cout, cols, w.co_rows) ||
-      !make_map_k64(&m2, dy2, cout, cols, w.co_rows) || !make_map_k64(&mb, xt, cin, cols, w.ntile))
-    return slbc::set_error("slbc_tc_wgrad: tensor map encoding failed"), 1;
-  static unsigned long long attr_done = 0;
-  cudaError_t e = smem_opt_in((const void *)k_wgrad, kWgSmem, attr_done);
-  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-  const dim3 grid((unsigned)(((27 + w.taps_per_tile - 1) / w.taps_per_tile) * w.co_tiles), (unsigned)(cin / w.ntile),
-                  (unsigned)splits);
-  const int smem = kStages * (kWgTileA + w.ntile * 128) + 1024;
-  k_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(m0, m1, m2, mb, w, err);
-  slbc::count_launch();
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-  const long long n = 27LL * cout * cin;
-  k_sum_splits<<<(int)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, (cudaStream_t)stream>>>(
-      partial, n, splits, dw);
-  slbc::count_launch();
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return slbc::set_error(std::string("slbc_tc_wgrad: ") + cudaGetErrorString(e)), 1;
-  return 0;
+  return wgrad_launch("slbc_tc_wgrad", dy0, dy1, dy2, nullptr, xt, B, D, H, W, Wp, pstride, cin, cout, partial,
+                      partial_floats, splits, dw, stream);
+}
+
+int slbc_tc_wgrad_tiles(const void *dyt, const void *xt, int B, int D, int H, int W, int Wp, long long pstride,
+                        int cin, int cout, float *partial, long long partial_floats, int splits, float *dw,
+                        void *stream) {
+  if (!dyt) return slbc::set_error("slbc_tc_wgrad_tiles: no dY blocks"), 1;
+  return wgrad_launch("slbc_tc_wgrad_tiles", nullptr, nullptr, nullptr, dyt, xt, B, D, H, W, Wp, pstride, cin, cout,
+                      partial, partial_floats, splits, dw, stream);
 }
 
 // Synchronises the device and returns (and clears) the tensor-core kernels'

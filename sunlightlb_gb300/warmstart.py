@@ -49,6 +49,8 @@ class Kernels:
             "slbc_tc_halo": [p] + [i] * 7 + [p],
             "slbc_tc_cmajor": [p] + [i] * 8 + [ll, i, i, p, p],
             "slbc_tc_wgrad": [p] * 4 + [i] * 5 + [ll, i, i, p, ll, i, p, p],
+            "slbc_tc_cmajor_tiles": [p] + [i] * 8 + [ll, i, i, i, p, p],
+            "slbc_tc_wgrad_tiles": [p] * 2 + [i] * 5 + [ll, i, i, p, ll, i, p, p],
             "slbc_nn_pool": [p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_pool_bwd": [p, i, i, p, i, i, p, i, i, p, i, i] + [i] * 5 + [p],
             "slbc_nn_up": [p, i, i, p, i, i] + [i] * 5 + [p],
@@ -249,7 +251,9 @@ class UNet:
         Wp, ps = flat_geometry(self.D, self.H, self.W)
         maxc = max(c for _, c in self.buf_spec.values())
         self.cm_x = torch.empty(maxc * self.B * ps, device=self.dev, dtype=torch.bfloat16)
-        self.cm_g = [torch.empty(w3 * self.B * ps, device=self.dev, dtype=torch.bfloat16) for _ in range(3)]
+        # the three x-shifted copies of an output gradient: K-tile blocks
+        # (cout <= 128), else three equally spaced channel-major copies
+        self.cm_g = torch.empty(3 * w3 * self.B * ps, device=self.dev, dtype=torch.bfloat16)
         self.ws_floats = 1 << 26
         self.ws = torch.empty(self.ws_floats, device=self.dev, dtype=torch.float32)
         self.loss_acc = torch.zeros(1, device=self.dev, dtype=torch.float64)
@@ -268,16 +272,27 @@ class UNet:
         Wp, ps = flat_geometry(d, h, w)
         g = self.grad[g_name]
         x = self.buf[x_name]
-        for c, shift in zip(self.cm_g, (-1, 0, 1)):
-            k.tc_cmajor(g.data_ptr(), self.B, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0, c.data_ptr(),
-                        self.stream)
+        tiles = cout <= 128
+        n = cout * self.B * ps
+        cm_g = [self.cm_g[i * n:(i + 1) * n] for i in range(3)]
+        for i, shift in enumerate((-1, 0, 1)):
+            if tiles:
+                k.tc_cmajor_tiles(g.data_ptr(), self.B, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, i, 3,
+                                  self.cm_g.data_ptr(), self.stream)
+            else:
+                k.tc_cmajor(g.data_ptr(), self.B, d, h, w, g.shape[-1], 0, cout, Wp, ps, shift, 0,
+                            cm_g[i].data_ptr(), self.stream)
         k.tc_cmajor(x.data_ptr(), self.B, d, h, w, x.shape[-1], x_coff, cin, Wp, ps, 0, 1, self.cm_x.data_ptr(),
                     self.stream)
         splits = k.tc_wgrad_splits(cin, cout, self.B * ps // 64, self.ws_floats // (27 * cout * cin))
         p = self.params[name]
-        k.tc_wgrad(self.cm_g[0].data_ptr(), self.cm_g[1].data_ptr(), self.cm_g[2].data_ptr(), self.cm_x.data_ptr(),
-                   self.B, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats, splits,
-                   p["gw"].data_ptr(), self.stream)
+        if tiles:
+            k.tc_wgrad_tiles(self.cm_g.data_ptr(), self.cm_x.data_ptr(), self.B, d, h, w, Wp, ps, cin, cout,
+                             self.ws.data_ptr(), self.ws_floats, splits, p["gw"].data_ptr(), self.stream)
+        else:
+            k.tc_wgrad(cm_g[0].data_ptr(), cm_g[1].data_ptr(), cm_g[2].data_ptr(), self.cm_x.data_ptr(),
+                       self.B, d, h, w, Wp, ps, cin, cout, self.ws.data_ptr(), self.ws_floats, splits,
+                       p["gw"].data_ptr(), self.stream)
         p["gb"].zero_()
         k.nn_bias_grad(g.data_ptr(), g.shape[-1], 0, self.B, d, h, w, cout, p["gb"].data_ptr(), self.stream)
 
@@ -707,8 +722,9 @@ def conv_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
 
 
 def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
-    """Weight-gradient time (slbc_tc_wgrad alone, from ready channel-major
-    copies; the split sum included) of every layer shape of the network on
+    """Weight-gradient time (slbc_tc_wgrad_tiles for cout <= 128, else
+    slbc_tc_wgrad, alone, from ready copies of dY and X; the split sum
+    included) of every layer shape of the network on
     `batch` grids of side^3, CUDA events over `reps` calls on random BF16
     data: [(level, cin, cout, splits, ms, TFLOP/s)], FLOPs 2 * 27 * cin *
     cout * interior voxels."""
@@ -726,17 +742,20 @@ def wgrad_layer_times(lib, side, batch, widths=(32, 64, 128, 256), reps=20):
         d = side >> lv
         Wp, ps = flat_geometry(d, d, d)
         xt = torch.randn(cin, batch * ps, device=dev).to(torch.bfloat16)
-        dys = [torch.randn(cout, batch * ps, device=dev).to(torch.bfloat16) for _ in range(3)]
+        dys = torch.randn(3, cout, batch * ps, device=dev).to(torch.bfloat16)
         dw = torch.empty(27 * cout * cin, device=dev, dtype=torch.float32)
         splits = k.tc_wgrad_splits(cin, cout, batch * ps // 64, ws_floats // (27 * cout * cin))
-        args = (dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), batch, d, d, d, Wp, ps, cin,
-                cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), stream)
+        tail = (batch, d, d, d, Wp, ps, cin, cout, ws.data_ptr(), ws_floats, splits, dw.data_ptr(), stream)
+        if cout <= 128:  # K-tile blocks, as UNet lays them out
+            fn, args = k.tc_wgrad_tiles, (dys.data_ptr(), xt.data_ptr()) + tail
+        else:
+            fn, args = k.tc_wgrad, (dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr()) + tail
         for _ in range(3):
-            k.tc_wgrad(*args)
+            fn(*args)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            k.tc_wgrad(*args)
+            fn(*args)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps

@@ -137,7 +137,14 @@ def wgrad_fns(gpu):
     wg.restype = C.c_int
     wg.argtypes = [C.c_void_p] * 4 + [C.c_int] * 5 + [C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
                                                      C.c_int, C.c_void_p, C.c_void_p]
-    return cm, wg
+    cmt = gpu.dll.slbc_tc_cmajor_tiles
+    cmt.restype = C.c_int
+    cmt.argtypes = [C.c_void_p] + [C.c_int] * 8 + [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    wgt = gpu.dll.slbc_tc_wgrad_tiles
+    wgt.restype = C.c_int
+    wgt.argtypes = [C.c_void_p] * 2 + [C.c_int] * 5 + [C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
+                                                       C.c_int, C.c_void_p, C.c_void_p]
+    return cm, wg, cmt, wgt
 
 
 def flat_geometry(D, H, W):
@@ -162,12 +169,40 @@ WGRAD_CASES = [  # B, D, H, W, cin, cout, splits
 ]
 
 
+@pytest.mark.parametrize("B,D,H,W,nch", [(1, 8, 8, 8, 32), (2, 8, 16, 8, 128)])
+def test_cmajor_tiles_layout(gpu, B, D, H, W, nch):
+    """slbc_tc_cmajor_tiles writes the same rows as slbc_tc_cmajor, regrouped
+    as [tile][copy][channel][64]."""
+    torch = pytest.importorskip("torch")
+    _, halo = conv_fns(gpu)
+    cm, _, cmt, _ = wgrad_fns(gpu)
+    g = torch.Generator(device="cuda").manual_seed(B * 100 + nch)
+    y = torch.randn(B, nch, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
+    st = torch.cuda.current_stream().cuda_stream
+    yb = to_padded(torch, y, nch, 0)
+    assert halo(yb.data_ptr(), B, D, H, W, nch, 0, nch, st) == 0
+    Wp, pstride = flat_geometry(D, H, W)
+    cols = B * pstride
+    plain = torch.empty(3, nch, cols, device="cuda", dtype=torch.bfloat16)
+    tiles = torch.full((cols // 64, 3, nch, 64), 7.0, device="cuda", dtype=torch.bfloat16)
+    for i, shift in enumerate((-1, 0, 1)):
+        assert cm(yb.data_ptr(), B, D, H, W, nch, 0, nch, Wp, pstride, shift, 0, plain[i].data_ptr(), st) == 0
+        assert cmt(yb.data_ptr(), B, D, H, W, nch, 0, nch, Wp, pstride, shift, i, 3, tiles.data_ptr(), st) == 0
+    torch.cuda.synchronize()
+    want = plain.view(3, nch, cols // 64, 64).permute(2, 0, 1, 3)
+    assert torch.equal(tiles, want)
+
+
+@pytest.mark.parametrize("layout", ["copies_apart", "copies_one_buffer", "tiles"])
 @pytest.mark.parametrize("case", WGRAD_CASES)
-def test_wgrad_matches_torch(gpu, case):
+def test_wgrad_matches_torch(gpu, case, layout):
+    """Against torch's weight gradient, with dY's three copies in separate
+    allocations, equally spaced in one (one TMA box per stage for them), or
+    as K-tile blocks (slbc_tc_cmajor_tiles + slbc_tc_wgrad_tiles)."""
     torch = pytest.importorskip("torch")
     F = torch.nn.functional
     _, halo = conv_fns(gpu)
-    cm, wg = wgrad_fns(gpu)
+    cm, wg, cmt, wgt = wgrad_fns(gpu)
     B, D, H, W, cin, cout, splits = case
     g = torch.Generator(device="cuda").manual_seed(sum(case) + 11)
     x = torch.randn(B, cin, D, H, W, device="cuda", generator=g).to(torch.bfloat16).float()
@@ -180,15 +215,26 @@ def test_wgrad_matches_torch(gpu, case):
     Wp, pstride = flat_geometry(D, H, W)
     xt = torch.empty(cin, B * pstride, device="cuda", dtype=torch.bfloat16)
     assert cm(xb.data_ptr(), B, D, H, W, cin, 0, cin, Wp, pstride, 0, 1, xt.data_ptr(), st) == 0
+    if layout == "tiles" and cout > 128:
+        pytest.skip("K-tile blocks: cout 32, 64 or 128")
     dys = []
-    for shift in (-1, 0, 1):
-        t = torch.empty(cout, B * pstride, device="cuda", dtype=torch.bfloat16)
+    whole = torch.empty(3, cout, B * pstride, device="cuda", dtype=torch.bfloat16)
+    for i, shift in enumerate((-1, 0, 1)):
+        if layout == "tiles":
+            assert cmt(yb.data_ptr(), B, D, H, W, cout, 0, cout, Wp, pstride, shift, i, 3, whole.data_ptr(), st) == 0
+            continue
+        t = whole[i] if layout == "copies_one_buffer" else torch.empty(cout, B * pstride, device="cuda",
+                                                                      dtype=torch.bfloat16)
         assert cm(yb.data_ptr(), B, D, H, W, cout, 0, cout, Wp, pstride, shift, 0, t.data_ptr(), st) == 0
         dys.append(t)
     partial = torch.empty(splits * 27 * cout * cin, device="cuda")
     dw = torch.empty(27, cout, cin, device="cuda")
-    rc = wg(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), B, D, H, W, Wp, pstride, cin,
-            cout, partial.data_ptr(), partial.numel(), splits, dw.data_ptr(), st)
+    if layout == "tiles":
+        rc = wgt(whole.data_ptr(), xt.data_ptr(), B, D, H, W, Wp, pstride, cin, cout, partial.data_ptr(),
+                 partial.numel(), splits, dw.data_ptr(), st)
+    else:
+        rc = wg(dys[0].data_ptr(), dys[1].data_ptr(), dys[2].data_ptr(), xt.data_ptr(), B, D, H, W, Wp, pstride,
+                cin, cout, partial.data_ptr(), partial.numel(), splits, dw.data_ptr(), st)
     assert rc == 0, gpu.dll.slbc_last_error
     assert gpu.dll.slbc_tc_status() == 0
     ref = torch.nn.grad.conv3d_weight(F.pad(x, (1, 1, 1, 1, 1, 1), mode="circular"), (cout, cin, 3, 3, 3), dy)
