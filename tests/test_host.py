@@ -262,3 +262,31 @@ def test_host_parallel_ranges_cover_once(gpu):
             assert lo == covered and hi >= lo, (n, seen)
             covered = hi
         assert covered == n, (n, seen)
+
+
+def test_wgrad_splits_fill_one_wave(gpu):
+    """slbc_tc_wgrad_splits (host logic): for every layer shape of the
+    network the K splits times the blocks per split fit the 152 SMs of a
+    GB300 in one wave (one block per SM for cout <= 128, two for the
+    256-channel layers); a block left over for a second wave doubles the
+    launch.  Without a device the function assumes 152 SMs."""
+    import ctypes as C
+    if gpu.dll.slbc_device_count() > 0:
+        pytest.skip("a GPU is present: the split count follows its SM count")
+    f = gpu.dll.slbc_tc_wgrad_splits
+    f.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong]
+    f.restype = C.c_int
+    big = 1 << 40
+    # (cin, cout): (splits, blocks per split)
+    want = {(32, 32): (152, 1), (96, 32): (50, 3), (32, 64): (76, 2), (64, 64): (25, 6), (192, 64): (8, 18),
+            (64, 128): (16, 9), (128, 128): (10, 15), (384, 128): (2, 54), (128, 256): (5, 54),
+            (256, 256): (5, 54)}
+    for (cin, cout), (splits, blocks) in want.items():
+        got = f(cin, cout, big, big)
+        assert got == splits, (cin, cout, got)
+        per_sm = 2 if cout > 128 else 1
+        assert got * blocks <= 152 * per_sm < (got + 1) * blocks, (cin, cout)
+    # capped by the K tiles (at least 8 per split) and by the partial buffer
+    assert f(32, 32, 80, big) == 10
+    assert f(32, 32, big, 7) == 7
+    assert f(32, 32, 3, big) == 1
