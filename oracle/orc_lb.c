@@ -3,7 +3,7 @@
  *
  * CPU restatement of the SunlightLB reference algorithm for the lattice
  * Boltzmann update path (setup, link bounce-back, streaming, collision,
- * measurement).  It is the checker for the GPU library, never part of it:
+ * measurement).  The GPU library is tested against it; it is never part of it:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs load
  * it.  It exports the same C API names and struct layout as the library
  * (include/sunlightlb.h), so one ctypes driver runs the library, this oracle
