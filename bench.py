@@ -1063,6 +1063,8 @@ def run_warmstart(args):
                 vs, ds = WS.predict_velocity(inf, sdev, force, WS.ETA_TAU1, force_shift=1.0), None
             elif name == "no_plane_flux":  # the state as decoded, without the plane-flux correction
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, plane_flux=False)
+            elif name == "cross_flux":  # the warm state with its y and z plane fluxes made uniform too
+                vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, cross_flux=True)
             elif name == "plane_flux_velocity":  # the plane-flux velocity scaling without its pressure
                 vs, ds = WS.predict_state(inf, sdev, force, WS.ETA_TAU1, plane_flux=False)
                 work = torch.empty(3 * ev_side + 1, device="cuda", dtype=torch.float64)

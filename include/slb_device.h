@@ -401,6 +401,12 @@ int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, in
  * applied). */
 int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D, int H, int W, float force,
                        float gain, double *work, void *stream);
+/* Cross fluxes of the same state made uniform: the flux of u_y through
+ * every y plane (u_z through every z plane) set to its mean by adding
+ * delta(plane) |u| to the component (|u| of the state before: zero in
+ * solids and at walls).  u: 3 x D*H*W, z the fastest index; work: 3 (H + W)
+ * doubles. */
+int slbc_nn_cross_flux(float *u, int D, int H, int W, double *work, void *stream);
 
 /* Mean-flow sums of slbc_vsum over buffers the caller owns, allocating no
  * device memory.  For callers that cannot call cudaMalloc where they need

@@ -500,6 +500,69 @@ __global__ void k_plane_apply(float *u, float *drho, const unsigned char *solid,
   }
 }
 
+// Uniform cross fluxes: the flux of u_y through every y plane (and of u_z
+// through every z plane) made equal to its mean, as mass conservation
+// requires of a steady periodic flow, by adding delta(plane) * |u| to the
+// component (|u| taken before: zero at walls and in solids, so no slip is
+// made).  u: 3 x D*H*W, x the slowest index, z the fastest.  work: q[H + W]
+// (plane fluxes, y planes then z planes), m[H + W] (plane sums of |u|),
+// delta[H + W].  One block per plane, a fixed summation order.
+__global__ void __launch_bounds__(256) k_cross_sum(const float *u, int D, int H, int W, double *work) {
+  __shared__ double sq[256], sm[256];
+  const int b = blockIdx.x;
+  const bool ydir = b < H;
+  const int c = ydir ? b : b - H;
+  const long long total = (long long)D * H * W;
+  const long long n = ydir ? (long long)D * W : (long long)D * H;
+  double aq = 0.0, am = 0.0;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    long long e;
+    if (ydir) e = ((t / W) * H + c) * W + t % W;  // t = i * W + k
+    else e = t * W + c;                           // t = i * H + j
+    const float ux = u[e], uy = u[total + e], uz = u[2 * total + e];
+    aq += (double)(ydir ? uy : uz);
+    am += sqrt((double)ux * ux + (double)uy * uy + (double)uz * uz);
+  }
+  sq[threadIdx.x] = aq;
+  sm[threadIdx.x] = am;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sq[threadIdx.x] += sq[threadIdx.x + o];
+      sm[threadIdx.x] += sm[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    work[b] = sq[0];
+    work[H + W + b] = sm[0];
+  }
+}
+
+__global__ void k_cross_fix(int H, int W, double *work) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double *q = work, *m = work + H + W;
+  double *delta = work + 2 * (H + W);
+  double my = 0.0, mz = 0.0;
+  for (int j = 0; j < H; j++) my += q[j];
+  for (int k = 0; k < W; k++) mz += q[H + k];
+  my /= H;
+  mz /= W;
+  for (int b = 0; b < H + W; b++) delta[b] = m[b] > 0.0 ? ((b < H ? my : mz) - q[b]) / m[b] : 0.0;
+}
+
+__global__ void k_cross_apply(float *u, int D, int H, int W, const double *work) {
+  const long long total = (long long)D * H * W;
+  const double *delta = work + 2 * (H + W);
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % W), j = (int)((e / W) % H);
+    const float ux = u[e], uy = u[total + e], uz = u[2 * total + e];
+    const double sp = sqrt((double)ux * ux + (double)uy * uy + (double)uz * uz);
+    u[total + e] = (float)(uy + delta[j] * sp);
+    u[2 * total + e] = (float)(uz + delta[H + k] * sp);
+  }
+}
+
 bool ok8(int ctot, int coff, int C) { return ctot % 8 == 0 && coff % 8 == 0 && C % 8 == 0 && C > 0 && coff + C <= ctot; }
 
 int launched(const char *what) {
@@ -678,6 +741,17 @@ int slbc_nn_plane_flux(float *u, float *drho, const unsigned char *solid, int D,
   if (launched("slbc_nn_plane_flux")) return 1;
   k_plane_apply<<<grid_for((long long)D * plane), 256, 0, st>>>(u, drho, solid, D, plane, gain, work);
   return launched("slbc_nn_plane_flux");
+}
+
+int slbc_nn_cross_flux(float *u, int D, int H, int W, double *work, void *stream) {
+  if (D < 1 || H < 1 || W < 1 || H + W > 65535 || !u || !work) return bad("slbc_nn_cross_flux: bad arguments");
+  const cudaStream_t st = (cudaStream_t)stream;
+  k_cross_sum<<<H + W, 256, 0, st>>>(u, D, H, W, work);
+  if (launched("slbc_nn_cross_flux")) return 1;
+  k_cross_fix<<<1, 32, 0, st>>>(H, W, work);
+  if (launched("slbc_nn_cross_flux")) return 1;
+  k_cross_apply<<<grid_for((long long)D * H * W), 256, 0, st>>>(u, D, H, W, work);
+  return launched("slbc_nn_cross_flux");
 }
 
 int slbc_nn_decode(const float *pred, int ctot_p, const unsigned char *solid, int D, int H, int W, float scale,

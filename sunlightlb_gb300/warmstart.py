@@ -67,6 +67,7 @@ class Kernels:
             "slbc_nn_encode": [p, i, i, i, i, p, i, i, p],
             "slbc_nn_decode": [p, i, p, i, i, i, f, f, p, f, p, p],
             "slbc_nn_plane_flux": [p, p, p, i, i, i, f, f, p, p],
+            "slbc_nn_cross_flux": [p, i, i, i, p, p],
             "slbc_tc_status": [],
         }
         self.dll = dll
@@ -557,7 +558,8 @@ def predict_velocity(net, solid_u8, force, eta, rho0=72.0, force_shift=1.0):
     return u
 
 
-def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_flux=True, info=None, gain=1.0):
+def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_flux=True, info=None, gain=1.0,
+                  cross_flux=False):
     """Velocity (3 x N) and density deviation (N) device FP32 fields from a
     network trained on labels with density (converged_flows(density=True)):
     with its own density a converged state is rebuilt exactly from
@@ -571,7 +573,9 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_f
     multiplies the state after the plane-flux step (plane_flux must be on
     for it; a global gain calibrated so that warm states start with the
     converged mean flow, 0.991 for the committed network, measured worse:
-    the fast transients of the first steps take flux with them)."""
+    the fast transients of the first steps take flux with them).
+    cross_flux: afterwards the y and z plane fluxes of u_y and u_z made
+    uniform too (slbc_nn_cross_flux)."""
     import torch
     net.encode(solid_u8.view(1, *solid_u8.shape))
     out = net.forward()
@@ -588,6 +592,9 @@ def predict_state(net, solid_u8, force, eta, rho0=72.0, force_shift=0.5, plane_f
                             float(gain), work.data_ptr(), net.stream)
         if info is not None:
             info["plane_flux_spread"] = float(work[3 * net.D])
+    if cross_flux:
+        work = torch.empty(3 * (net.H + net.W), device="cuda", dtype=torch.float64)
+        net.k.nn_cross_flux(u.data_ptr(), net.D, net.H, net.W, work.data_ptr(), net.stream)
     return u, drho
 
 

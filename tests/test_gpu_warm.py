@@ -269,6 +269,42 @@ def test_plane_flux_correction(gpu):
     assert np.abs(got_d - 0.75 * want_d).max() <= 1e-6 * np.abs(want_d).max()
 
 
+def test_cross_flux_correction(gpu):
+    """slbc_nn_cross_flux against float64 numpy: u_y gets (mean - Q_y[j]) /
+    M[j] |u| in y plane j (Q the plane flux, M the plane sum of |u|), u_z
+    the same over z planes; afterwards every y plane carries the mean y
+    flux and every z plane the mean z flux, u_x and the x plane fluxes are
+    unchanged, and solid nodes (u = 0) stay 0."""
+    torch = pytest.importorskip("torch")
+    from sunlightlb_gb300 import warmstart as WS
+    k = WS.Kernels(gpu.dll)
+    D, H, W = 10, 12, 14
+    rng = np.random.default_rng(8)
+    solid = rng.random((D, H, W)) < 0.3
+    u0 = (rng.random((3, D, H, W)) - 0.3) * ~solid * 1e-4
+    u0[1] += 2e-5 * np.sin(np.arange(H) / 2.0)[None, :, None] * ~solid
+    u0[2] += 3e-5 * np.cos(np.arange(W) / 3.0)[None, None, :] * ~solid
+    st = torch.cuda.current_stream().cuda_stream
+    u = torch.as_tensor(u0.astype(np.float32).ravel(), device="cuda")
+    work = torch.zeros(3 * (H + W), device="cuda", dtype=torch.float64)
+    k.nn_cross_flux(u.data_ptr(), D, H, W, work.data_ptr(), st)
+    torch.cuda.synchronize()
+    u32 = u0.astype(np.float32).astype(np.float64)
+    sp = np.sqrt((u32 ** 2).sum(axis=0))
+    qy, my = u32[1].sum(axis=(0, 2)), sp.sum(axis=(0, 2))
+    qz, mz = u32[2].sum(axis=(0, 1)), sp.sum(axis=(0, 1))
+    want = u32.copy()
+    want[1] += ((qy.mean() - qy) / my)[None, :, None] * sp
+    want[2] += ((qz.mean() - qz) / mz)[None, None, :] * sp
+    got = u.cpu().numpy().astype(np.float64).reshape(3, D, H, W)
+    assert np.abs(got - want).max() <= 1e-6 * np.abs(want).max()
+    assert np.array_equal(got[0], u32[0])
+    assert not got[:, solid].any()
+    scale = np.abs(u32).sum(axis=(1, 2, 3)).max() / D
+    assert np.abs(got[1].sum(axis=(0, 2)) - qy.mean()).max() <= 1e-5 * scale
+    assert np.abs(got[2].sum(axis=(0, 1)) - qz.mean()).max() <= 1e-5 * scale
+
+
 def test_gradient_clipping(gpu):
     """Device-side clipping against the running gradient norm: the first
     call sets the running norm, a 10x spike is scaled to 3x the running
